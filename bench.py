@@ -1,0 +1,346 @@
+"""Benchmark of the UJ step on the random-cloud workload (N = 2^20 particles,
+X ~ U[0,1]^3, Gamma ~ N(0, 1e-3), sigma ~ U[0.01, 0.03], Gaussian-erf kernel,
+FP32-comp form).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one all-pairs UJ evaluation (U and J of every particle from every
+particle: N^2 pair slots).  `value` times steps on device-resident inputs
+(vpm_uj_dev); `e2e` times the reference-facing drop-in (vpm_uj on the host
+46-row particle matrix, host<->device copies included).  One JSON line is
+printed by rank 0.  Under torchrun each rank evaluates its own field
+(independent replicas, weak scaling, no collective on the data path).
+
+--impl reference times the oracle port of the reference's CPU UJ_direct
+(oracle/, OpenMP over every host core) on a bounded sample of the same
+workload: the reference itself (Julia + FastMultipole.jl) cannot be installed
+here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "flowvpm.jl_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+N_PARTICLES = 1 << 20
+KERNEL = 2            # gaussianerf
+FLOP_PER_PAIR = 74    # VPM_FLOP_PER_UJ_PAIR
+METRIC = "UJ pair-interactions/s (random cloud N=2^20, Gaussian-erf, FP32-comp)"
+WORKLOAD = "random cloud UJ: N=2^20, X~U[0,1]^3, Gamma~N(0,1e-3), sigma~U[0.01,0.03], gaussianerf"
+
+
+def random_cloud(n, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.uniform(0.0, 1.0, (n, 3)), rng.normal(0.0, 1e-3, (n, 3)), rng.uniform(0.01, 0.03, n))
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- helpers
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(X, G, s, budget_s=12.0):
+    """The oracle (FP64 reference formula) on every host core, on a bounded
+    sample: all N sources against a prefix of the targets."""
+    import oracle
+    cores = os.cpu_count() or 1
+    nt = 64
+    t0 = time.perf_counter()
+    oracle.uj_pairs(X[:nt], X, G, s, KERNEL)
+    dt = time.perf_counter() - t0
+    rate0 = nt * X.shape[0] / dt
+    nt = int(min(X.shape[0], max(cores * 16, rate0 * budget_s / X.shape[0])))
+    nt -= nt % (cores * 16) or 0
+    nt = max(nt, cores * 16)
+    t0 = time.perf_counter()
+    oracle.uj_pairs(X[:nt], X, G, s, KERNEL)
+    dt = time.perf_counter() - t0
+    return {"value": nt * X.shape[0] / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
+            "sample": f"{nt} targets x {X.shape[0]} sources ({nt * X.shape[0]:.3e} pairs) in {dt:.1f} s; "
+                      "oracle/vpm_oracle.c oracle_uj_pairs, FP64 reference formula, OpenMP"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port of UJ_direct on the host cores."""
+    if rank != 0:
+        return
+    X, G, s = random_cloud(N_PARTICLES, seed=0)
+    import oracle
+    cores = os.cpu_count() or 1
+    # bounded sample per step: all sources against `nt` targets (~5 s of CPU work)
+    nt = cores * 32
+    for _ in range(max(0, args.warmup)):
+        oracle.uj_pairs(X[:cores * 4], X, G, s, KERNEL)
+    times = []
+    for k in range(args.steps):
+        sl = slice((k * nt) % (N_PARTICLES - nt), (k * nt) % (N_PARTICLES - nt) + nt)
+        t0 = time.perf_counter()
+        oracle.uj_pairs(X[sl], X, G, s, KERNEL)
+        times.append(time.perf_counter() - t0)
+    pairs = nt * N_PARTICLES
+    value = pairs * len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_per_step": f"{nt} targets x {N_PARTICLES} sources"},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                             "sample": f"{nt} targets x {N_PARTICLES} sources per step, {args.steps} steps"},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "oracle port (oracle/vpm_oracle.c) of UJ_direct's pair loop: the reference (Julia + "
+                    "FastMultipole.jl) cannot be installed in this environment"}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world):
+    import torch
+    import vpm_gb300 as vpm
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    ctx = vpm.Context(dev)
+    n = N_PARTICLES
+    X, G, s = random_cloud(n, seed=1000 * rank)
+    d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
+    xt, gs, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    flush = torch.empty(64 << 20, device="cuda", dtype=torch.float32)   # 256 MB > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    def step():
+        U.zero_()
+        J.zero_()
+        ctx.uj_dev(xt, xt, gs, sg, U, J, KERNEL, vpm.FP32COMP)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    launches0 = ctx.launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(dev) as clk:
+        barrier()
+        t_start = time.perf_counter()
+        total = torch.cuda.Event(enable_timing=True)
+        total_end = torch.cuda.Event(enable_timing=True)
+        total.record(stream)
+        for k in range(args.steps):
+            flush.fill_(float(k))            # L2 flush between timed steps
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        total_end.record(stream)
+        barrier()
+        wall = time.perf_counter() - t_start
+    launches = ctx.launches - launches0
+    elapsed_ms = total.elapsed_time(total_end)
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    pairs_per_step = float(n) * n
+    value = world * pairs_per_step * args.steps / (elapsed_ms / 1e3)
+    # dominant kernel: the UJ launch (pack is O(N), microseconds); flops per launch / avg duration
+    avg_kernel_s = statistics.mean(kernel_ms) / 1e3
+    achieved_tflops = FLOP_PER_PAIR * pairs_per_step / avg_kernel_s / 1e12
+
+    # FP32 FFMA peak of this GPU, measured now (the driver's peaks file has HBM and bf16 only)
+    ffma = vpm.Context(dev)
+    peak_tflops = measure_ffma_peak(ffma)
+
+    # ---- end to end through the reference-facing call (host 46-row matrix)
+    P = np.zeros((46, n), order="F")
+    P[0:3] = X.T
+    P[3:6] = G.T
+    P[6] = s
+    ctx.set_stream(None)
+    ctx.uj(P, n, KERNEL, vpm.FP32COMP, vpm._lib.RESET)   # warm (allocations)
+    e2e_times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        ctx.uj(P, n, KERNEL, vpm.FP32COMP, vpm._lib.RESET)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = world * pairs_per_step / statistics.mean(e2e_times)
+
+    out = None
+    if rank == 0:
+        # accuracy of this very run against the oracle on a seeded subset of targets
+        import oracle
+        sub = np.sort(np.random.default_rng(5).choice(n, 256, replace=False))
+        Ur, Jr = oracle.uj_pairs(X[sub], X, G, s, KERNEL)
+        Uh, Jh = U.cpu().numpy()[sub], J.cpu().numpy()[sub]
+        err = {"U_max_rel": float(np.abs(Uh - Ur).max() / np.abs(Ur).max()),
+               "J_max_rel": float(np.abs(Jh - Jr).max() / np.abs(Jr).max()),
+               "U_rms_rel": float(np.linalg.norm(Uh - Ur) / np.linalg.norm(Ur)),
+               "J_rms_rel": float(np.linalg.norm(Jh - Jr) / np.linalg.norm(Jr)),
+               "targets_checked": 256}
+        fp64 = fp64_rate(ctx, vpm, torch)
+        base = cpu_baseline(X, G, s)
+        mp = measured_peaks()
+        out = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 positions/accumulation)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_particles": n, "kernel": "gaussianerf",
+                       "precision": "fp32comp", "pairs_per_step": pairs_per_step,
+                       "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": 46 * 8 * n,
+                    "d2h_bytes_per_step": 18 * 8 * n, "ms_per_step": 1e3 * statistics.mean(e2e_times),
+                    "call": "vpm_uj(ctx, host 46xN matrix, RESET) = UJ_gb300_mixed(pfield)"},
+            "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops,
+                         "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops, "traffic": None,
+                         "kernel": "uj_mixed_kernel<gaussianerf>",
+                         "flop_per_pair": FLOP_PER_PAIR,
+                         "peak_source": "FFMA-loop kernel measured in this run (no FP32 figure in "
+                                        "MEASURED_PEAKS.json)",
+                         "peak_nominal_2070MHz": 152 * 128 * 2 * 2.07e9 / 1e12,
+                         "hbm_peak_gbs_measured": mp.get("hbm_gbs")},
+            "cpu_baseline": base,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "fp64_gpu": fp64,
+            "mixed_over_fp64": value / fp64["value"] if fp64 else None,
+            "error_vs_oracle": err,
+            "wall_s_timed_region": wall,
+        }
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+def fp64_rate(ctx, vpm, torch):
+    """Plain FP64 GPU form on a 2^17 cloud (one timed evaluation)."""
+    n = 1 << 17
+    X, G, s = random_cloud(n, seed=77)
+    d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
+    xt, gs, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    ctx.uj_dev(xt[:4096], xt[:4096], gs[:4096], sg[:4096], U[:4096], J[:4096], KERNEL, vpm.FP64)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    ctx.uj_dev(xt, xt, gs, sg, U, J, KERNEL, vpm.FP64)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    return {"value": float(n) * n / (ms / 1e3), "unit": "pairs/s", "n_particles": n, "ms": ms,
+            "kernel": "uj_f64_kernel<gaussianerf>"}
+
+
+def measure_ffma_peak(ctx) -> float:
+    """TFLOP/s of a pure FFMA loop (vpm_probe_ffma in the library)."""
+    import vpm_gb300._lib as L
+    out = np.zeros(1)
+    rc = ctx._L.vpm_probe_ffma(ctx._h, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(ctx._L.vpm_last_error(ctx._h).decode())
+    return float(out[0])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

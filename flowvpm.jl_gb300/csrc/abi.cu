@@ -1,0 +1,542 @@
+// abi.cu -- the C ABI of libvpm_gb300.so (include/vpm_gb300.h): contexts,
+// argument checking, host<->device staging of the reference's 46-row particle
+// matrix, and dispatch to the UJ / Estr launchers.
+#include "../../include/vpm_gb300.h"
+#include "internal.h"
+#include "vpm_math.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+
+using namespace vpm;
+
+namespace {
+
+// 0-based rows of the particle column, src/FLOWVPM_particlefield.jl:239-252
+enum : int { R_X = 0, R_G = 3, R_SIG = 6, R_U = 9, R_W = 12, R_J = 15, R_PSE = 24, R_SFS = 39, R_STATIC = 42 };
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t grow(size_t bytes)
+    {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes + bytes / 8;  // grow with some headroom, never shrink
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct vpm_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    double timeout_s = 3600.0;
+    std::mutex mu;
+    std::string err;
+    bool broken = false;
+    int64_t launches = 0;
+    // device copies of host matrices and SoA views of them
+    DevBuf mat, mat2, x, g, s, st, xt;
+    // packing and split-K scratch
+    DevBuf src_pack, tgt_pack, partial, flag;
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int fail(vpm_ctx* c, int code, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
+int fail(vpm_ctx* c, int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_create_error = buf;
+    return code;
+}
+
+int cuda_fail(vpm_ctx* c, cudaError_t e, const char* what)
+{
+    // A sticky error (e.g. an illegal address) poisons the context for good.
+    cudaError_t last = cudaGetLastError();
+    (void)last;
+    if (e == cudaErrorIllegalAddress || e == cudaErrorLaunchFailure || e == cudaErrorIllegalInstruction ||
+        e == cudaErrorMisalignedAddress || e == cudaErrorHardwareStackError)
+        c->broken = true;
+    return fail(c, VPM_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)
+
+// Wait for the context stream with a bound; the host never blocks forever.
+int bounded_wait(vpm_ctx* c)
+{
+    CK(cudaEventRecord(c->done, c->stream), "cudaEventRecord");
+    auto t0 = std::chrono::steady_clock::now();
+    int sleep_us = 2;
+    for (;;) {
+        cudaError_t q = cudaEventQuery(c->done);
+        if (q == cudaSuccess) return VPM_OK;
+        if (q != cudaErrorNotReady) return cuda_fail(c, q, "device work");
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > c->timeout_s) {
+            c->broken = true;
+            return fail(c, VPM_ERR_TIMEOUT, "device work did not finish within %.1f s", c->timeout_s);
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(sleep_us));
+        if (sleep_us < 1000) sleep_us *= 2;
+    }
+}
+
+bool is_device_ptr(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// ------------------------------------------------------------ matrix kernels
+// Gather X, Gamma, sigma, static of the 46-row columns into SoA arrays and apply
+// _reset_particles / _reset_particles_sfs (src/FLOWVPM_particlefield.jl:464-507).
+__global__ void unpack_matrix(int64_t np, double* __restrict__ mat, int flags, double* __restrict__ x,
+                              double* __restrict__ g, double* __restrict__ s, uint8_t* __restrict__ st)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    double* p = mat + (int64_t)VPM_NFIELDS * i;
+    for (int k = 0; k < 3; k++) { x[3 * i + k] = p[R_X + k]; g[3 * i + k] = p[R_G + k]; }
+    s[i] = p[R_SIG];
+    const bool is_static = p[R_STATIC] != 0.0;
+    st[i] = is_static ? 1 : 0;
+    if (!is_static) {
+        if (flags & VPM_RESET)
+            for (int k = R_U; k < R_PSE + 3; k++) p[k] = 0.0;
+        if (flags & VPM_RESET_SFS)
+            for (int k = R_SFS; k < R_SFS + 3; k++) p[k] = 0.0;
+    }
+}
+
+__global__ void positions_of_matrix(int64_t np, const double* __restrict__ mat, double* __restrict__ x)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    for (int k = 0; k < 3; k++) x[3 * i + k] = mat[(int64_t)VPM_NFIELDS * i + R_X + k];
+}
+
+// Sets *flag if any of rows [r0, r1) of the first np columns is not finite.
+__global__ void check_rows_finite(int64_t np, const double* __restrict__ mat, int r0, int r1, int* flag)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const double* p = mat + (int64_t)VPM_NFIELDS * i;
+    for (int k = r0; k < r1; k++)
+        if (!isfinite(p[k])) { atomicOr(flag, 1); return; }
+}
+
+// FP32 pipe probe: 8 independent FFMA chains per thread, 16x unrolled.
+__global__ void ffma_probe_kernel(float* out, int iters, float a, float b)
+{
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = threadIdx.x * 1e-3f + k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) x[k] = fmaf(x[k], a, b);
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    if (s == 1234.5678f) out[0] = s;  // keeps the chains live; never true in practice
+}
+
+constexpr int EB = 256;  // threads per block of the O(N) helper kernels
+inline unsigned nblk(int64_t n) { return (unsigned)((n + EB - 1) / EB); }
+
+int check_kernel(vpm_ctx* c, int kernel, int precision)
+{
+    if (kernel < VPM_KERNEL_SINGULAR || kernel > VPM_KERNEL_WINCKELMANS)
+        return fail(c, VPM_ERR_ARG, "unknown kernel id %d (expected 0..3: singular, gaussian, gaussianerf, winckelmans)", kernel);
+    if (precision != VPM_FP64 && precision != VPM_FP32COMP)
+        return fail(c, VPM_ERR_ARG, "unknown precision %d (expected 0 = FP64, 1 = FP32-comp)", precision);
+    return VPM_OK;
+}
+
+// Grow the packing / scratch buffers for a UJ and (optionally) an Estr pass.
+int ensure_work(vpm_ctx* c, int64_t nt, int64_t ns, int precision, bool estr, Workspace* w)
+{
+    size_t sp = uj_src_pack_bytes(ns, precision);
+    if (estr) { size_t e = estr_src_pack_bytes(ns, precision); if (e > sp) sp = e; }
+    size_t tp = precision ? estr_src_pack_bytes(nt, 1) : 0;  // >= the UJ target pack
+    const int nsplit = uj_num_splits(nt, ns, c->num_sms);
+    const size_t pb = uj_partial_bytes(nt, nsplit);
+    if (c->src_pack.grow(sp) != cudaSuccess || (tp && c->tgt_pack.grow(tp) != cudaSuccess) ||
+        (pb && c->partial.grow(pb) != cudaSuccess)) {
+        cudaGetLastError();
+        return fail(c, VPM_ERR_CAPACITY, "could not allocate %zu B of packing/scratch memory", sp + tp + pb);
+    }
+    w->src_pack = c->src_pack.p; w->src_pack_bytes = c->src_pack.cap;
+    w->tgt_pack = c->tgt_pack.p; w->tgt_pack_bytes = c->tgt_pack.cap;
+    w->partial = (double*)c->partial.p; w->partial_bytes = c->partial.cap;
+    return VPM_OK;
+}
+
+int grow(vpm_ctx* c, DevBuf& b, size_t bytes, const char* what)
+{
+    if (b.grow(bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, VPM_ERR_CAPACITY, "could not allocate %zu B for %s", bytes, what);
+    }
+    return VPM_OK;
+}
+
+#define RC(call)                   \
+    do {                           \
+        int rc_ = (call);          \
+        if (rc_ != VPM_OK) return rc_; \
+    } while (0)
+
+int enter(vpm_ctx* c)
+{
+    if (c->broken) return fail(c, VPM_ERR_STATE, "context is unusable after an earlier device error: %s", c->err.c_str());
+    c->err.clear();
+    return VPM_OK;
+}
+
+}  // namespace
+
+// =================================================================== ABI
+extern "C" {
+
+int vpm_abi_version(void) { return VPM_ABI_VERSION; }
+
+const char* vpm_build_info(void)
+{
+    return "libvpm_gb300 abi " "1" " sm_103a; UJ fp64 + fp32comp, Estr fp64 + fp32comp";
+}
+
+int vpm_ctx_create(vpm_ctx** out, int device)
+{
+    if (!out) return fail(nullptr, VPM_ERR_ARG, "vpm_ctx_create: out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(nullptr, VPM_ERR_NODEVICE, "no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n) return fail(nullptr, VPM_ERR_ARG, "device %d out of range (0..%d)", device, n - 1);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+        return fail(nullptr, VPM_ERR_NODEVICE, "cudaGetDeviceProperties failed");
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(nullptr, VPM_ERR_NODEVICE, "device %d is sm_%d%d; this library is built for sm_103a only",
+                    device, prop.major, prop.minor);
+    DeviceGuard dg(device);
+    vpm_ctx* c = new vpm_ctx();
+    c->device = device;
+    c->num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return fail(nullptr, VPM_ERR_CUDA, "could not create a stream/event on device %d", device);
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return VPM_OK;
+}
+
+int vpm_ctx_destroy(vpm_ctx* c)
+{
+    if (!c) return VPM_OK;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        DeviceGuard dg(c->device);
+        if (!c->broken) cudaStreamSynchronize(c->stream);
+        for (DevBuf* b : {&c->mat, &c->mat2, &c->x, &c->g, &c->s, &c->st, &c->xt, &c->src_pack, &c->tgt_pack,
+                          &c->partial, &c->flag})
+            b->release();
+        if (c->done) cudaEventDestroy(c->done);
+        if (c->own_stream) cudaStreamDestroy(c->own_stream);
+        cudaGetLastError();
+    }
+    delete c;
+    return VPM_OK;
+}
+
+const char* vpm_last_error(const vpm_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+int vpm_ctx_set_stream(vpm_ctx* c, void* stream)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_ctx_set_stream: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return VPM_OK;
+}
+
+int vpm_ctx_set_timeout(vpm_ctx* c, double seconds)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_ctx_set_timeout: ctx is NULL");
+    if (!(seconds > 0)) return fail(c, VPM_ERR_ARG, "timeout must be > 0 s");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->timeout_s = seconds;
+    return VPM_OK;
+}
+
+int64_t vpm_launch_count(const vpm_ctx* c) { return c ? c->launches : 0; }
+
+int vpm_probe_ffma(vpm_ctx* c, double* tflops)
+{
+    if (!c || !tflops) return fail(c, VPM_ERR_ARG, "vpm_probe_ffma: NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    DeviceGuard dg(c->device);
+    RC(grow(c, c->flag, sizeof(int), "flag"));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "cudaEventCreate");
+    CK(cudaEventCreate(&e1), "cudaEventCreate");
+    const int blocks = c->num_sms * 8, threads = 256, iters = 4096;
+    double best = 0.0;
+    for (int rep = 0; rep < 4; rep++) {
+        CK(cudaEventRecord(e0, c->stream), "cudaEventRecord");
+        ffma_probe_kernel<<<blocks, threads, 0, c->stream>>>((float*)c->flag.p, iters, 0.9999999f, 1e-7f);
+        CK(cudaEventRecord(e1, c->stream), "cudaEventRecord");
+        c->launches++;
+        RC(bounded_wait(c));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        const double flops = 2.0 * 16 * 8 * (double)iters * blocks * threads;
+        if (rep > 0 && ms > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return VPM_OK;
+}
+
+// ------------------------------------------------------------- UJ_direct drop-in
+int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, int precision, int flags)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (!particles && np > 0) return fail(c, VPM_ERR_ARG, "vpm_uj: particles is NULL");
+    if (ld != VPM_NFIELDS) return fail(c, VPM_ERR_ARG, "vpm_uj: ld must be %d (got %lld)", VPM_NFIELDS, (long long)ld);
+    if (np < 0 || np > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj: np=%lld out of range", (long long)np);
+    if (flags & ~(VPM_RESET | VPM_RESET_SFS | VPM_SFS | VPM_TRANSPOSED | VPM_CHECK_FINITE))
+        return fail(c, VPM_ERR_ARG, "vpm_uj: unknown flag bits 0x%x", flags);
+    RC(check_kernel(c, kernel, precision));
+    if (np == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    cudaStream_t st = c->stream;
+    const size_t mat_bytes = (size_t)VPM_NFIELDS * np * sizeof(double);
+    RC(grow(c, c->mat, mat_bytes, "particle matrix"));
+    RC(grow(c, c->x, 3 * np * sizeof(double), "positions"));
+    RC(grow(c, c->g, 3 * np * sizeof(double), "strengths"));
+    RC(grow(c, c->s, np * sizeof(double), "core sizes"));
+    RC(grow(c, c->st, np, "static flags"));
+    RC(grow(c, c->flag, sizeof(int), "flag"));
+    Workspace w;
+    const bool sfs = (flags & VPM_SFS) != 0;
+    RC(ensure_work(c, np, np, precision, sfs, &w));
+    double* mat = (double*)c->mat.p;
+    double* x = (double*)c->x.p;
+    double* g = (double*)c->g.p;
+    double* s = (double*)c->s.p;
+    uint8_t* stf = (uint8_t*)c->st.p;
+
+    CK(cudaMemcpyAsync(mat, particles, mat_bytes, cudaMemcpyHostToDevice, st), "H2D particle matrix");
+    unpack_matrix<<<nblk(np), EB, 0, st>>>(np, mat, flags, x, g, s, stf);
+    c->launches++;
+    CK(cudaGetLastError(), "unpack_matrix");
+
+    UJArgs a;
+    a.nt = np; a.ns = np; a.xt = x; a.xs = x; a.gs = g; a.sgs = s;
+    a.U = mat + R_U; a.ldU = VPM_NFIELDS; a.J = mat + R_J; a.ldJ = VPM_NFIELDS;
+    a.kernel = kernel; a.precision = precision; a.self = true;
+    CK(launch_uj(a, w, c->num_sms, st, &c->launches), "UJ kernels");
+    if (sfs) {
+        EstrArgs e;
+        e.nt = np; e.ns = np;
+        e.xt = x; e.Jt = mat + R_J; e.ldJt = VPM_NFIELDS; e.static_t = stf;
+        e.xs = x; e.gs = g; e.sgs = s; e.Js = mat + R_J; e.ldJs = VPM_NFIELDS; e.static_s = stf;
+        e.SFS = mat + R_SFS; e.ldS = VPM_NFIELDS;
+        e.kernel = kernel; e.precision = precision;
+        e.transposed = (flags & VPM_TRANSPOSED) != 0; e.self = true;
+        CK(launch_estr(e, w, c->num_sms, st, &c->launches), "Estr kernels");
+    }
+    int* dflag = (int*)c->flag.p;
+    if (flags & VPM_CHECK_FINITE) {
+        CK(cudaMemsetAsync(dflag, 0, sizeof(int), st), "memset flag");
+        check_rows_finite<<<nblk(np), EB, 0, st>>>(np, mat, R_U, R_PSE + 3, dflag);
+        c->launches++;
+        if (sfs) { check_rows_finite<<<nblk(np), EB, 0, st>>>(np, mat, R_SFS, R_SFS + 3, dflag); c->launches++; }
+        CK(cudaGetLastError(), "check_rows_finite");
+    }
+    RC(bounded_wait(c));
+    // rows 10:27 (U, vorticity, J, PSE) and, when touched, rows 40:42 (SFS)
+    const size_t pitch = VPM_NFIELDS * sizeof(double);
+    CK(cudaMemcpy2DAsync(particles + R_U, pitch, mat + R_U, pitch, 18 * sizeof(double), (size_t)np,
+                         cudaMemcpyDeviceToHost, st), "D2H rows 10:27");
+    if (flags & (VPM_SFS | VPM_RESET_SFS))
+        CK(cudaMemcpy2DAsync(particles + R_SFS, pitch, mat + R_SFS, pitch, 3 * sizeof(double), (size_t)np,
+                             cudaMemcpyDeviceToHost, st), "D2H rows 40:42");
+    int hflag = 0;
+    if (flags & VPM_CHECK_FINITE)
+        CK(cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H flag");
+    CK(cudaStreamSynchronize(st), "D2H");
+    if (hflag) return fail(c, VPM_ERR_NONFINITE, "vpm_uj: NaN or Inf in the computed U/J/SFS");
+    return VPM_OK;
+}
+
+int vpm_uj_cross(vpm_ctx* c, const double* src, int64_t ld_src, int64_t ns, double* tgt, int64_t ld_tgt,
+                 int64_t nt, int kernel, int precision)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_cross: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if ((!src && ns > 0) || (!tgt && nt > 0)) return fail(c, VPM_ERR_ARG, "vpm_uj_cross: NULL matrix");
+    if (ld_src != VPM_NFIELDS || ld_tgt != VPM_NFIELDS)
+        return fail(c, VPM_ERR_ARG, "vpm_uj_cross: ld must be %d", VPM_NFIELDS);
+    if (ns < 0 || nt < 0 || ns > (int64_t)1 << 31 || nt > (int64_t)1 << 31)
+        return fail(c, VPM_ERR_ARG, "vpm_uj_cross: sizes out of range");
+    RC(check_kernel(c, kernel, precision));
+    if (ns == 0 || nt == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    cudaStream_t st = c->stream;
+    RC(grow(c, c->mat, (size_t)VPM_NFIELDS * ns * sizeof(double), "source matrix"));
+    RC(grow(c, c->mat2, (size_t)VPM_NFIELDS * nt * sizeof(double), "target matrix"));
+    RC(grow(c, c->x, 3 * ns * sizeof(double), "positions"));
+    RC(grow(c, c->g, 3 * ns * sizeof(double), "strengths"));
+    RC(grow(c, c->s, ns * sizeof(double), "core sizes"));
+    RC(grow(c, c->st, ns, "static flags"));
+    RC(grow(c, c->xt, 3 * nt * sizeof(double), "target positions"));
+    Workspace w;
+    RC(ensure_work(c, nt, ns, precision, false, &w));
+    double* ms = (double*)c->mat.p;
+    double* mt = (double*)c->mat2.p;
+    CK(cudaMemcpyAsync(ms, src, (size_t)VPM_NFIELDS * ns * sizeof(double), cudaMemcpyHostToDevice, st), "H2D src");
+    CK(cudaMemcpyAsync(mt, tgt, (size_t)VPM_NFIELDS * nt * sizeof(double), cudaMemcpyHostToDevice, st), "H2D tgt");
+    unpack_matrix<<<nblk(ns), EB, 0, st>>>(ns, ms, 0, (double*)c->x.p, (double*)c->g.p, (double*)c->s.p,
+                                           (uint8_t*)c->st.p);
+    positions_of_matrix<<<nblk(nt), EB, 0, st>>>(nt, mt, (double*)c->xt.p);
+    c->launches += 2;
+    CK(cudaGetLastError(), "unpack");
+    UJArgs a;
+    a.nt = nt; a.ns = ns; a.xt = (double*)c->xt.p; a.xs = (double*)c->x.p; a.gs = (double*)c->g.p;
+    a.sgs = (double*)c->s.p; a.U = mt + R_U; a.ldU = VPM_NFIELDS; a.J = mt + R_J; a.ldJ = VPM_NFIELDS;
+    a.kernel = kernel; a.precision = precision; a.self = false;
+    CK(launch_uj(a, w, c->num_sms, st, &c->launches), "UJ kernels");
+    RC(bounded_wait(c));
+    const size_t pitch = VPM_NFIELDS * sizeof(double);
+    CK(cudaMemcpy2DAsync(tgt + R_U, pitch, mt + R_U, pitch, 15 * sizeof(double), (size_t)nt,
+                         cudaMemcpyDeviceToHost, st), "D2H rows 10:24");
+    CK(cudaStreamSynchronize(st), "D2H");
+    return VPM_OK;
+}
+
+// --------------------------------------------------------- device-pointer API
+int vpm_uj_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const double* xs, const double* gs,
+               const double* sgs, double* U, double* J, int kernel, int precision)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_dev: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+        return fail(c, VPM_ERR_ARG, "vpm_uj_dev: sizes out of range");
+    RC(check_kernel(c, kernel, precision));
+    if (nt == 0 || ns == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(xt) || !is_device_ptr(xs) || !is_device_ptr(gs) || !is_device_ptr(sgs) ||
+        !is_device_ptr(U) || !is_device_ptr(J))
+        return fail(c, VPM_ERR_ARG, "vpm_uj_dev: every array must be a device pointer");
+    Workspace w;
+    const bool self = (xt == xs) && (nt == ns);
+    RC(ensure_work(c, nt, ns, precision, false, &w));
+    UJArgs a;
+    a.nt = nt; a.ns = ns; a.xt = xt; a.xs = xs; a.gs = gs; a.sgs = sgs;
+    a.U = U; a.ldU = 3; a.J = J; a.ldJ = 9; a.kernel = kernel; a.precision = precision; a.self = self;
+    CK(launch_uj(a, w, c->num_sms, c->stream, &c->launches), "UJ kernels");
+    return bounded_wait(c);
+}
+
+int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, const uint8_t* static_t, int64_t ns,
+                 const double* xs, const double* gs, const double* sgs, const double* Js, const uint8_t* static_s,
+                 double* SFS, int kernel, int precision, int flags)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_estr_dev: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+        return fail(c, VPM_ERR_ARG, "vpm_estr_dev: sizes out of range");
+    if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "vpm_estr_dev: only VPM_TRANSPOSED is accepted in flags");
+    RC(check_kernel(c, kernel, precision));
+    if (nt == 0 || ns == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(xt) || !is_device_ptr(Jt) || !is_device_ptr(xs) || !is_device_ptr(gs) ||
+        !is_device_ptr(sgs) || !is_device_ptr(Js) || !is_device_ptr(SFS) ||
+        (static_t && !is_device_ptr(static_t)) || (static_s && !is_device_ptr(static_s)))
+        return fail(c, VPM_ERR_ARG, "vpm_estr_dev: every array must be a device pointer");
+    Workspace w;
+    RC(ensure_work(c, nt, ns, precision, true, &w));
+    EstrArgs e;
+    e.nt = nt; e.ns = ns; e.xt = xt; e.Jt = Jt; e.ldJt = 9; e.static_t = static_t;
+    e.xs = xs; e.gs = gs; e.sgs = sgs; e.Js = Js; e.ldJs = 9; e.static_s = static_s;
+    e.SFS = SFS; e.ldS = 3; e.kernel = kernel; e.precision = precision;
+    e.transposed = (flags & VPM_TRANSPOSED) != 0;
+    e.self = (xt == xs) && (nt == ns);
+    CK(launch_estr(e, w, c->num_sms, c->stream, &c->launches), "Estr kernels");
+    return bounded_wait(c);
+}
+
+}  // extern "C"

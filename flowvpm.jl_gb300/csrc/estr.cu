@@ -1,0 +1,303 @@
+// estr.cu -- SFS vortex-stretching pass Estr (src/FLOWVPM_subfilterscale_models.jl:16-92).
+//
+// The reference adds, for every non-static target t and non-static source s,
+//     SFS_t += zeta(r/sigma_s)/sigma_s^3 * (J_t - J_s)^T Gamma_s      (transposed)
+// This is evaluated in the exactly equivalent factored form
+//     SFS_t += J_t^T Zg_t - Zv_t,   Zg_t = sum_s z_ts Gamma_s,  Zv_t = sum_s z_ts v_s,
+// with z_ts = zeta(r/sigma_s)/sigma_s^3 and v_s = J_s^T Gamma_s (J_s Gamma_s for
+// the classic scheme), so a source carries 10 numbers instead of 16 and a pair
+// costs about 25 flop.  The self pair, which the reference includes but which
+// contributes exactly zero there, is excluded by index (in the factored form
+// its two terms would only cancel to rounding).  Static sources are packed with
+// zero strength; static targets are left untouched.  The FP64 kernel keeps the
+// reference's zeta formula; the mixed kernel uses FP32 pair math with a
+// double-float displacement and FP64 accumulation of FP32 blocks.
+#include "internal.h"
+#include "vpm_math.cuh"
+
+namespace vpm {
+
+static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+size_t estr_src_pack_bytes(int64_t ns, int precision)
+{
+    const int64_t n = round_up(ns, UJ_TILE);
+    return (size_t)n * (precision ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64));
+}
+
+// v = J^T Gamma (transposed) or J Gamma (classic); J column-major 3x3.
+__device__ __forceinline__ void stretch_vec(const double* J, double gx, double gy, double gz,
+                                            bool transposed, double& vx, double& vy, double& vz)
+{
+    if (transposed) {
+        vx = J[0] * gx + J[1] * gy + J[2] * gz;
+        vy = J[3] * gx + J[4] * gy + J[5] * gz;
+        vz = J[6] * gx + J[7] * gy + J[8] * gz;
+    } else {
+        vx = J[0] * gx + J[3] * gy + J[6] * gz;
+        vy = J[1] * gx + J[4] * gy + J[7] * gz;
+        vz = J[2] * gx + J[5] * gy + J[8] * gz;
+    }
+}
+
+template <int K>
+__global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __restrict__ xs,
+                                const double* __restrict__ gs, const double* __restrict__ sgs,
+                                const double* __restrict__ Js, int64_t ldJs,
+                                const uint8_t* __restrict__ static_s, bool transposed,
+                                SrcEstrMixed* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= ns_pad) return;
+    SrcEstrMixed p;
+    if (i < ns) {
+        const double x = xs[3 * i], y = xs[3 * i + 1], z = xs[3 * i + 2];
+        const float xh = (float)x, yh = (float)y, zh = (float)z;
+        const double isig = 1.0 / sgs[i];
+        const double isig2 = isig * isig;
+        p.a = make_float4(xh, yh, zh, (float)isig2);
+        p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
+        const bool off = static_s && static_s[i];
+        const double k = off ? 0.0 : zeta_norm(K) * isig2 * isig;
+        const double gx = gs[3 * i], gy = gs[3 * i + 1], gz = gs[3 * i + 2];
+        double vx, vy, vz;
+        stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
+        p.c = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), (float)(k * vx));
+        p.d = make_float4((float)(k * vy), (float)(k * vz), 0.f, 0.f);
+    } else {
+        p.a = make_float4(0.f, 0.f, 0.f, 1.f);
+        p.b = p.c = p.d = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    out[i] = p;
+}
+
+// Target positions of the mixed Estr kernel (only fields a and b are read).
+__global__ void pack_estr_tgt(int64_t nt, const double* __restrict__ xt, SrcEstrMixed* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const double x = xt[3 * i], y = xt[3 * i + 1], z = xt[3 * i + 2];
+    const float xh = (float)x, yh = (float)y, zh = (float)z;
+    SrcEstrMixed p;
+    p.a = make_float4(xh, yh, zh, 0.f);
+    p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
+    p.c = p.d = make_float4(0.f, 0.f, 0.f, 0.f);
+    out[i] = p;
+}
+
+template <int K>
+__global__ void pack_estr_f64(int64_t ns, int64_t ns_pad, const double* __restrict__ xs,
+                              const double* __restrict__ gs, const double* __restrict__ sgs,
+                              const double* __restrict__ Js, int64_t ldJs,
+                              const uint8_t* __restrict__ static_s, bool transposed,
+                              SrcEstrF64* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= ns_pad) return;
+    SrcEstrF64 p;
+    if (i < ns) {
+        const bool off = static_s && static_s[i];
+        const double gx = off ? 0.0 : gs[3 * i], gy = off ? 0.0 : gs[3 * i + 1], gz = off ? 0.0 : gs[3 * i + 2];
+        double vx, vy, vz;
+        stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
+        p.xy = make_double2(xs[3 * i], xs[3 * i + 1]);
+        p.z_isig = make_double2(xs[3 * i + 2], 1.0 / sgs[i]);
+        p.gxy = make_double2(gx, gy);
+        p.gz_vx = make_double2(gz, vx);
+        p.vyz = make_double2(vy, vz);
+    } else {
+        p.xy = make_double2(0.0, 0.0);
+        p.z_isig = make_double2(0.0, 1.0);
+        p.gxy = p.gz_vx = p.vyz = make_double2(0.0, 0.0);
+    }
+    out[i] = p;
+}
+
+// SFS_t += J_t^T Zg - Zv  (or J_t Zg - Zv), FP64.
+__device__ __forceinline__ void estr_combine(const double* Jt, const double (&zg)[3], const double (&zv)[3],
+                                             bool transposed, double (&out)[3])
+{
+    double sx, sy, sz;
+    stretch_vec(Jt, zg[0], zg[1], zg[2], transposed, sx, sy, sz);
+    out[0] = sx - zv[0];
+    out[1] = sy - zv[1];
+    out[2] = sz - zv[2];
+}
+
+__device__ __forceinline__ void write_estr(int64_t t, const double (&o)[3], double* SFS, int64_t ldS,
+                                           double* partial, int64_t nt_pad)
+{
+    if (partial) {
+        double* p = partial + (int64_t)blockIdx.y * 3 * nt_pad + t;
+        p[0] = o[0]; p[nt_pad] = o[1]; p[2 * nt_pad] = o[2];
+    } else {
+        SFS[t * ldS] += o[0]; SFS[t * ldS + 1] += o[1]; SFS[t * ldS + 2] += o[2];
+    }
+}
+
+__global__ void estr_reduce(int64_t nt, int nsplit, const double* __restrict__ partial, int64_t nt_pad,
+                            const uint8_t* __restrict__ static_t, double* SFS, int64_t ldS)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt || (static_t && static_t[t])) return;
+    for (int k = 0; k < 3; k++) {
+        double s = 0.0;
+        for (int sp = 0; sp < nsplit; sp++) s += partial[((int64_t)sp * 3 + k) * nt_pad + t];
+        SFS[t * ldS + k] += s;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(UJ_THREADS)
+estr_f64_kernel(int64_t nt, const double* __restrict__ xt, const double* __restrict__ Jt, int64_t ldJt,
+                const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrF64* __restrict__ src,
+                int64_t per_split, bool self, bool transposed, double* SFS, int64_t ldS,
+                double* partial, int64_t nt_pad)
+{
+    __shared__ SrcEstrF64 tile[UJ_TILE];
+    const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
+    const bool valid = t < nt && !(static_t && static_t[t]);
+    const double tx = t < nt ? xt[3 * t] : 1.0e3;
+    const double ty = t < nt ? xt[3 * t + 1] : 1.0e3;
+    const double tz = t < nt ? xt[3 * t + 2] : 1.0e3;
+    double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
+    const int64_t s0 = (int64_t)blockIdx.y * per_split;
+    const int64_t s1 = min(s0 + per_split, ns_pad);
+    for (int64_t base = s0; base < s1; base += UJ_TILE) {
+        __syncthreads();
+        tile[threadIdx.x] = src[base + threadIdx.x];
+        __syncthreads();
+#pragma unroll 2
+        for (int j = 0; j < UJ_TILE; j++) {
+            const SrcEstrF64& p = tile[j];
+            if (self && base + j == t) continue;
+            const double dx = p.xy.x - tx, dy = p.xy.y - ty, dz = p.z_isig.x - tz;
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            const double isig = p.z_isig.y;
+            const double z = zeta_f64<K>(r * isig) * isig * isig * isig;
+            zg[0] += z * p.gxy.x; zg[1] += z * p.gxy.y; zg[2] += z * p.gz_vx.x;
+            zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y;
+        }
+    }
+    if (!valid) return;
+    double o[3];
+    estr_combine(Jt + t * ldJt, zg, zv, transposed, o);
+    write_estr(t, o, SFS, ldS, partial, nt_pad);
+}
+
+template <int K>
+__global__ void __launch_bounds__(UJ_THREADS)
+estr_mixed_kernel(int64_t nt, const SrcEstrMixed* __restrict__ tgt, const double* __restrict__ Jt,
+                  int64_t ldJt, const uint8_t* __restrict__ static_t, int64_t ns_pad,
+                  const SrcEstrMixed* __restrict__ src, int64_t per_split, bool self, bool transposed,
+                  double* SFS, int64_t ldS, double* partial, int64_t nt_pad)
+{
+    __shared__ SrcEstrMixed tile[UJ_TILE];
+    const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
+    const bool valid = t < nt && !(static_t && static_t[t]);
+    float3 th = make_float3(1.0e4f, 1.0e4f, 1.0e4f), tl = make_float3(0.f, 0.f, 0.f);
+    if (t < nt) {
+        const float4 a = tgt[t].a, b = tgt[t].b;
+        th = make_float3(a.x, a.y, a.z);
+        tl = make_float3(b.x, b.y, b.z);
+    }
+    double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
+    const int64_t s0 = (int64_t)blockIdx.y * per_split;
+    const int64_t s1 = min(s0 + per_split, ns_pad);
+    for (int64_t base = s0; base < s1; base += UJ_TILE) {
+        __syncthreads();
+        tile[threadIdx.x] = src[base + threadIdx.x];
+        __syncthreads();
+        const int64_t jself = self ? t - base : -1;
+#pragma unroll 1
+        for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
+            float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
+#pragma unroll 4
+            for (int j = 0; j < UJ_BLOCK; j++) {
+                const SrcEstrMixed& p = tile[sb + j];
+                const float dx = (th.x - p.a.x) + (tl.x - p.b.x);
+                const float dy = (th.y - p.a.y) + (tl.y - p.b.y);
+                const float dz = (th.z - p.a.z) + (tl.z - p.b.z);
+                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * p.a.w;
+                if constexpr (zeta_skip_s<K>() > 0.0f) {
+                    if (__all_sync(0xffffffffu, s > zeta_skip_s<K>())) continue;
+                }
+                float z = zhat_f32<K>(s);
+                z = (sb + j == jself) ? 0.0f : z;
+                fg[0] = fmaf(z, p.c.x, fg[0]);
+                fg[1] = fmaf(z, p.c.y, fg[1]);
+                fg[2] = fmaf(z, p.c.z, fg[2]);
+                fv[0] = fmaf(z, p.c.w, fv[0]);
+                fv[1] = fmaf(z, p.d.x, fv[1]);
+                fv[2] = fmaf(z, p.d.y, fv[2]);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) { zg[k] += (double)fg[k]; zv[k] += (double)fv[k]; }
+        }
+    }
+    if (!valid) return;
+    double o[3];
+    estr_combine(Jt + t * ldJt, zg, zv, transposed, o);
+    write_estr(t, o, SFS, ldS, partial, nt_pad);
+}
+
+template <int K>
+static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
+                                 int64_t* launches)
+{
+    const int64_t ns_pad = round_up(a.ns, UJ_TILE);
+    const int64_t nt_pad = round_up(a.nt, UJ_THREADS);
+    const int nsplit = uj_num_splits(a.nt, a.ns, num_sms);
+    const int64_t tiles = ns_pad / UJ_TILE;
+    const int64_t per_split = ((tiles + nsplit - 1) / nsplit) * UJ_TILE;
+    double* partial = nsplit > 1 ? w.partial : nullptr;
+    const dim3 grid((unsigned)(nt_pad / UJ_THREADS), (unsigned)nsplit);
+    const int pb = 256;
+    const unsigned pgrid = (unsigned)((ns_pad + pb - 1) / pb);
+    if (a.precision == 0) {
+        SrcEstrF64* src = (SrcEstrF64*)w.src_pack;
+        pack_estr_f64<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
+                                                a.transposed, src);
+        estr_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, a.xt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
+                                                        per_split, a.self, a.transposed, a.SFS, a.ldS,
+                                                        partial, nt_pad);
+        *launches += 2;
+    } else {
+        SrcEstrMixed* src = (SrcEstrMixed*)w.src_pack;
+        pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
+                                                  a.transposed, src);
+        const SrcEstrMixed* tgt = src;
+        *launches += 1;
+        if (!a.self) {
+            SrcEstrMixed* tp = (SrcEstrMixed*)w.tgt_pack;
+            pack_estr_tgt<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, a.xt, tp);
+            tgt = tp;
+            *launches += 1;
+        }
+        estr_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
+                                                          per_split, a.self, a.transposed, a.SFS, a.ldS,
+                                                          partial, nt_pad);
+        *launches += 1;
+    }
+    if (partial) {
+        estr_reduce<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, nsplit, partial, nt_pad,
+                                                                   a.static_t, a.SFS, a.ldS);
+        *launches += 1;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_estr(const EstrArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
+                        int64_t* launches)
+{
+    if (a.nt <= 0 || a.ns <= 0) return cudaSuccess;
+    switch (a.kernel) {
+    case K_SING: return launch_estr_k<K_SING>(a, w, num_sms, st, launches);
+    case K_GAUS: return launch_estr_k<K_GAUS>(a, w, num_sms, st, launches);
+    case K_GAUSERF: return launch_estr_k<K_GAUSERF>(a, w, num_sms, st, launches);
+    case K_WNKLMNS: return launch_estr_k<K_WNKLMNS>(a, w, num_sms, st, launches);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace vpm

@@ -1,0 +1,192 @@
+"""ctypes binding of libvpm_gb300.so (C ABI declared in include/vpm_gb300.h).
+
+The library is the product path: there is no CPU fallback.  If the shared
+library has not been built, or no sm_103 GPU is present, every entry point
+raises instead of computing anything.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libvpm_gb300.so")
+
+# status codes, kernels, precisions and flags of include/vpm_gb300.h
+OK, ERR_ARG, ERR_CAPACITY, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NODEVICE, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
+KERNEL_SINGULAR, KERNEL_GAUSSIAN, KERNEL_GAUSSIANERF, KERNEL_WINCKELMANS = 0, 1, 2, 3
+FP64, FP32COMP = 0, 1
+RESET, RESET_SFS, SFS, TRANSPOSED, CHECK_FINITE = 1, 2, 4, 8, 16
+NFIELDS = 46
+FLOP_PER_UJ_PAIR = 74
+FLOP_PER_ESTR_PAIR = 25
+
+_STATUS_NAMES = {ERR_ARG: "VPM_ERR_ARG", ERR_CAPACITY: "VPM_ERR_CAPACITY", ERR_CUDA: "VPM_ERR_CUDA",
+                 ERR_NONFINITE: "VPM_ERR_NONFINITE", ERR_TIMEOUT: "VPM_ERR_TIMEOUT",
+                 ERR_NODEVICE: "VPM_ERR_NODEVICE", ERR_STATE: "VPM_ERR_STATE"}
+
+# Every exported symbol of include/vpm_gb300.h, with (restype, argtypes).
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_dbl = ctypes.c_double
+SIGNATURES = {
+    "vpm_ctx_create": (_int, [ctypes.POINTER(_vp), _int]),
+    "vpm_ctx_destroy": (_int, [_vp]),
+    "vpm_last_error": (ctypes.c_char_p, [_vp]),
+    "vpm_ctx_set_stream": (_int, [_vp, _vp]),
+    "vpm_ctx_set_timeout": (_int, [_vp, _dbl]),
+    "vpm_abi_version": (_int, []),
+    "vpm_build_info": (ctypes.c_char_p, []),
+    "vpm_launch_count": (_i64, [_vp]),
+    "vpm_probe_ffma": (_int, [_vp, _vp]),
+    "vpm_uj": (_int, [_vp, _vp, _i64, _i64, _int, _int, _int]),
+    "vpm_uj_cross": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _i64, _int, _int]),
+    "vpm_uj_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int]),
+    "vpm_estr_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int]),
+}
+
+
+class VPMError(RuntimeError):
+    """A non-zero status returned by libvpm_gb300.so."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load() -> ctypes.CDLL:
+    """Load libvpm_gb300.so and declare its signatures; raise if it is missing."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is not built: run `python flowvpm.jl_gb300/build.py` "
+                    "(or __graft_entry__.build()); there is no CPU fallback")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (or None)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, int):
+        return a
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+class Context:
+    """One libvpm_gb300 context (device buffers, a stream, a mutex)."""
+
+    def __init__(self, device: int = 0):
+        self._L = load()
+        h = ctypes.c_void_p()
+        rc = self._L.vpm_ctx_create(ctypes.byref(h), int(device))
+        if rc != OK:
+            raise VPMError(rc, self._L.vpm_last_error(None).decode())
+        self._h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.vpm_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != OK:
+            raise VPMError(rc, self._L.vpm_last_error(self._h).decode())
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.vpm_launch_count(self._h))
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self._L.vpm_ctx_set_stream(self._h, stream_handle))
+
+    def set_timeout(self, seconds: float):
+        self._check(self._L.vpm_ctx_set_timeout(self._h, float(seconds)))
+
+    # --------------------------------------------------- host-matrix drop-in
+    def uj(self, particles: np.ndarray, np_: int, kernel: int, precision: int, flags: int):
+        """vpm_uj on a Fortran-ordered (46, maxparticles) float64 matrix, in place."""
+        if not (isinstance(particles, np.ndarray) and particles.dtype == np.float64
+                and particles.flags.f_contiguous and particles.shape[0] == NFIELDS):
+            raise TypeError("particles must be a Fortran-ordered float64 array of shape (46, maxparticles)")
+        if np_ > particles.shape[1]:
+            raise ValueError(f"np={np_} exceeds maxparticles={particles.shape[1]}")
+        self._check(self._L.vpm_uj(self._h, _ptr(particles), NFIELDS, int(np_), int(kernel),
+                                   int(precision), int(flags)))
+
+    def uj_cross(self, src: np.ndarray, ns: int, tgt: np.ndarray, nt: int, kernel: int, precision: int):
+        for m in (src, tgt):
+            if not (isinstance(m, np.ndarray) and m.dtype == np.float64 and m.flags.f_contiguous
+                    and m.shape[0] == NFIELDS):
+                raise TypeError("matrices must be Fortran-ordered float64 arrays of shape (46, n)")
+        self._check(self._L.vpm_uj_cross(self._h, _ptr(src), NFIELDS, int(ns), _ptr(tgt), NFIELDS,
+                                         int(nt), int(kernel), int(precision)))
+
+    # --------------------------------------------------- device-pointer API
+    def _torch_stream(self):
+        import torch
+        self.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    def uj_dev(self, xt, xs, gs, sgs, U, J, kernel: int, precision: int):
+        """U += and J += on CUDA float64 tensors x[n,3], gamma[n,3], sigma[n], U[n,3], J[n,9]."""
+        _check_dev(xt, 3); _check_dev(xs, 3); _check_dev(gs, 3); _check_dev(sgs, 1)
+        _check_dev(U, 3); _check_dev(J, 9)
+        self._torch_stream()
+        self._check(self._L.vpm_uj_dev(self._h, xt.shape[0], _ptr(xt), xs.shape[0], _ptr(xs), _ptr(gs),
+                                       _ptr(sgs), _ptr(U), _ptr(J), int(kernel), int(precision)))
+
+    def estr_dev(self, xt, Jt, xs, gs, sgs, Js, SFS, kernel: int, precision: int, transposed: bool = True,
+                 static_t=None, static_s=None):
+        _check_dev(xt, 3); _check_dev(Jt, 9); _check_dev(xs, 3); _check_dev(gs, 3); _check_dev(sgs, 1)
+        _check_dev(Js, 9); _check_dev(SFS, 3)
+        self._torch_stream()
+        self._check(self._L.vpm_estr_dev(self._h, xt.shape[0], _ptr(xt), _ptr(Jt), _ptr(static_t),
+                                         xs.shape[0], _ptr(xs), _ptr(gs), _ptr(sgs), _ptr(Js),
+                                         _ptr(static_s), _ptr(SFS), int(kernel), int(precision),
+                                         TRANSPOSED if transposed else 0))
+
+
+def _check_dev(t, ncol: int):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+        raise TypeError("expected a contiguous float64 CUDA tensor")
+    if ncol > 1 and (t.dim() != 2 or t.shape[1] != ncol):
+        raise TypeError(f"expected shape [n, {ncol}], got {tuple(t.shape)}")
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    """A process-wide context on CUDA device 0 (created on first use)."""
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx

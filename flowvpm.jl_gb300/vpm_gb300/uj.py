@@ -1,0 +1,60 @@
+"""The drop-in UJ hooks: `UJ_gb300` (FP64) and `UJ_gb300_mixed` (FP32-comp).
+
+Both have the signature and semantics of `UJ_direct(pfield; rbf, sfs, reset,
+reset_sfs)` (src/FLOWVPM_UJ.jl:21-37) and run through `vpm_uj` of the C ABI on
+the particle matrix itself, so a ParticleField built with `UJ=UJ_gb300` runs
+the time integration unchanged.  A kernel other than the four standard ones
+cannot cross the ABI and raises, like the reference's own error() paths.
+"""
+from __future__ import annotations
+
+from . import _lib
+from .particlefield import ParticleField, standard_kernels
+
+
+def _flags(pfield: ParticleField, sfs: bool, reset: bool, reset_sfs: bool) -> int:
+    f = 0
+    if reset:
+        f |= _lib.RESET
+    if reset_sfs:
+        f |= _lib.RESET_SFS
+    if sfs:
+        f |= _lib.SFS
+    if pfield.transposed:
+        f |= _lib.TRANSPOSED
+    return f
+
+
+def _kernel_id(pfield: ParticleField) -> int:
+    k = pfield.kernel
+    if k not in standard_kernels:
+        raise ValueError(f"UJ_gb300 supports only the standard kernels (singular, gaussian, gaussianerf, "
+                         f"winckelmans); got {k!r}")
+    return k.kid
+
+
+def _uj(pfield: ParticleField, precision: int, rbf: bool, sfs: bool, reset: bool, reset_sfs: bool,
+        ctx: _lib.Context | None):
+    if rbf:
+        raise NotImplementedError("rbf=true (zeta evaluation for the RBF solve) is not part of UJ_gb300")
+    c = ctx if ctx is not None else _lib.default_context()
+    c.uj(pfield.particles, pfield.np, _kernel_id(pfield), precision, _flags(pfield, sfs, reset, reset_sfs))
+
+
+def UJ_gb300(pfield: ParticleField, *, rbf: bool = False, sfs: bool = False, reset: bool = True,
+             reset_sfs: bool = False, ctx: _lib.Context | None = None, **optargs) -> None:
+    """UJ_direct on the GB300 in FP64 (the reference formula)."""
+    _uj(pfield, _lib.FP64, rbf, sfs, reset, reset_sfs, ctx)
+
+
+def UJ_gb300_mixed(pfield: ParticleField, *, rbf: bool = False, sfs: bool = False, reset: bool = True,
+                   reset_sfs: bool = False, ctx: _lib.Context | None = None, **optargs) -> None:
+    """UJ_direct on the GB300 with FP32 pair math and FP64 block reduction."""
+    _uj(pfield, _lib.FP32COMP, rbf, sfs, reset, reset_sfs, ctx)
+
+
+def UJ_gb300_cross(source: ParticleField, target: ParticleField, *, precision: int = _lib.FP64,
+                   ctx: _lib.Context | None = None) -> None:
+    """UJ_direct(source, target), src/FLOWVPM_UJ.jl:48-50: accumulate, no reset."""
+    c = ctx if ctx is not None else _lib.default_context()
+    c.uj_cross(source.particles, source.np, target.particles, target.np, _kernel_id(source), precision)

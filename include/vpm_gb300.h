@@ -1,0 +1,159 @@
+/*
+ * vpm_gb300.h -- C ABI of the GB300-native UJ evaluator for FLOWVPM.jl particle
+ * fields (libvpm_gb300.so).
+ *
+ * The library replaces the particle-to-particle evaluation behind the
+ * `pfield.UJ` hook of FLOWVPM.jl (struct field `UJ::TUJ`,
+ * src/FLOWVPM_particlefield.jl:81,127): the all-pairs regularized Biot-Savart
+ * sum of velocity U and velocity gradient J (src/FLOWVPM_fmm.jl:102-168), the
+ * SFS vortex-stretching pass Estr (src/FLOWVPM_subfilterscale_models.jl:16-92),
+ * their reverse-mode adjoint (replacing src/FLOWVPM_rrules.jl:179-330) and the
+ * near-field leaf-pair P2P leg of UJ_fmm (src/FLOWVPM_UJ.jl:90-125).
+ *
+ * Conventions shared by every entry point:
+ *   - Plain pointers and sizes only; no exceptions cross the ABI.
+ *   - Every call returns an int status: 0 = VPM_OK, negative = error.  The text
+ *     of the last error of a context is returned by vpm_last_error().
+ *   - Calls are synchronous on return (like the reference, which calls UJ
+ *     serially from the main task), unless the name ends in `_async`.
+ *   - A context is bound to one CUDA device and one stream and serialises its
+ *     calls with a mutex.  Different contexts may be used from different
+ *     threads.
+ *   - Host particle matrices use the reference layout: column-major
+ *     Matrix{Float64}(46, maxparticles), one 46-row column per particle
+ *     (src/FLOWVPM_particlefield.jl:11,134,239-252).  Row numbers below are the
+ *     reference's 1-based rows.
+ *   - "_dev" entry points take device pointers (e.g. torch CUDA tensors).
+ *     Particle vectors are per-particle interleaved: x[3*i+k], gamma[3*i+k],
+ *     U[3*i+k], J[9*i + (k + 3*l)] = dU_k/dx_l (column-major 3x3, the same
+ *     order as rows 16:24 of the reference, src/FLOWVPM_fmm.jl:160).
+ */
+#ifndef VPM_GB300_H
+#define VPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VPM_ABI_VERSION 1
+#define VPM_NFIELDS 46   /* rows per particle, src/FLOWVPM_particlefield.jl:11 */
+
+typedef struct vpm_ctx vpm_ctx;
+
+/* status codes */
+enum {
+    VPM_OK            =  0,
+    VPM_ERR_ARG       = -1,  /* bad pointer, size, id or flag */
+    VPM_ERR_CAPACITY  = -2,  /* device memory could not be grown to the request */
+    VPM_ERR_CUDA      = -3,  /* a CUDA runtime call failed */
+    VPM_ERR_NONFINITE = -4,  /* NaN/Inf found in an input or an output */
+    VPM_ERR_TIMEOUT   = -5,  /* a bounded device wait gave up */
+    VPM_ERR_NODEVICE  = -6,  /* no CUDA device / wrong architecture */
+    VPM_ERR_STATE     = -7   /* context used after an unrecoverable error */
+};
+
+/* regularizing kernels, src/FLOWVPM.jl:129-132 (singular, gaussian,
+ * gaussianerf, winckelmans); src/FLOWVPM_kernel.jl:45-84 */
+enum {
+    VPM_KERNEL_SINGULAR    = 0,
+    VPM_KERNEL_GAUSSIAN    = 1,
+    VPM_KERNEL_GAUSSIANERF = 2,
+    VPM_KERNEL_WINCKELMANS = 3
+};
+
+/* arithmetic of the pair evaluation */
+enum {
+    VPM_FP64     = 0,  /* the reference's FP64 formula, FP64 throughout */
+    VPM_FP32COMP = 1   /* FP32 pair math, double-float displacement, FP64 block reduction */
+};
+
+/* flags of vpm_uj, mirroring the keyword arguments of UJ_direct
+ * (src/FLOWVPM_UJ.jl:21-37) and ParticleField.transposed */
+enum {
+    VPM_RESET      = 1,  /* reset=true: zero rows 10:27 of non-static particles first */
+    VPM_RESET_SFS  = 2,  /* reset_sfs=true: zero rows 40:42 of non-static particles */
+    VPM_SFS        = 4,  /* sfs=true: accumulate Estr into rows 40:42 after U,J */
+    VPM_TRANSPOSED = 8,  /* transposed stretching scheme (pfield.transposed) */
+    VPM_CHECK_FINITE = 16 /* scan outputs for NaN/Inf and return VPM_ERR_NONFINITE */
+};
+
+/* Work per pair used for all throughput and roofline figures (flop: add, sub,
+ * mul = 1, fma = 2; sqrt/exp/erf/reciprocals counted separately). */
+#define VPM_FLOP_PER_UJ_PAIR   74
+#define VPM_FLOP_PER_ESTR_PAIR 25
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device`.  Fails with VPM_ERR_NODEVICE if
+ * there is no device or it is not an sm_103 part. */
+int vpm_ctx_create(vpm_ctx** out, int device);
+int vpm_ctx_destroy(vpm_ctx* ctx);
+/* Text of the last error of `ctx` (or of the last failed vpm_ctx_create when
+ * ctx is NULL).  Valid until the next call on the same context. */
+const char* vpm_last_error(const vpm_ctx* ctx);
+/* Use `stream` (a cudaStream_t) for all later work of this context.  NULL
+ * selects the context's own stream. */
+int vpm_ctx_set_stream(vpm_ctx* ctx, void* stream);
+/* Bound, in seconds, on every host wait for device work of this context
+ * (default 3600).  A wait that runs out returns VPM_ERR_TIMEOUT and marks the
+ * context unusable. */
+int vpm_ctx_set_timeout(vpm_ctx* ctx, double seconds);
+/* Library and ABI identification. */
+int vpm_abi_version(void);
+const char* vpm_build_info(void);
+/* Number of kernel launches issued by this context since creation. */
+int64_t vpm_launch_count(const vpm_ctx* ctx);
+/* Measurement helper (no counterpart in the reference): FP32 FFMA throughput
+ * of this device in TFLOP/s, from a pure FFMA-chain kernel timed with CUDA
+ * events.  Used as the FP32-pipe roofline denominator. */
+int vpm_probe_ffma(vpm_ctx* ctx, double* tflops);
+
+/* -------------------------------------------------- reference-facing drop-in */
+
+/* UJ_direct(pfield; sfs, reset, reset_sfs) on the host particle matrix.
+ * Replaces src/FLOWVPM_UJ.jl:21-37 (pair math src/FLOWVPM_fmm.jl:102-168,
+ * resets src/FLOWVPM_particlefield.jl:464-507, Estr
+ * src/FLOWVPM_subfilterscale_models.jl:16-92).
+ *   particles : host pointer, column-major ld x np doubles (ld must be 46)
+ *   np        : number of particles in the field (pfield.np)
+ * Semantics: if VPM_RESET, zero rows 10:27 of non-static particles; if
+ * VPM_RESET_SFS, zero rows 40:42 of non-static particles; add U (rows 10:12)
+ * and J (rows 16:24) induced on every particle by every particle, skipping
+ * pairs with r^2 == 0; if VPM_SFS, then add Estr (rows 40:42) on non-static
+ * targets from non-static sources, using the accumulated J. */
+int vpm_uj(vpm_ctx* ctx, double* particles, int64_t ld, int64_t np,
+           int kernel, int precision, int flags);
+
+/* UJ_direct(source, target): U and J that field `src` induces on every
+ * particle of field `tgt`, accumulated without reset.
+ * Replaces src/FLOWVPM_UJ.jl:48-50. */
+int vpm_uj_cross(vpm_ctx* ctx, const double* src, int64_t ld_src, int64_t ns,
+                 double* tgt, int64_t ld_tgt, int64_t nt, int kernel, int precision);
+
+/* ------------------------------------------------------ device-pointer API */
+
+/* U[nt,3] += and J[nt,9] += the field of sources (xs, gs, sgs) at targets xt.
+ * Pairs with r^2 == 0 are skipped (src/FLOWVPM_fmm.jl:118), so xt may alias xs.
+ * Device pointers. */
+int vpm_uj_dev(vpm_ctx* ctx, int64_t nt, const double* xt,
+               int64_t ns, const double* xs, const double* gs, const double* sgs,
+               double* U, double* J, int kernel, int precision);
+
+/* SFS[nt,3] += Estr of sources on targets (src/FLOWVPM_subfilterscale_models.jl:16-41):
+ *   SFS_t += zeta(r/sigma_s)/sigma_s^3 * (J_t - J_s)^T Gamma_s   (VPM_TRANSPOSED)
+ *   SFS_t += zeta(r/sigma_s)/sigma_s^3 * (J_t - J_s)   Gamma_s   (otherwise)
+ * static_t / static_s (may be NULL = none static) are 0/1 flags; static
+ * targets are left untouched and static sources contribute nothing
+ * (iterator default, src/FLOWVPM_particlefield.jl:368-373).  Device pointers. */
+int vpm_estr_dev(vpm_ctx* ctx, int64_t nt, const double* xt, const double* Jt,
+                 const uint8_t* static_t,
+                 int64_t ns, const double* xs, const double* gs, const double* sgs,
+                 const double* Js, const uint8_t* static_s,
+                 double* SFS, int kernel, int precision, int flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VPM_GB300_H */
