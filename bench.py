@@ -327,16 +327,57 @@ def measure_ffma_peak(ctx) -> float:
     return float(out[0])
 
 
+def run_kernel_only(args):
+    """Profiling helper: only the UJ (or Estr) kernels on an n-particle cloud,
+    `warmup` + `steps` evaluations, no other work (for ncu captures)."""
+    import torch
+    import vpm_gb300 as vpm
+    n = args.n
+    prec = vpm.FP64 if args.precision == "fp64" else vpm.FP32COMP
+    kern = {"singular": 0, "gaussian": 1, "gaussianerf": 2, "winckelmans": 3}[args.kernel]
+    ctx = vpm.Context(0)
+    X, G, s = random_cloud(n, seed=1)
+    d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
+    xt, gs, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    SFS = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    times = []
+    for k in range(args.warmup + args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        if args.estr:
+            ctx.estr_dev(xt, J, xt, gs, sg, J, SFS, kern, prec, True)
+        else:
+            ctx.uj_dev(xt, xt, gs, sg, U, J, kern, prec)
+        b.record()
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            times.append(a.elapsed_time(b))
+    ms = statistics.mean(times) if times else float("nan")
+    print(json.dumps({"mode": "kernel-only", "n": n, "precision": args.precision, "kernel": args.kernel,
+                      "estr": bool(args.estr), "ms": ms, "pairs_per_s": n * n / (ms / 1e3),
+                      "launches": ctx.launches}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    # profiling helpers (not the bench line): kernels alone on a smaller cloud
+    ap.add_argument("--kernel-only", action="store_true")
+    ap.add_argument("--n", type=int, default=1 << 16)
+    ap.add_argument("--precision", default="fp32comp", choices=["fp64", "fp32comp"])
+    ap.add_argument("--kernel", default="gaussianerf", choices=["singular", "gaussian", "gaussianerf", "winckelmans"])
+    ap.add_argument("--estr", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
-    if args.impl == "reference":
+    if args.kernel_only:
+        run_kernel_only(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_gpu(args, rank, world)

@@ -61,7 +61,7 @@ struct vpm_ctx {
     // device copies of host matrices and SoA views of them
     DevBuf mat, mat2, x, g, s, st, xt;
     // packing and split-K scratch
-    DevBuf src_pack, tgt_pack, partial, flag;
+    DevBuf src_pack, order, partial, flag;
 };
 
 namespace {
@@ -216,16 +216,16 @@ int ensure_work(vpm_ctx* c, int64_t nt, int64_t ns, int precision, bool estr, Wo
 {
     size_t sp = uj_src_pack_bytes(ns, precision);
     if (estr) { size_t e = estr_src_pack_bytes(ns, precision); if (e > sp) sp = e; }
-    size_t tp = precision ? estr_src_pack_bytes(nt, 1) : 0;  // >= the UJ target pack
+    const size_t ob = order_bytes(nt);
     const int nsplit = uj_num_splits(nt, ns, c->num_sms);
     const size_t pb = uj_partial_bytes(nt, nsplit);
-    if (c->src_pack.grow(sp) != cudaSuccess || (tp && c->tgt_pack.grow(tp) != cudaSuccess) ||
+    if (c->src_pack.grow(sp) != cudaSuccess || c->order.grow(ob) != cudaSuccess ||
         (pb && c->partial.grow(pb) != cudaSuccess)) {
         cudaGetLastError();
-        return fail(c, VPM_ERR_CAPACITY, "could not allocate %zu B of packing/scratch memory", sp + tp + pb);
+        return fail(c, VPM_ERR_CAPACITY, "could not allocate %zu B of packing/scratch memory", sp + ob + pb);
     }
     w->src_pack = c->src_pack.p; w->src_pack_bytes = c->src_pack.cap;
-    w->tgt_pack = c->tgt_pack.p; w->tgt_pack_bytes = c->tgt_pack.cap;
+    w->order = c->order.p; w->order_bytes = c->order.cap;
     w->partial = (double*)c->partial.p; w->partial_bytes = c->partial.cap;
     return VPM_OK;
 }
@@ -303,7 +303,7 @@ int vpm_ctx_destroy(vpm_ctx* c)
         std::lock_guard<std::mutex> lk(c->mu);
         DeviceGuard dg(c->device);
         if (!c->broken) cudaStreamSynchronize(c->stream);
-        for (DevBuf* b : {&c->mat, &c->mat2, &c->x, &c->g, &c->s, &c->st, &c->xt, &c->src_pack, &c->tgt_pack,
+        for (DevBuf* b : {&c->mat, &c->mat2, &c->x, &c->g, &c->s, &c->st, &c->xt, &c->src_pack, &c->order,
                           &c->partial, &c->flag})
             b->release();
         if (c->done) cudaEventDestroy(c->done);

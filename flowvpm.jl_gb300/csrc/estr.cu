@@ -9,9 +9,10 @@
 // costs about 25 flop.  The self pair, which the reference includes but which
 // contributes exactly zero there, is excluded by index (in the factored form
 // its two terms would only cancel to rounding).  Static sources are packed with
-// zero strength; static targets are left untouched.  The FP64 kernel keeps the
-// reference's zeta formula; the mixed kernel uses FP32 pair math with a
-// double-float displacement and FP64 accumulation of FP32 blocks.
+// zero strength; static targets are left untouched.  Targets run in Morton
+// order (order.cu) like the UJ kernels.  The FP64 kernel keeps the reference's
+// zeta formula; the mixed kernel uses FP32 pair math on per-warp FP32 offsets
+// (see uj.cu) and FP64 accumulation of FP32 blocks.
 #include "internal.h"
 #include "vpm_math.cuh"
 
@@ -50,38 +51,24 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= ns_pad) return;
     SrcEstrMixed p;
+    p.pad = 0.f;
     if (i < ns) {
-        const double x = xs[3 * i], y = xs[3 * i + 1], z = xs[3 * i + 2];
-        const float xh = (float)x, yh = (float)y, zh = (float)z;
         const double isig = 1.0 / sgs[i];
         const double isig2 = isig * isig;
-        p.a = make_float4(xh, yh, zh, (float)isig2);
-        p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
+        p.x = xs[3 * i]; p.y = xs[3 * i + 1]; p.z = xs[3 * i + 2];
+        p.isig2 = (float)isig2;
         const bool off = static_s && static_s[i];
         const double k = off ? 0.0 : zeta_norm(K) * isig2 * isig;
         const double gx = gs[3 * i], gy = gs[3 * i + 1], gz = gs[3 * i + 2];
         double vx, vy, vz;
         stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
-        p.c = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), (float)(k * vx));
-        p.d = make_float4((float)(k * vy), (float)(k * vz), 0.f, 0.f);
+        p.g = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), 0.f);
+        p.v = make_float4((float)(k * vx), (float)(k * vy), (float)(k * vz), 0.f);
     } else {
-        p.a = make_float4(0.f, 0.f, 0.f, 1.f);
-        p.b = p.c = p.d = make_float4(0.f, 0.f, 0.f, 0.f);
+        p.x = p.y = p.z = 0.0;
+        p.isig2 = 1.f;
+        p.g = p.v = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    out[i] = p;
-}
-
-// Target positions of the mixed Estr kernel (only fields a and b are read).
-__global__ void pack_estr_tgt(int64_t nt, const double* __restrict__ xt, SrcEstrMixed* __restrict__ out)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= nt) return;
-    const double x = xt[3 * i], y = xt[3 * i + 1], z = xt[3 * i + 2];
-    const float xh = (float)x, yh = (float)y, zh = (float)z;
-    SrcEstrMixed p;
-    p.a = make_float4(xh, yh, zh, 0.f);
-    p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
-    p.c = p.d = make_float4(0.f, 0.f, 0.f, 0.f);
     out[i] = p;
 }
 
@@ -113,7 +100,7 @@ __global__ void pack_estr_f64(int64_t ns, int64_t ns_pad, const double* __restri
     out[i] = p;
 }
 
-// SFS_t += J_t^T Zg - Zv  (or J_t Zg - Zv), FP64.
+// SFS contribution J_t^T Zg - Zv  (or J_t Zg - Zv), FP64.
 __device__ __forceinline__ void estr_combine(const double* Jt, const double (&zg)[3], const double (&zv)[3],
                                              bool transposed, double (&out)[3])
 {
@@ -124,42 +111,49 @@ __device__ __forceinline__ void estr_combine(const double* Jt, const double (&zg
     out[2] = sz - zv[2];
 }
 
-__device__ __forceinline__ void write_estr(int64_t t, const double (&o)[3], double* SFS, int64_t ldS,
+__device__ __forceinline__ void write_estr(int64_t t, int64_t idx, const double (&o)[3], double* SFS, int64_t ldS,
                                            double* partial, int64_t nt_pad)
 {
     if (partial) {
         double* p = partial + (int64_t)blockIdx.y * 3 * nt_pad + t;
         p[0] = o[0]; p[nt_pad] = o[1]; p[2 * nt_pad] = o[2];
     } else {
-        SFS[t * ldS] += o[0]; SFS[t * ldS + 1] += o[1]; SFS[t * ldS + 2] += o[2];
+        SFS[idx * ldS] += o[0]; SFS[idx * ldS + 1] += o[1]; SFS[idx * ldS + 2] += o[2];
     }
 }
 
 __global__ void estr_reduce(int64_t nt, int nsplit, const double* __restrict__ partial, int64_t nt_pad,
-                            const uint8_t* __restrict__ static_t, double* SFS, int64_t ldS)
+                            const TgtPos* __restrict__ tgt, const uint8_t* __restrict__ static_t,
+                            double* SFS, int64_t ldS)
 {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= nt || (static_t && static_t[t])) return;
+    if (t >= nt) return;
+    const int64_t i = tgt[t].idx;
+    if (static_t && static_t[i]) return;
     for (int k = 0; k < 3; k++) {
         double s = 0.0;
         for (int sp = 0; sp < nsplit; sp++) s += partial[((int64_t)sp * 3 + k) * nt_pad + t];
-        SFS[t * ldS + k] += s;
+        SFS[i * ldS + k] += s;
     }
 }
 
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
-estr_f64_kernel(int64_t nt, const double* __restrict__ xt, const double* __restrict__ Jt, int64_t ldJt,
+estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
                 const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrF64* __restrict__ src,
                 int64_t per_split, bool self, bool transposed, double* SFS, int64_t ldS,
                 double* partial, int64_t nt_pad)
 {
     __shared__ SrcEstrF64 tile[UJ_TILE];
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
-    const bool valid = t < nt && !(static_t && static_t[t]);
-    const double tx = t < nt ? xt[3 * t] : 1.0e3;
-    const double ty = t < nt ? xt[3 * t + 1] : 1.0e3;
-    const double tz = t < nt ? xt[3 * t + 2] : 1.0e3;
+    double tx = 1.0e3, ty = 1.0e3, tz = 1.0e3;
+    int64_t idx = -1;
+    if (t < nt) {
+        const TgtPos p = tgt[t];
+        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
+    }
+    const bool valid = t < nt && !(static_t && static_t[idx]);
+    const int64_t self_idx = self ? idx : -1;
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
@@ -170,7 +164,7 @@ estr_f64_kernel(int64_t nt, const double* __restrict__ xt, const double* __restr
 #pragma unroll 2
         for (int j = 0; j < UJ_TILE; j++) {
             const SrcEstrF64& p = tile[j];
-            if (self && base + j == t) continue;
+            if (base + j == self_idx) continue;
             const double dx = p.xy.x - tx, dy = p.xy.y - ty, dz = p.z_isig.x - tz;
             const double r = sqrt(dx * dx + dy * dy + dz * dz);
             const double isig = p.z_isig.y;
@@ -181,26 +175,33 @@ estr_f64_kernel(int64_t nt, const double* __restrict__ xt, const double* __restr
     }
     if (!valid) return;
     double o[3];
-    estr_combine(Jt + t * ldJt, zg, zv, transposed, o);
-    write_estr(t, o, SFS, ldS, partial, nt_pad);
+    estr_combine(Jt + idx * ldJt, zg, zv, transposed, o);
+    write_estr(t, idx, o, SFS, ldS, partial, nt_pad);
 }
 
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
-estr_mixed_kernel(int64_t nt, const SrcEstrMixed* __restrict__ tgt, const double* __restrict__ Jt,
-                  int64_t ldJt, const uint8_t* __restrict__ static_t, int64_t ns_pad,
-                  const SrcEstrMixed* __restrict__ src, int64_t per_split, bool self, bool transposed,
-                  double* SFS, int64_t ldS, double* partial, int64_t nt_pad)
+estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
+                  const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrMixed* __restrict__ src,
+                  int64_t per_split, bool self, bool transposed, double* SFS, int64_t ldS, double* partial,
+                  int64_t nt_pad)
 {
     __shared__ SrcEstrMixed tile[UJ_TILE];
+    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
-    const bool valid = t < nt && !(static_t && static_t[t]);
-    float3 th = make_float3(1.0e4f, 1.0e4f, 1.0e4f), tl = make_float3(0.f, 0.f, 0.f);
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    int64_t idx = -1;
     if (t < nt) {
-        const float4 a = tgt[t].a, b = tgt[t].b;
-        th = make_float3(a.x, a.y, a.z);
-        tl = make_float3(b.x, b.y, b.z);
+        const TgtPos p = tgt[t];
+        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
     }
+    const bool valid = t < nt && !(static_t && static_t[idx]);
+    const double ox = __shfl_sync(0xffffffffu, tx, 0);
+    const double oy = __shfl_sync(0xffffffffu, ty, 0);
+    const double oz = __shfl_sync(0xffffffffu, tz, 0);
+    const float3 to = t < nt ? make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz))
+                             : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
@@ -208,28 +209,34 @@ estr_mixed_kernel(int64_t nt, const SrcEstrMixed* __restrict__ tgt, const double
         __syncthreads();
         tile[threadIdx.x] = src[base + threadIdx.x];
         __syncthreads();
-        const int64_t jself = self ? t - base : -1;
+#pragma unroll
+        for (int q = 0; q < UJ_TILE / 32; q++) {
+            const int j = lane + 32 * q;
+            off[warp][j] = make_float4((float)(tile[j].x - ox), (float)(tile[j].y - oy),
+                                       (float)(tile[j].z - oz), tile[j].isig2);
+        }
+        __syncwarp();
+        const int64_t jself = self ? idx - base : -1;
 #pragma unroll 1
         for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
             float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
 #pragma unroll 4
             for (int j = 0; j < UJ_BLOCK; j++) {
-                const SrcEstrMixed& p = tile[sb + j];
-                const float dx = (th.x - p.a.x) + (tl.x - p.b.x);
-                const float dy = (th.y - p.a.y) + (tl.y - p.b.y);
-                const float dz = (th.z - p.a.z) + (tl.z - p.b.z);
-                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * p.a.w;
+                const float4 a = off[warp][sb + j];
+                const float dx = to.x - a.x, dy = to.y - a.y, dz = to.z - a.z;
+                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * a.w;
                 if constexpr (zeta_skip_s<K>() > 0.0f) {
                     if (__all_sync(0xffffffffu, s > zeta_skip_s<K>())) continue;
                 }
                 float z = zhat_f32<K>(s);
                 z = (sb + j == jself) ? 0.0f : z;
-                fg[0] = fmaf(z, p.c.x, fg[0]);
-                fg[1] = fmaf(z, p.c.y, fg[1]);
-                fg[2] = fmaf(z, p.c.z, fg[2]);
-                fv[0] = fmaf(z, p.c.w, fv[0]);
-                fv[1] = fmaf(z, p.d.x, fv[1]);
-                fv[2] = fmaf(z, p.d.y, fv[2]);
+                const float4 g = tile[sb + j].g, v = tile[sb + j].v;
+                fg[0] = fmaf(z, g.x, fg[0]);
+                fg[1] = fmaf(z, g.y, fg[1]);
+                fg[2] = fmaf(z, g.z, fg[2]);
+                fv[0] = fmaf(z, v.x, fv[0]);
+                fv[1] = fmaf(z, v.y, fv[1]);
+                fv[2] = fmaf(z, v.z, fv[2]);
             }
 #pragma unroll
             for (int k = 0; k < 3; k++) { zg[k] += (double)fg[k]; zv[k] += (double)fv[k]; }
@@ -237,8 +244,8 @@ estr_mixed_kernel(int64_t nt, const SrcEstrMixed* __restrict__ tgt, const double
     }
     if (!valid) return;
     double o[3];
-    estr_combine(Jt + t * ldJt, zg, zv, transposed, o);
-    write_estr(t, o, SFS, ldS, partial, nt_pad);
+    estr_combine(Jt + idx * ldJt, zg, zv, transposed, o);
+    write_estr(t, idx, o, SFS, ldS, partial, nt_pad);
 }
 
 template <int K>
@@ -254,33 +261,27 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
     const dim3 grid((unsigned)(nt_pad / UJ_THREADS), (unsigned)nsplit);
     const int pb = 256;
     const unsigned pgrid = (unsigned)((ns_pad + pb - 1) / pb);
+    const TgtPos* tgt = nullptr;
+    cudaError_t e = order_targets(a.nt, a.xt, w.order, w.order_bytes, st, launches, &tgt);
+    if (e != cudaSuccess) return e;
     if (a.precision == 0) {
         SrcEstrF64* src = (SrcEstrF64*)w.src_pack;
         pack_estr_f64<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
                                                 a.transposed, src);
-        estr_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, a.xt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
+        estr_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
                                                         per_split, a.self, a.transposed, a.SFS, a.ldS,
                                                         partial, nt_pad);
-        *launches += 2;
     } else {
         SrcEstrMixed* src = (SrcEstrMixed*)w.src_pack;
         pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
                                                   a.transposed, src);
-        const SrcEstrMixed* tgt = src;
-        *launches += 1;
-        if (!a.self) {
-            SrcEstrMixed* tp = (SrcEstrMixed*)w.tgt_pack;
-            pack_estr_tgt<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, a.xt, tp);
-            tgt = tp;
-            *launches += 1;
-        }
         estr_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
                                                           per_split, a.self, a.transposed, a.SFS, a.ldS,
                                                           partial, nt_pad);
-        *launches += 1;
     }
+    *launches += 2;
     if (partial) {
-        estr_reduce<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, nsplit, partial, nt_pad,
+        estr_reduce<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, nsplit, partial, nt_pad, tgt,
                                                                    a.static_t, a.SFS, a.ldS);
         *launches += 1;
     }

@@ -6,31 +6,35 @@
 
 namespace vpm {
 
-// Packed source payload of the mixed (FP32-comp) UJ kernel, 48 B per source:
-//   a = (x_hi, y_hi, z_hi, 1/sigma^2)
-//   b = (x_lo, y_lo, z_lo, 0)           x = x_hi + x_lo (double-float position)
-//   c = (-Gamma/(4 pi sigma^3), 0)
-// For the singular kernel sigma is taken as 1 (g == 1 does not depend on it).
-struct __align__(16) SrcMixed { float4 a, b, c; };
+// A target in Morton order: FP64 position and its index in the caller's arrays.
+struct __align__(16) TgtPos { double x, y, z; int32_t idx, pad; };
 
-// Packed source payload of the FP64 UJ kernel, 64 B per source.
+// Packed source of the mixed (FP32-comp) UJ kernel, 48 B:
+//   a   = (x_hi, y_hi, z_hi, sigma^2)     position as a double-float x_hi + x_lo
+//   b   = (x_lo, y_lo, z_lo, 1/sigma)
+//   gam = -Gamma/(4 pi)            for kernels with a singular tail (all but Winckelmans)
+//         -Gamma/(4 pi sigma^3)    for Winckelmans
+// For the singular kernel sigma is taken as 1 (g == 1 does not depend on it).
+struct __align__(16) SrcMixed { float4 a, b, gam; };
+
+// Packed source of the FP64 UJ kernel, 64 B.
 struct __align__(16) SrcF64 { double2 xy, z_isig, gxy, gz_sig; };
 
-// Packed source payload of the mixed Estr kernel, 64 B per source:
-//   a = (x_hi, y_hi, z_hi, 1/sigma^2), b = (x_lo, y_lo, z_lo, 0)
-//   c = (Gt_x, Gt_y, Gt_z, vt_x), d = (vt_y, vt_z, 0, 0)
-// with Gt = ZNORM * Gamma / sigma^3 and vt = ZNORM * v / sigma^3, v = J^T Gamma
-// (transposed scheme) or J Gamma; zero for static sources.
-struct __align__(16) SrcEstrMixed { float4 a, b, c, d; };
+// Packed source of the mixed Estr kernel, 64 B: FP64 position, 1/sigma^2,
+// g = ZNORM Gamma / sigma^3 and v = ZNORM (J^T Gamma) / sigma^3 (or J Gamma), in
+// FP32; g = v = 0 for static sources.
+struct __align__(16) SrcEstrMixed { double x, y, z; float isig2, pad; float4 g; float4 v; };
 
-// Packed source payload of the FP64 Estr kernel, 80 B per source:
+// Packed source of the FP64 Estr kernel, 80 B:
 //   (x, y), (z, 1/sigma), (Gamma_x, Gamma_y), (Gamma_z, v_x), (v_y, v_z)
 // with Gamma and v = J^T Gamma zero for static sources.
 struct __align__(16) SrcEstrF64 { double2 xy, z_isig, gxy, gz_vx, vyz; };
 
 constexpr int UJ_THREADS = 128;   // targets per block, one per thread
+constexpr int UJ_WARPS = UJ_THREADS / 32;
 constexpr int UJ_TILE = 128;      // sources staged in shared memory per tile
-constexpr int UJ_BLOCK = 64;      // sources summed in FP32 before the FP64 add
+constexpr int UJ_BLOCK = 64;      // sources summed in FP32 per inner block
+constexpr int UJ_FLUSH_TILES = 2; // tiles summed in FP32 before the FP64 add
 
 // Problem description handed from the ABI layer to the kernel launchers.
 struct UJArgs {
@@ -58,17 +62,19 @@ struct EstrArgs {
 // Scratch and packing buffers supplied by the caller (the context).
 struct Workspace {
     void* src_pack; size_t src_pack_bytes;
-    void* tgt_pack; size_t tgt_pack_bytes;
-    double* partial; size_t partial_bytes;   // split-K partial sums
+    void* order; size_t order_bytes;          // Morton ordering of the targets
+    double* partial; size_t partial_bytes;    // split-source partial sums
 };
 
-// Bytes of workspace needed for a problem (computed on the host).
 size_t uj_src_pack_bytes(int64_t ns, int precision);
-size_t uj_tgt_pack_bytes(int64_t nt, int precision);
 size_t estr_src_pack_bytes(int64_t ns, int precision);
-// Number of source splits used for nt targets / ns sources and partial bytes.
+size_t order_bytes(int64_t nt);
 int uj_num_splits(int64_t nt, int64_t ns, int num_sms);
 size_t uj_partial_bytes(int64_t nt, int nsplit);
+
+// Morton-order the nt targets xt; *out receives nt TgtPos records in scratch.
+cudaError_t order_targets(int64_t nt, const double* xt, void* scratch, size_t scratch_bytes, cudaStream_t st,
+                          int64_t* launches, const TgtPos** out);
 
 // Launchers; return cudaError_t of the launches and count kernel launches.
 cudaError_t launch_uj(const UJArgs& a, const Workspace& w, int num_sms, cudaStream_t st,

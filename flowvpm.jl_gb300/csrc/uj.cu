@@ -2,11 +2,25 @@
 // src/FLOWVPM_fmm.jl:102-168, over all sources as UJ_direct does,
 // src/FLOWVPM_UJ.jl:35).
 //
-// Layout: one target per thread, UJ_THREADS targets per block; sources are
-// packed once per call into a padded payload array and streamed through shared
-// memory in tiles of UJ_TILE.  gridDim.y splits the sources when there are too
-// few target blocks to fill the GPU; each split then writes FP64 partial sums
-// to scratch and uj_reduce adds them, in split order, to the outputs.
+// Layout: one target per thread, UJ_THREADS targets per block, targets in
+// Morton order (order.cu) so each warp holds 32 neighbouring targets.  Sources
+// are packed once per call and streamed through shared memory in tiles of
+// UJ_TILE.  gridDim.y splits the sources when there are too few target blocks
+// to fill the GPU; each split then writes FP64 partial sums to scratch and
+// uj_reduce adds them, in split order, to the outputs.
+//
+// Mixed (FP32-comp) kernel.  Positions are double-floats (hi + lo in FP32).
+//  * Far pairs: each warp takes its first target as origin and, once per tile,
+//    converts every source to an FP32 offset from it; dx = o_t - o_s then costs
+//    3 FP32 subtractions with an error of a few ulp of |dx| + the warp's extent
+//    b.  A source is "far" for a lane when r^2 > max(s_far sigma^2, (2b)^2):
+//    the kernel is then in its singular form (G = r^-3, Q = r^-5, no sigma) and
+//    the offset error is below 1.5 ulp of |dx|.
+//  * When any lane of the warp has a near pair among 4 sources (one vote), the
+//    warp evaluates those 4 pairs with dx = (x_t,hi - x_s,hi) + (x_t,lo - x_s,lo)
+//    and the full regular form of the kernel (vpm_math.cuh).
+// Sums run in FP32 over blocks of UJ_BLOCK sources, then in an FP32 mid-level
+// sum over UJ_FLUSH_TILES tiles, then in FP64.
 #include "internal.h"
 #include "vpm_math.cuh"
 
@@ -14,6 +28,8 @@ namespace vpm {
 
 static_assert(UJ_TILE == UJ_THREADS, "one source loaded per thread per tile");
 static_assert(UJ_TILE % UJ_BLOCK == 0, "FP32 blocks must tile the shared tile");
+static_assert(UJ_BLOCK % 4 == 0, "far/near votes cover groups of 4 sources");
+static_assert(UJ_TILE % 32 == 0, "per-warp conversion covers the tile in whole passes");
 
 static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
@@ -21,11 +37,6 @@ size_t uj_src_pack_bytes(int64_t ns, int precision)
 {
     const int64_t n = round_up(ns, UJ_TILE);
     return (size_t)n * (precision ? sizeof(SrcMixed) : sizeof(SrcF64));
-}
-
-size_t uj_tgt_pack_bytes(int64_t nt, int precision)
-{
-    return precision ? (size_t)round_up(nt, UJ_THREADS) * sizeof(SrcMixed) : 0;
 }
 
 int uj_num_splits(int64_t nt, int64_t ns, int num_sms)
@@ -39,8 +50,7 @@ int uj_num_splits(int64_t nt, int64_t ns, int num_sms)
     if (max_split < 1) max_split = 1;
     if (nsplit > max_split) nsplit = max_split;
     if (nsplit < 1) nsplit = 1;
-    // no empty splits
-    const int64_t per = (tiles + nsplit - 1) / nsplit;
+    const int64_t per = (tiles + nsplit - 1) / nsplit;   // no empty splits
     nsplit = (tiles + per - 1) / per;
     return (int)nsplit;
 }
@@ -49,6 +59,10 @@ size_t uj_partial_bytes(int64_t nt, int nsplit)
 {
     return nsplit > 1 ? (size_t)nsplit * 12 * (size_t)round_up(nt, UJ_THREADS) * sizeof(double) : 0;
 }
+
+// true for kernels equal to their singular form beyond some rho
+template <int K>
+__host__ __device__ constexpr bool singular_tail() { return K != K_WNKLMNS; }
 
 // ------------------------------------------------------------------ packing
 template <int K>
@@ -63,30 +77,16 @@ __global__ void pack_src_mixed(int64_t ns, int64_t ns_pad, const double* __restr
         const double x = xs[3 * i], y = xs[3 * i + 1], z = xs[3 * i + 2];
         const float xh = (float)x, yh = (float)y, zh = (float)z;
         const double sig = (K == K_SING) ? 1.0 : sgs[i];
-        const double isig = 1.0 / sig;
-        const double isig2 = isig * isig;
-        const double k = -C4 * isig2 * isig;
-        p.a = make_float4(xh, yh, zh, (float)isig2);
-        p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
-        p.c = make_float4((float)(k * gs[3 * i]), (float)(k * gs[3 * i + 1]), (float)(k * gs[3 * i + 2]), 0.f);
+        const double k = singular_tail<K>() ? -C4 : -C4 / (sig * sig * sig);
+        p.a = make_float4(xh, yh, zh, (float)(sig * sig));
+        p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh),
+                          (float)(1.0 / sig));
+        p.gam = make_float4((float)(k * gs[3 * i]), (float)(k * gs[3 * i + 1]), (float)(k * gs[3 * i + 2]), 0.f);
     } else {  // padding: no strength, at the origin, unit core
         p.a = make_float4(0.f, 0.f, 0.f, 1.f);
-        p.b = make_float4(0.f, 0.f, 0.f, 0.f);
-        p.c = make_float4(0.f, 0.f, 0.f, 0.f);
+        p.b = make_float4(0.f, 0.f, 0.f, 1.f);
+        p.gam = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    out[i] = p;
-}
-
-__global__ void pack_tgt_mixed(int64_t nt, const double* __restrict__ xt, SrcMixed* __restrict__ out)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= nt) return;
-    const double x = xt[3 * i], y = xt[3 * i + 1], z = xt[3 * i + 2];
-    const float xh = (float)x, yh = (float)y, zh = (float)z;
-    SrcMixed p;
-    p.a = make_float4(xh, yh, zh, 0.f);
-    p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
-    p.c = make_float4(0.f, 0.f, 0.f, 0.f);
     out[i] = p;
 }
 
@@ -153,87 +153,140 @@ __device__ __forceinline__ void pair_f64(double tx, double ty, double tz, const 
 }
 
 // ----------------------------------------------------------- pair: mixed
-// FP32 regular form (vpm_math.cuh).  With c = dx x Gamma'' (Gamma'' =
-// -Gamma/(4 pi sigma^3)):  U += G c ;  J_ij += (H/sigma^2) c_i dx_j ;
-// W += G Gamma''  (the Kronecker term, folded into J once per target).
-template <int K>
-__device__ __forceinline__ void pair_mixed(const float3& th, const float3& tl, const SrcMixed& p,
-                                           float (&u)[3], float (&jj)[9], float (&w)[3])
+// Accumulates U += G c, W += G gam, J' += Q c_i dx_j with c = dx x gam.  The
+// trace of J' vanishes (c . dx = 0), so J'_33 is not accumulated; the caller
+// sets it to -(J'_11 + J'_22).
+__device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float G, float Q, const float4& g,
+                                           float (&u)[3], float (&jq)[8], float (&w)[3])
 {
-    const float dx = (th.x - p.a.x) + (tl.x - p.b.x);
-    const float dy = (th.y - p.a.y) + (tl.y - p.b.y);
-    const float dz = (th.z - p.a.z) + (tl.z - p.b.z);
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float s = r2 * p.a.w;
-    float G, H;
-    kernel_GH<K>(s, G, H);
-    const bool nz = r2 > 0.0f;
-    G = nz ? G : 0.0f;
-    H = nz ? H : 0.0f;
-    const float cx = fmaf(dy, p.c.z, -dz * p.c.y);
-    const float cy = fmaf(dz, p.c.x, -dx * p.c.z);
-    const float cz = fmaf(dx, p.c.y, -dy * p.c.x);
+    const float cx = fmaf(dy, g.z, -dz * g.y);
+    const float cy = fmaf(dz, g.x, -dx * g.z);
+    const float cz = fmaf(dx, g.y, -dy * g.x);
     u[0] = fmaf(G, cx, u[0]);
     u[1] = fmaf(G, cy, u[1]);
     u[2] = fmaf(G, cz, u[2]);
-    w[0] = fmaf(G, p.c.x, w[0]);
-    w[1] = fmaf(G, p.c.y, w[1]);
-    w[2] = fmaf(G, p.c.z, w[2]);
-    const float hb = H * p.a.w;
-    const float bx = hb * cx, by = hb * cy, bz = hb * cz;
-    jj[0] = fmaf(bx, dx, jj[0]);
-    jj[1] = fmaf(by, dx, jj[1]);
-    jj[2] = fmaf(bz, dx, jj[2]);
-    jj[3] = fmaf(bx, dy, jj[3]);
-    jj[4] = fmaf(by, dy, jj[4]);
-    jj[5] = fmaf(bz, dy, jj[5]);
-    jj[6] = fmaf(bx, dz, jj[6]);
-    jj[7] = fmaf(by, dz, jj[7]);
-    jj[8] = fmaf(bz, dz, jj[8]);
+    w[0] = fmaf(G, g.x, w[0]);
+    w[1] = fmaf(G, g.y, w[1]);
+    w[2] = fmaf(G, g.z, w[2]);
+    const float bx = Q * cx, by = Q * cy, bz = Q * cz;
+    jq[0] = fmaf(bx, dx, jq[0]);
+    jq[1] = fmaf(by, dx, jq[1]);
+    jq[2] = fmaf(bz, dx, jq[2]);
+    jq[3] = fmaf(bx, dy, jq[3]);
+    jq[4] = fmaf(by, dy, jq[4]);
+    jq[5] = fmaf(bz, dy, jq[5]);
+    jq[6] = fmaf(bx, dz, jq[6]);
+    jq[7] = fmaf(by, dz, jq[7]);
+}
+
+// Four sources j0..j0+3 of the tile against this lane's target.
+//   to      : target offset from the warp origin (FP32)
+//   th, tl  : target double-float position
+//   r2n     : (2 b)^2, b = the warp's extent around its origin
+template <int K>
+__device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, const float3& tl, float r2n,
+                                            const float4* __restrict__ off, const SrcMixed* __restrict__ tile,
+                                            int j0, float (&u)[3], float (&jq)[8], float (&w)[3])
+{
+    float dx[4], dy[4], dz[4], r2[4], hw[4];
+    bool far = true;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float4 h = off[j0 + q];
+        dx[q] = to.x - h.x;
+        dy[q] = to.y - h.y;
+        dz[q] = to.z - h.z;
+        r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
+        hw[q] = h.w;
+        far = far && (r2[q] > (singular_tail<K>() ? h.w : r2n));
+    }
+    if (__all_sync(0xffffffffu, far)) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float G, Q;
+            if constexpr (singular_tail<K>()) {
+                const float rs = rsqrtf(r2[q]);
+                const float rs2 = rs * rs;
+                G = rs * rs2;
+                Q = G * rs2;
+            } else {
+                near_GQ<K>(r2[q] * hw[q], hw[q], G, Q);
+            }
+            accum_pair(dx[q], dy[q], dz[q], G, Q, tile[j0 + q].gam, u, jq, w);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float4 a = tile[j0 + q].a, b = tile[j0 + q].b;
+            const float ex = (th.x - a.x) + (tl.x - b.x);
+            const float ey = (th.y - a.y) + (tl.y - b.y);
+            const float ez = (th.z - a.z) + (tl.z - b.z);
+            const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+            float G, Q;
+            if constexpr (singular_tail<K>()) {
+                const float isig2 = b.w * b.w;
+                near_GQ<K>(e2 * isig2, isig2, G, Q);
+                const float isig3 = isig2 * b.w;
+                G *= isig3;
+                Q *= isig3;
+            } else {
+                near_GQ<K>(e2 * hw[q], hw[q], G, Q);
+            }
+            const bool nz = e2 > 0.0f;
+            G = nz ? G : 0.0f;
+            Q = nz ? Q : 0.0f;
+            accum_pair(ex, ey, ez, G, Q, tile[j0 + q].gam, u, jq, w);
+        }
+    }
 }
 
 // --------------------------------------------------------------- epilogue
-__device__ __forceinline__ void write_uj(int64_t t, const double (&acc)[12], double* U, int64_t ldU,
-                                         double* J, int64_t ldJ, double* partial, int64_t nt_pad)
+__device__ __forceinline__ void write_uj(int64_t t, int32_t idx, const double (&acc)[12], double* U,
+                                         int64_t ldU, double* J, int64_t ldJ, double* partial, int64_t nt_pad)
 {
     if (partial) {
         double* p = partial + (int64_t)blockIdx.y * 12 * nt_pad + t;
 #pragma unroll
         for (int k = 0; k < 12; k++) p[k * nt_pad] = acc[k];
     } else {
+        const int64_t i = idx;
 #pragma unroll
-        for (int k = 0; k < 3; k++) U[t * ldU + k] += acc[k];
+        for (int k = 0; k < 3; k++) U[i * ldU + k] += acc[k];
 #pragma unroll
-        for (int k = 0; k < 9; k++) J[t * ldJ + k] += acc[3 + k];
+        for (int k = 0; k < 9; k++) J[i * ldJ + k] += acc[3 + k];
     }
 }
 
 __global__ void uj_reduce(int64_t nt, int nsplit, const double* __restrict__ partial, int64_t nt_pad,
-                          double* U, int64_t ldU, double* J, int64_t ldJ)
+                          const TgtPos* __restrict__ tgt, double* U, int64_t ldU, double* J, int64_t ldJ)
 {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nt) return;
+    const int64_t i = tgt[t].idx;
     for (int k = 0; k < 12; k++) {
         double s = 0.0;
         for (int sp = 0; sp < nsplit; sp++) s += partial[((int64_t)sp * 12 + k) * nt_pad + t];
-        if (k < 3) U[t * ldU + k] += s;
-        else J[t * ldJ + (k - 3)] += s;
+        if (k < 3) U[i * ldU + k] += s;
+        else J[i * ldJ + (k - 3)] += s;
     }
 }
 
 // ------------------------------------------------------------ main kernels
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
-uj_f64_kernel(int64_t nt, const double* __restrict__ xt, int64_t ns_pad, const SrcF64* __restrict__ src,
+uj_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad, const SrcF64* __restrict__ src,
               int64_t per_split, double* U, int64_t ldU, double* J, int64_t ldJ,
               double* partial, int64_t nt_pad)
 {
     __shared__ SrcF64 tile[UJ_TILE];
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const bool valid = t < nt;
-    const double tx = valid ? xt[3 * t] : 1.0e3;
-    const double ty = valid ? xt[3 * t + 1] : 1.0e3;
-    const double tz = valid ? xt[3 * t + 2] : 1.0e3;
+    double tx = 1.0e3, ty = 1.0e3, tz = 1.0e3;
+    int32_t idx = 0;
+    if (valid) {
+        const TgtPos p = tgt[t];
+        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
+    }
     double acc[12];
 #pragma unroll
     for (int k = 0; k < 12; k++) acc[k] = 0.0;
@@ -246,58 +299,106 @@ uj_f64_kernel(int64_t nt, const double* __restrict__ xt, int64_t ns_pad, const S
 #pragma unroll 2
         for (int j = 0; j < UJ_TILE; j++) pair_f64<K>(tx, ty, tz, tile[j], acc);
     }
-    if (valid) write_uj(t, acc, U, ldU, J, ldJ, partial, nt_pad);
+    if (valid) write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
 
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
-uj_mixed_kernel(int64_t nt, const SrcMixed* __restrict__ tgt, int64_t ns_pad,
+uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
                 const SrcMixed* __restrict__ src, int64_t per_split, double* U, int64_t ldU,
                 double* J, int64_t ldJ, double* partial, int64_t nt_pad)
 {
     __shared__ SrcMixed tile[UJ_TILE];
+    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const bool valid = t < nt;
-    float3 th = make_float3(1.0e4f, 1.0e4f, 1.0e4f), tl = make_float3(0.f, 0.f, 0.f);
+    double tx = 3.0e4, ty = 3.0e4, tz = 3.0e4;
+    int32_t idx = 0;
     if (valid) {
-        const float4 a = tgt[t].a, b = tgt[t].b;
-        th = make_float3(a.x, a.y, a.z);
-        tl = make_float3(b.x, b.y, b.z);
+        const TgtPos p = tgt[t];
+        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
     }
-    double dU[3] = {0.0, 0.0, 0.0}, dW[3] = {0.0, 0.0, 0.0};
-    double dJ[9];
+    const float3 th = make_float3((float)tx, (float)ty, (float)tz);
+    const float3 tl = make_float3((float)(tx - (double)th.x), (float)(ty - (double)th.y), (float)(tz - (double)th.z));
+    // warp origin: lane 0's target (valid whenever any lane of the warp is)
+    const double ox = __shfl_sync(0xffffffffu, tx, 0);
+    const double oy = __shfl_sync(0xffffffffu, ty, 0);
+    const double oz = __shfl_sync(0xffffffffu, tz, 0);
+    const float3 oh = make_float3(__shfl_sync(0xffffffffu, th.x, 0), __shfl_sync(0xffffffffu, th.y, 0),
+                                  __shfl_sync(0xffffffffu, th.z, 0));
+    const float3 ol = make_float3(__shfl_sync(0xffffffffu, tl.x, 0), __shfl_sync(0xffffffffu, tl.y, 0),
+                                  __shfl_sync(0xffffffffu, tl.z, 0));
+    const float3 to = valid ? make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz))
+                            : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
+    // (2 b)^2 with b the largest |offset| of the warp's valid targets
+    float b2 = valid ? fmaf(to.x, to.x, fmaf(to.y, to.y, to.z * to.z)) : 0.0f;
 #pragma unroll
-    for (int k = 0; k < 9; k++) dJ[k] = 0.0;
+    for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
+    const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
+    const float sfar = s_far<K>();
+
+    double dU[3] = {0.0, 0.0, 0.0}, dW[3] = {0.0, 0.0, 0.0};
+    double dJ[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) dJ[k] = 0.0;
+    float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) mj[k] = 0.f;
+    int tiles_in_mid = 0;
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
     for (int64_t base = s0; base < s1; base += UJ_TILE) {
         __syncthreads();
         tile[threadIdx.x] = src[base + threadIdx.x];
         __syncthreads();
+        // this warp's FP32 offsets of the tile's sources and their far thresholds
+#pragma unroll
+        for (int q = 0; q < UJ_TILE / 32; q++) {
+            const int j = lane + 32 * q;
+            const float4 a = tile[j].a, b = tile[j].b;
+            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : b.w * b.w;
+            off[warp][j] = make_float4((a.x - oh.x) + (b.x - ol.x), (a.y - oh.y) + (b.y - ol.y),
+                                       (a.z - oh.z) + (b.z - ol.z), thr);
+        }
+        __syncwarp();
 #pragma unroll 1
         for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
             float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f};
-            float jj[9];
+            float jq[8];
 #pragma unroll
-            for (int k = 0; k < 9; k++) jj[k] = 0.f;
-#pragma unroll 4
-            for (int j = 0; j < UJ_BLOCK; j++) pair_mixed<K>(th, tl, tile[sb + j], u, jj, w);
+            for (int k = 0; k < 8; k++) jq[k] = 0.f;
+#pragma unroll 2
+            for (int j = 0; j < UJ_BLOCK; j += 4)
+                pair4_mixed<K>(to, th, tl, r2n, off[warp], tile, sb + j, u, jq, w);
 #pragma unroll
-            for (int k = 0; k < 3; k++) { dU[k] += (double)u[k]; dW[k] += (double)w[k]; }
+            for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; }
 #pragma unroll
-            for (int k = 0; k < 9; k++) dJ[k] += (double)jj[k];
+            for (int k = 0; k < 8; k++) mj[k] += jq[k];
+        }
+        if (++tiles_in_mid == UJ_FLUSH_TILES || base + UJ_TILE >= s1) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
+#pragma unroll
+            for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
+            tiles_in_mid = 0;
         }
     }
     if (!valid) return;
-    // Kronecker term of src/FLOWVPM_fmm.jl:148-159: W = sum aux2 * Gamma
-    dJ[1] -= dW[2];
-    dJ[2] += dW[1];
-    dJ[3] += dW[2];
-    dJ[5] -= dW[0];
-    dJ[6] -= dW[1];
-    dJ[7] += dW[0];
-    double acc[12] = {dU[0], dU[1], dU[2], dJ[0], dJ[1], dJ[2], dJ[3], dJ[4], dJ[5], dJ[6], dJ[7], dJ[8]};
-    write_uj(t, acc, U, ldU, J, ldJ, partial, nt_pad);
+    // J = -3 J' (J'_33 = -J'_11 - J'_22) plus the Kronecker term of
+    // src/FLOWVPM_fmm.jl:148-159 (W = sum aux2 Gamma)
+    double j9[9];
+#pragma unroll
+    for (int k = 0; k < 8; k++) j9[k] = -3.0 * dJ[k];
+    j9[8] = 3.0 * (dJ[0] + dJ[4]);
+    j9[1] -= dW[2];
+    j9[2] += dW[1];
+    j9[3] += dW[2];
+    j9[5] -= dW[0];
+    j9[6] -= dW[1];
+    j9[7] += dW[0];
+    double acc[12] = {dU[0], dU[1], dU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
+    write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
 
 // --------------------------------------------------------------- launcher
@@ -313,30 +414,24 @@ static cudaError_t launch_uj_k(const UJArgs& a, const Workspace& w, int num_sms,
     double* partial = nsplit > 1 ? w.partial : nullptr;
     const dim3 grid((unsigned)(nt_pad / UJ_THREADS), (unsigned)nsplit);
     const int pb = 256;
+    const TgtPos* tgt = nullptr;
+    cudaError_t e = order_targets(a.nt, a.xt, w.order, w.order_bytes, st, launches, &tgt);
+    if (e != cudaSuccess) return e;
     if (a.precision == 0) {
         SrcF64* src = (SrcF64*)w.src_pack;
         pack_src_f64<K><<<(unsigned)((ns_pad + pb - 1) / pb), pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, src);
-        uj_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, a.xt, ns_pad, src, per_split, a.U, a.ldU,
+        uj_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
                                                        a.J, a.ldJ, partial, nt_pad);
-        *launches += 2;
     } else {
         SrcMixed* src = (SrcMixed*)w.src_pack;
         pack_src_mixed<K><<<(unsigned)((ns_pad + pb - 1) / pb), pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, src);
-        const SrcMixed* tgt = src;
-        *launches += 1;
-        if (!a.self) {
-            SrcMixed* tp = (SrcMixed*)w.tgt_pack;
-            pack_tgt_mixed<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, a.xt, tp);
-            tgt = tp;
-            *launches += 1;
-        }
         uj_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
                                                          a.J, a.ldJ, partial, nt_pad);
-        *launches += 1;
     }
+    *launches += 2;
     if (partial) {
-        uj_reduce<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, nsplit, partial, nt_pad, a.U, a.ldU,
-                                                                 a.J, a.ldJ);
+        uj_reduce<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, nsplit, partial, nt_pad, tgt, a.U,
+                                                                 a.ldU, a.J, a.ldJ);
         *launches += 1;
     }
     return cudaGetLastError();

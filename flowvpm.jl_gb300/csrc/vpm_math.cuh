@@ -152,54 +152,96 @@ __device__ __forceinline__ float gaus_H_series(float t)
     return p;
 }
 
-// G(s), H(s) of kernel K (see the header comment).  Must be called by all 32
-// lanes of a warp together (the Gaussian kernels vote on a shared far path).
+// The mixed kernels accumulate, per pair,
+//     U += G c,   W += G gam,   J' += Q c_i dx_j,
+// with c = dx x gam, gam = -Gamma/(4 pi sigma^3), and Q = -H/(3 sigma^2), so
+// that J = -3 J' + (Kronecker term from W) once per target.  In the singular
+// (far) form Q = G / r^2.
+
+// s above which the kernel equals its singular form to FP32 resolution; 0 for
+// the singular kernel (every pair with r > 0), +inf for Winckelmans (never).
 template <int K>
-__device__ __forceinline__ void kernel_GH(float s, float& G, float& H)
+__host__ __device__ constexpr float s_far()
+{
+    return K == K_SING ? 0.0f : K == K_GAUSERF ? S_FAR_GERF : K == K_GAUS ? S_FAR_GAUS : 3.0e38f;
+}
+
+// Singular form: G = s^-1.5, Q = G / r^2 = G s^-1 / sigma^2.
+__device__ __forceinline__ void far_GQ(float s, float isig2, float& G, float& Q)
+{
+    const float rs = rsqrtf(s);
+    const float rs2 = rs * rs;
+    G = rs * rs2;
+    Q = G * (rs2 * isig2);
+}
+
+// Full form of kernel K for one lane (any s > 0).
+template <int K>
+__device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q)
 {
     if constexpr (K == K_WNKLMNS) {
-        // g/rho^3 = (s+2.5)(s+1)^-2.5 ; H = -(3s+10.5)(s+1)^-3.5
+        // g/rho^3 = (s+2.5)(s+1)^-2.5 ; -H/3 = (s+3.5)(s+1)^-3.5
         const float q = s + 1.0f;
         const float t = __frcp_rn(q);
-        const float u = rsqrtf(q);
-        const float t2u = t * t * u;
+        const float t2u = t * t * rsqrtf(q);
         G = (s + 2.5f) * t2u;
-        H = -fmaf(3.0f, s, 10.5f) * t * t2u;
+        Q = (s + 3.5f) * t * t2u * isig2;
+    } else if constexpr (K == K_SING) {
+        far_GQ(s, isig2, G, Q);
+    } else if constexpr (K == K_GAUSERF) {
+        if (s > S_FAR_GERF) {
+            far_GQ(s, isig2, G, Q);
+        } else if (s < S_SERIES) {
+            G = gerf_G_series(s);
+            Q = gerf_H_series(s) * (isig2 * -0.33333333333333333f);
+        } else {
+            const float rs = rsqrtf(s);
+            const float rs2 = rs * rs;
+            const float rho = s * rs;
+            const float e = expf(-0.5f * s);
+            const float g = erff(rho * 0.70710678118654752f) - F_C2 * rho * e;
+            G = g * rs * rs2;
+            Q = fmaf(F_C2 * -0.33333333333333333f, e, G) * rs2 * isig2;   // -H/3 = (G - c2 e / 3)/s
+        }
+    } else {  // Gaussian
+        if (s > S_FAR_GAUS) {
+            far_GQ(s, isig2, G, Q);
+        } else {
+            const float rs = rsqrtf(s);
+            const float rho = s * rs;
+            const float t = s * rho;
+            if (t < 1.0f) {
+                G = gaus_G_series(t);
+                Q = -rho * gaus_H_series(t) * isig2;
+            } else {
+                const float e = expf(-t);
+                G = (1.0f - e) * __frcp_rn(t);
+                const float rs2 = rs * rs;
+                Q = fmaf(-t, e, 1.0f - e) * rs2 * rs2 * rs * isig2;   // -H/3 = (1 - e - t e)/rho^5
+            }
+        }
+    }
+}
+
+// (G, Q) of one pair for the whole warp: the singular form when every lane is
+// past s_far (no divergence), else each lane's full form; pairs with r^2 == 0
+// contribute nothing (src/FLOWVPM_fmm.jl:118).  All 32 lanes must call it.
+template <int K>
+__device__ __forceinline__ void pair_GQ(float r2, float s, float isig2, float& G, float& Q)
+{
+    if constexpr (K == K_WNKLMNS) {
+        near_GQ<K>(s, isig2, G, Q);
+        const bool nz = r2 > 0.0f;
+        G = nz ? G : 0.0f;
+        Q = nz ? Q : 0.0f;
     } else {
-        const float rs = rsqrtf(s);
-        const float rs2 = rs * rs;
-        G = rs * rs2;
-        H = -3.0f * G * rs2;
-        if constexpr (K == K_GAUSERF) {
-            if (!__all_sync(0xffffffffu, s > S_FAR_GERF)) {
-                if (s <= S_FAR_GERF) {
-                    if (s < S_SERIES) {
-                        G = gerf_G_series(s);
-                        H = gerf_H_series(s);
-                    } else {
-                        const float rho = s * rs;
-                        const float e = expf(-0.5f * s);
-                        const float g = erff(rho * 0.70710678118654752f) - F_C2 * rho * e;
-                        G = g * rs * rs2;
-                        H = fmaf(-3.0f, G, F_C2 * e) * rs2;
-                    }
-                }
-            }
-        } else if constexpr (K == K_GAUS) {
-            if (!__all_sync(0xffffffffu, s > S_FAR_GAUS)) {
-                if (s <= S_FAR_GAUS) {
-                    const float rho = s * rs;
-                    const float t = s * rho;
-                    if (t < 1.0f) {
-                        G = gaus_G_series(t);
-                        H = 3.0f * rho * gaus_H_series(t);
-                    } else {
-                        const float e = expf(-t);
-                        G = (1.0f - e) * __frcp_rn(t);
-                        H = 3.0f * fmaf(t, e, e - 1.0f) * rs2 * rs2 * rs;
-                    }
-                }
-            }
+        if (__all_sync(0xffffffffu, s > s_far<K>())) {
+            far_GQ(s, isig2, G, Q);
+        } else {
+            near_GQ<K>(s, isig2, G, Q);
+            const bool nz = r2 > 0.0f;
+            G = nz ? G : 0.0f;
+            Q = nz ? Q : 0.0f;
         }
     }
 }
