@@ -47,6 +47,8 @@ thread_local std::string g_create_error;
 
 }  // namespace
 
+void vpm::set_thread_error(const char* msg) { g_create_error = msg; }
+
 struct vpm_ctx {
     int device = 0;
     int num_sms = 0;

@@ -76,6 +76,9 @@ size_t uj_partial_bytes(int64_t nt, int nsplit);
 cudaError_t order_targets(int64_t nt, const double* xt, void* scratch, size_t scratch_bytes, cudaStream_t st,
                           int64_t* launches, const TgtPos** out);
 
+// Sets the calling thread's context-free error text (vpm_last_error(NULL)).
+void set_thread_error(const char* msg);
+
 // Launchers; return cudaError_t of the launches and count kernel launches.
 cudaError_t launch_uj(const UJArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
                       int64_t* launches);

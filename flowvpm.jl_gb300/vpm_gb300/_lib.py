@@ -47,7 +47,9 @@ SIGNATURES = {
     "vpm_uj_cross": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _i64, _int, _int]),
     "vpm_uj_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int]),
     "vpm_estr_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int]),
+    "vpm_uj_dev_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp]),
 }
+NOALLOC_SCRATCH_BYTES = 64 << 20   # VPM_NOALLOC_SCRATCH_BYTES
 
 
 class VPMError(RuntimeError):

@@ -90,8 +90,9 @@ enum {
  * there is no device or it is not an sm_103 part. */
 int vpm_ctx_create(vpm_ctx** out, int device);
 int vpm_ctx_destroy(vpm_ctx* ctx);
-/* Text of the last error of `ctx` (or of the last failed vpm_ctx_create when
- * ctx is NULL).  Valid until the next call on the same context. */
+/* Text of the last error of `ctx` (or, when ctx is NULL, of the calling
+ * thread's last failed context-free call: vpm_ctx_create or
+ * vpm_uj_dev_noalloc).  Valid until the next call on the same context. */
 const char* vpm_last_error(const vpm_ctx* ctx);
 /* Use `stream` (a cudaStream_t) for all later work of this context.  NULL
  * selects the context's own stream. */
@@ -152,6 +153,29 @@ int vpm_estr_dev(vpm_ctx* ctx, int64_t nt, const double* xt, const double* Jt,
                  int64_t ns, const double* xs, const double* gs, const double* sgs,
                  const double* Js, const uint8_t* static_s,
                  double* SFS, int kernel, int precision, int flags);
+
+/* ------------------------------------------------ allocation-free variant */
+
+/* Size of the static device scratch array behind vpm_uj_dev_noalloc (64 MiB). */
+#define VPM_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* vpm_uj_dev without any device allocation (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc -- their device memory is owned by
+ * another allocator (a framework's caching pool, an arena reserved at
+ * start-up) or they must not allocate once running.  Same arguments and
+ * results as vpm_uj_dev, plus the caller's stream (a cudaStream_t; NULL = the
+ * legacy default stream), on the current CUDA device, with no context.  The
+ * call returns after the work on `stream` has finished.
+ * Scratch lives in one file-scope __device__ array of VPM_NOALLOC_SCRATCH_BYTES
+ * held by every GPU that loads it until the process exits; problems needing
+ * more scratch than that (roughly N > 2^19 particles) return VPM_ERR_CAPACITY.
+ * The first call on each device looks up the array's device address (with
+ * that device current), so make that first call before any stream capture.
+ * All calls share the array: calls whose device work overlaps race on it.
+ * Errors are described by vpm_last_error(NULL). */
+int vpm_uj_dev_noalloc(int64_t nt, const double* xt,
+                       int64_t ns, const double* xs, const double* gs, const double* sgs,
+                       double* U, double* J, int kernel, int precision, void* stream);
 
 #ifdef __cplusplus
 }
