@@ -4,6 +4,7 @@
 #include "../../include/vpm_gb300.h"
 #include "internal.h"
 #include "vpm_math.cuh"
+#include "tree.h"
 
 #include <algorithm>
 #include <chrono>
@@ -64,6 +65,8 @@ struct vpm_ctx {
     DevBuf mat, mat2, x, g, s, st, xt;
     // packing and split-K scratch
     DevBuf src_pack, order, partial, flag;
+    // near-field leaf-pair lists and their packed particles
+    DevBuf leaf;
 };
 
 namespace {
@@ -306,7 +309,7 @@ int vpm_ctx_destroy(vpm_ctx* c)
         DeviceGuard dg(c->device);
         if (!c->broken) cudaStreamSynchronize(c->stream);
         for (DevBuf* b : {&c->mat, &c->mat2, &c->x, &c->g, &c->s, &c->st, &c->xt, &c->src_pack, &c->order,
-                          &c->partial, &c->flag})
+                          &c->partial, &c->flag, &c->leaf})
             b->release();
         if (c->done) cudaEventDestroy(c->done);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -538,6 +541,95 @@ int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, con
     e.transposed = (flags & VPM_TRANSPOSED) != 0;
     e.self = (xt == xs) && (nt == ns);
     CK(launch_estr(e, w, c->num_sms, c->stream, &c->launches), "Estr kernels");
+    return bounded_wait(c);
+}
+
+int vpm_p2p_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
+                         const uint8_t* static_flags, double* U, double* J, double* SFS, int leaf_size,
+                         double theta, int kernel, int precision, int flags, int64_t* stats)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: n out of range");
+    if (leaf_size < 1 || leaf_size > LEAF_SIZE_MAX)
+        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: leaf_size must be in 1..%d", LEAF_SIZE_MAX);
+    if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: bad theta");
+    if (flags & ~(VPM_SFS | VPM_TRANSPOSED))
+        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: only VPM_SFS and VPM_TRANSPOSED are accepted");
+    RC(check_kernel(c, kernel, precision));
+    if (stats) stats[0] = stats[1] = stats[2] = 0;
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    const bool sfs = (flags & VPM_SFS) != 0;
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(U) ||
+        !is_device_ptr(J) || (sfs && !is_device_ptr(SFS)) || (static_flags && !is_device_ptr(static_flags)))
+        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: every array must be a device pointer");
+    // the host builds the octree and the leaf-pair list
+    std::vector<double> hx(3 * n);
+    CK(cudaMemcpyAsync(hx.data(), x, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H positions");
+    CK(cudaStreamSynchronize(c->stream), "D2H positions");
+    LeafLists L;
+    if (build_leaf_lists(n, hx.data(), leaf_size, theta, &L) != 0)
+        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: octree construction failed");
+    if (L.col.size() > (size_t)INT32_MAX)
+        return fail(c, VPM_ERR_CAPACITY, "vpm_p2p_leaflist_dev: too many leaf pairs (%zu)", L.col.size());
+    RC(grow(c, c->leaf, leaf_work_bytes(n, (int64_t)L.leaf_begin.size(), (int64_t)L.col.size()), "leaf lists"));
+    LeafArgs a;
+    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = U; a.J = J; a.SFS = SFS; a.static_flags = static_flags;
+    a.kernel = kernel; a.precision = precision; a.sfs = sfs; a.transposed = (flags & VPM_TRANSPOSED) != 0;
+    CK(launch_leaflist(a, L, c->leaf.p, c->stream, &c->launches), "leaf-list P2P kernels");
+    RC(bounded_wait(c));
+    if (stats) {
+        stats[0] = (int64_t)L.leaf_begin.size();
+        stats[1] = (int64_t)L.col.size();
+        stats[2] = L.pairs;
+    }
+    return VPM_OK;
+}
+
+int vpm_leaflist_host(int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
+                      int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes)
+{
+    if (!x || !sizes || n <= 0 || leaf_size < 1 || leaf_size > LEAF_SIZE_MAX || !(theta >= 0.0))
+        return fail(nullptr, VPM_ERR_ARG, "vpm_leaflist_host: bad arguments");
+    LeafLists L;
+    if (build_leaf_lists(n, x, leaf_size, theta, &L) != 0)
+        return fail(nullptr, VPM_ERR_ARG, "vpm_leaflist_host: octree construction failed");
+    const int64_t nl = (int64_t)L.leaf_begin.size();
+    sizes[0] = nl;
+    sizes[1] = (int64_t)L.col.size();
+    if (!perm) return VPM_OK;
+    if (!leaf_begin || !leaf_end || !row || !col) return fail(nullptr, VPM_ERR_ARG, "vpm_leaflist_host: NULL output");
+    std::memcpy(perm, L.perm.data(), n * sizeof(int32_t));
+    std::memcpy(leaf_begin, L.leaf_begin.data(), nl * sizeof(int64_t));
+    std::memcpy(leaf_end, L.leaf_end.data(), nl * sizeof(int64_t));
+    std::memcpy(row, L.row.data(), (nl + 1) * sizeof(int64_t));
+    std::memcpy(col, L.col.data(), L.col.size() * sizeof(int32_t));
+    return VPM_OK;
+}
+
+int vpm_uj_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
+                       const double* Ubar, const double* Jbar, double* xbar, double* gbar, double* sbar,
+                       int kernel, int precision)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_adjoint_dev: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: n out of range");
+    RC(check_kernel(c, kernel, precision));
+    if (precision != VPM_FP64) return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: only VPM_FP64 is implemented");
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(Ubar) ||
+        !is_device_ptr(Jbar) || !is_device_ptr(xbar) || !is_device_ptr(gbar) || !is_device_ptr(sbar))
+        return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: every array must be a device pointer");
+    Workspace w;
+    RC(ensure_work(c, n, n, VPM_FP64, false, &w));
+    AdjArgs a;
+    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.Ubar = Ubar; a.Jbar = Jbar;
+    a.xbar = xbar; a.gbar = gbar; a.sbar = sbar; a.kernel = kernel; a.precision = precision;
+    CK(launch_uj_adjoint(a, w, c->num_sms, c->stream, &c->launches), "UJ adjoint kernels");
     return bounded_wait(c);
 }
 

@@ -46,13 +46,15 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
                                 const double* __restrict__ gs, const double* __restrict__ sgs,
                                 const double* __restrict__ Js, int64_t ldJs,
                                 const uint8_t* __restrict__ static_s, bool transposed,
-                                SrcEstrMixed* __restrict__ out)
+                                const TgtPos* __restrict__ order, SrcEstrMixed* __restrict__ out)
 {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= ns_pad) return;
+    // with `order` (sources = targets) the pack follows the targets' Morton order
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= ns_pad) return;
     SrcEstrMixed p;
     p.pad = 0.f;
-    if (i < ns) {
+    if (o < ns) {
+        const int64_t i = order ? (int64_t)order[o].idx : o;
         const double isig = 1.0 / sgs[i];
         const double isig2 = isig * isig;
         p.x = xs[3 * i]; p.y = xs[3 * i + 1]; p.z = xs[3 * i + 2];
@@ -69,7 +71,7 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
         p.isig2 = 1.f;
         p.g = p.v = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    out[i] = p;
+    out[o] = p;
 }
 
 template <int K>
@@ -216,7 +218,8 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
                                        (float)(tile[j].z - oz), tile[j].isig2);
         }
         __syncwarp();
-        const int64_t jself = self ? idx - base : -1;
+        // sources follow the targets' Morton order: the self pair is source position t
+        const int64_t jself = self ? t - base : -1;
 #pragma unroll 1
         for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
             float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
@@ -274,7 +277,7 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
     } else {
         SrcEstrMixed* src = (SrcEstrMixed*)w.src_pack;
         pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
-                                                  a.transposed, src);
+                                                  a.transposed, a.self ? tgt : nullptr, src);
         estr_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
                                                           per_split, a.self, a.transposed, a.SFS, a.ldS,
                                                           partial, nt_pad);

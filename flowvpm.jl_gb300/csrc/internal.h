@@ -59,6 +59,25 @@ struct EstrArgs {
     bool transposed, self;
 };
 
+// Reverse mode of the self-induced UJ of one particle set.
+struct AdjArgs {
+    int64_t n;
+    const double* x; const double* gam; const double* sig;   // [n,3], [n,3], [n]
+    const double* Ubar; const double* Jbar;                  // [n,3], [n,9]
+    double* xbar; double* gbar; double* sbar;                // += outputs
+    int kernel, precision;
+};
+
+// Near-field P2P over octree leaf pairs (leaflist.cu).
+struct LeafArgs {
+    int64_t n;
+    const double* x; const double* gam; const double* sig;   // [n,3], [n,3], [n]
+    double* U; double* J; double* SFS;                        // += outputs, original order
+    const uint8_t* static_flags;                              // [n] or null
+    int kernel, precision;
+    bool sfs, transposed;
+};
+
 // Scratch and packing buffers supplied by the caller (the context).
 struct Workspace {
     void* src_pack; size_t src_pack_bytes;
@@ -84,5 +103,12 @@ cudaError_t launch_uj(const UJArgs& a, const Workspace& w, int num_sms, cudaStre
                       int64_t* launches);
 cudaError_t launch_estr(const EstrArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
                         int64_t* launches);
+cudaError_t launch_uj_adjoint(const AdjArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
+                              int64_t* launches);
+
+struct LeafLists;
+constexpr int LEAF_SIZE_MAX = 64;
+size_t leaf_work_bytes(int64_t n, int64_t nleaves, int64_t nleafpairs);
+cudaError_t launch_leaflist(const LeafArgs& a, const LeafLists& L, void* work, cudaStream_t st, int64_t* launches);
 
 }  // namespace vpm

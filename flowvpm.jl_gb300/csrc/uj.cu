@@ -4,8 +4,11 @@
 //
 // Layout: one target per thread, UJ_THREADS targets per block, targets in
 // Morton order (order.cu) so each warp holds 32 neighbouring targets.  Sources
-// are packed once per call and streamed through shared memory in tiles of
-// UJ_TILE.  gridDim.y splits the sources when there are too few target blocks
+// are packed once per call (in the same Morton order when they are the
+// targets).  The FP64 kernel streams them through shared memory in block-wide
+// tiles of UJ_TILE; in the mixed kernel every warp streams them on its own in
+// tiles of 32, double-buffered with cp.async, so warps never wait for one
+// another.  gridDim.y splits the sources when there are too few target blocks
 // to fill the GPU; each split then writes FP64 partial sums to scratch and
 // uj_reduce adds them, in split order, to the outputs.
 //
@@ -22,6 +25,7 @@
 // Sums run in FP32 over blocks of UJ_BLOCK sources, then in an FP32 mid-level
 // sum over UJ_FLUSH_TILES tiles, then in FP64.
 #include "internal.h"
+#include "uj_pair.cuh"
 #include "vpm_math.cuh"
 
 namespace vpm {
@@ -60,20 +64,22 @@ size_t uj_partial_bytes(int64_t nt, int nsplit)
     return nsplit > 1 ? (size_t)nsplit * 12 * (size_t)round_up(nt, UJ_THREADS) * sizeof(double) : 0;
 }
 
-// true for kernels equal to their singular form beyond some rho
-template <int K>
-__host__ __device__ constexpr bool singular_tail() { return K != K_WNKLMNS; }
 
 // ------------------------------------------------------------------ packing
+// When `order` is given (sources = targets), source i of the pack is particle
+// order[i].idx, i.e. the sources follow the targets' Morton order: a warp's
+// near sources then sit in few 4-source groups, so fewer groups take the near
+// path.  The order of a sum's terms does not otherwise matter.
 template <int K>
 __global__ void pack_src_mixed(int64_t ns, int64_t ns_pad, const double* __restrict__ xs,
                                const double* __restrict__ gs, const double* __restrict__ sgs,
-                               SrcMixed* __restrict__ out)
+                               const TgtPos* __restrict__ order, SrcMixed* __restrict__ out)
 {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= ns_pad) return;
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= ns_pad) return;
     SrcMixed p;
-    if (i < ns) {
+    if (o < ns) {
+        const int64_t i = order ? (int64_t)order[o].idx : o;
         const double x = xs[3 * i], y = xs[3 * i + 1], z = xs[3 * i + 2];
         const float xh = (float)x, yh = (float)y, zh = (float)z;
         const double sig = (K == K_SING) ? 1.0 : sgs[i];
@@ -87,7 +93,7 @@ __global__ void pack_src_mixed(int64_t ns, int64_t ns_pad, const double* __restr
         p.b = make_float4(0.f, 0.f, 0.f, 1.f);
         p.gam = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    out[i] = p;
+    out[o] = p;
 }
 
 template <int K>
@@ -149,94 +155,6 @@ __device__ __forceinline__ void pair_f64(double tx, double ty, double tz, const 
         acc[9] += a1 * dz - aux2 * gy;
         acc[10] += a2 * dz + aux2 * gx;
         acc[11] += a3 * dz;
-    }
-}
-
-// ----------------------------------------------------------- pair: mixed
-// Accumulates U += G c, W += G gam, J' += Q c_i dx_j with c = dx x gam.  The
-// trace of J' vanishes (c . dx = 0), so J'_33 is not accumulated; the caller
-// sets it to -(J'_11 + J'_22).
-__device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float G, float Q, const float4& g,
-                                           float (&u)[3], float (&jq)[8], float (&w)[3])
-{
-    const float cx = fmaf(dy, g.z, -dz * g.y);
-    const float cy = fmaf(dz, g.x, -dx * g.z);
-    const float cz = fmaf(dx, g.y, -dy * g.x);
-    u[0] = fmaf(G, cx, u[0]);
-    u[1] = fmaf(G, cy, u[1]);
-    u[2] = fmaf(G, cz, u[2]);
-    w[0] = fmaf(G, g.x, w[0]);
-    w[1] = fmaf(G, g.y, w[1]);
-    w[2] = fmaf(G, g.z, w[2]);
-    const float bx = Q * cx, by = Q * cy, bz = Q * cz;
-    jq[0] = fmaf(bx, dx, jq[0]);
-    jq[1] = fmaf(by, dx, jq[1]);
-    jq[2] = fmaf(bz, dx, jq[2]);
-    jq[3] = fmaf(bx, dy, jq[3]);
-    jq[4] = fmaf(by, dy, jq[4]);
-    jq[5] = fmaf(bz, dy, jq[5]);
-    jq[6] = fmaf(bx, dz, jq[6]);
-    jq[7] = fmaf(by, dz, jq[7]);
-}
-
-// Four sources j0..j0+3 of the tile against this lane's target.
-//   to      : target offset from the warp origin (FP32)
-//   th, tl  : target double-float position
-//   r2n     : (2 b)^2, b = the warp's extent around its origin
-template <int K>
-__device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, const float3& tl, float r2n,
-                                            const float4* __restrict__ off, const SrcMixed* __restrict__ tile,
-                                            int j0, float (&u)[3], float (&jq)[8], float (&w)[3])
-{
-    float dx[4], dy[4], dz[4], r2[4], hw[4];
-    bool far = true;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        const float4 h = off[j0 + q];
-        dx[q] = to.x - h.x;
-        dy[q] = to.y - h.y;
-        dz[q] = to.z - h.z;
-        r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
-        hw[q] = h.w;
-        far = far && (r2[q] > (singular_tail<K>() ? h.w : r2n));
-    }
-    if (__all_sync(0xffffffffu, far)) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            float G, Q;
-            if constexpr (singular_tail<K>()) {
-                const float rs = rsqrtf(r2[q]);
-                const float rs2 = rs * rs;
-                G = rs * rs2;
-                Q = G * rs2;
-            } else {
-                near_GQ<K>(r2[q] * hw[q], hw[q], G, Q);
-            }
-            accum_pair(dx[q], dy[q], dz[q], G, Q, tile[j0 + q].gam, u, jq, w);
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const float4 a = tile[j0 + q].a, b = tile[j0 + q].b;
-            const float ex = (th.x - a.x) + (tl.x - b.x);
-            const float ey = (th.y - a.y) + (tl.y - b.y);
-            const float ez = (th.z - a.z) + (tl.z - b.z);
-            const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-            float G, Q;
-            if constexpr (singular_tail<K>()) {
-                const float isig2 = b.w * b.w;
-                near_GQ<K>(e2 * isig2, isig2, G, Q);
-                const float isig3 = isig2 * b.w;
-                G *= isig3;
-                Q *= isig3;
-            } else {
-                near_GQ<K>(e2 * hw[q], hw[q], G, Q);
-            }
-            const bool nz = e2 > 0.0f;
-            G = nz ? G : 0.0f;
-            Q = nz ? Q : 0.0f;
-            accum_pair(ex, ey, ez, G, Q, tile[j0 + q].gam, u, jq, w);
-        }
     }
 }
 
@@ -302,14 +220,33 @@ uj_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad, const 
     if (valid) write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
 
+// 16-byte asynchronous global->shared copy (LDGSTS), L2-cached.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int WT = 32;                      // sources per warp tile (one per lane)
+constexpr int BLOCK_TILES = UJ_BLOCK / WT;  // warp tiles per FP32 block
+constexpr int MID_BLOCKS = 4;               // FP32 blocks per FP32 mid-level sum
+#ifndef VPM_UJ_MIN_BLOCKS
+#define VPM_UJ_MIN_BLOCKS 5                 // resident blocks per SM the register budget targets
+#endif
+
+// Each warp streams the sources on its own: 32 per tile, double-buffered with
+// cp.async, so warps never wait for each other (no block-wide barrier).
 template <int K>
-__global__ void __launch_bounds__(UJ_THREADS)
+__global__ void __launch_bounds__(UJ_THREADS, VPM_UJ_MIN_BLOCKS)
 uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
                 const SrcMixed* __restrict__ src, int64_t per_split, double* U, int64_t ldU,
                 double* J, int64_t ldJ, double* partial, int64_t nt_pad)
 {
-    __shared__ SrcMixed tile[UJ_TILE];
-    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    __shared__ SrcMixed stage[UJ_WARPS][2][WT];
+    __shared__ float4 offs[UJ_WARPS][2][WT];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const bool valid = t < nt;
@@ -343,47 +280,67 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
 #pragma unroll
     for (int k = 0; k < 8; k++) dJ[k] = 0.0;
     float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
+    float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) mj[k] = 0.f;
-    int tiles_in_mid = 0;
+    for (int k = 0; k < 8; k++) { mj[k] = 0.f; jq[k] = 0.f; }
+
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
-    for (int64_t base = s0; base < s1; base += UJ_TILE) {
-        __syncthreads();
-        tile[threadIdx.x] = src[base + threadIdx.x];
-        __syncthreads();
-        // this warp's FP32 offsets of the tile's sources and their far thresholds
-#pragma unroll
-        for (int q = 0; q < UJ_TILE / 32; q++) {
-            const int j = lane + 32 * q;
-            const float4 a = tile[j].a, b = tile[j].b;
-            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : b.w * b.w;
-            off[warp][j] = make_float4((a.x - oh.x) + (b.x - ol.x), (a.y - oh.y) + (b.y - ol.y),
-                                       (a.z - oh.z) + (b.z - ol.z), thr);
+    const int ntiles = (int)((s1 - s0) / WT);
+    const SrcMixed* wsrc = src + s0 + lane;
+    if (ntiles > 0) {
+        SrcMixed* d = &stage[warp][0][lane];
+        cp_async16(&d->a, &wsrc->a);
+        cp_async16(&d->b, &wsrc->b);
+        cp_async16(&d->gam, &wsrc->gam);
+        cp_async_commit();
+    }
+    int in_block = 0, in_mid = 0;
+    for (int it = 0; it < ntiles; it++) {
+        const int buf = it & 1;
+        if (it + 1 < ntiles) {
+            const SrcMixed* g = wsrc + (int64_t)(it + 1) * WT;
+            SrcMixed* d = &stage[warp][buf ^ 1][lane];
+            cp_async16(&d->a, &g->a);
+            cp_async16(&d->b, &g->b);
+            cp_async16(&d->gam, &g->gam);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncwarp();
-#pragma unroll 1
-        for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
-            float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f};
-            float jq[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++) jq[k] = 0.f;
+        {   // this lane's source: FP32 offset from the warp origin and its far threshold
+            const float4 a = stage[warp][buf][lane].a, b = stage[warp][buf][lane].b;
+            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : b.w * b.w;
+            offs[warp][buf][lane] = make_float4((a.x - oh.x) + (b.x - ol.x), (a.y - oh.y) + (b.y - ol.y),
+                                                (a.z - oh.z) + (b.z - ol.z), thr);
+        }
+        __syncwarp();
 #pragma unroll 2
-            for (int j = 0; j < UJ_BLOCK; j += 4)
-                pair4_mixed<K>(to, th, tl, r2n, off[warp], tile, sb + j, u, jq, w);
+        for (int j = 0; j < WT; j += 4)
+            pair4_mixed<K>(to, th, tl, r2n, offs[warp][buf], stage[warp][buf], j, u, jq, w);
+        if (++in_block == BLOCK_TILES) {
 #pragma unroll
-            for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; }
+            for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }
 #pragma unroll
-            for (int k = 0; k < 8; k++) mj[k] += jq[k];
+            for (int k = 0; k < 8; k++) { mj[k] += jq[k]; jq[k] = 0.f; }
+            in_block = 0;
+            if (++in_mid == MID_BLOCKS) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
+#pragma unroll
+                for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
+                in_mid = 0;
+            }
         }
-        if (++tiles_in_mid == UJ_FLUSH_TILES || base + UJ_TILE >= s1) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
-#pragma unroll
-            for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
-            tiles_in_mid = 0;
-        }
+        __syncwarp();   // every lane is done with `buf` before it is refilled
     }
+    // remaining partial block and mid-level sums
+#pragma unroll
+    for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k] + (double)u[k]; dW[k] += (double)mw[k] + (double)w[k]; }
+#pragma unroll
+    for (int k = 0; k < 8; k++) dJ[k] += (double)mj[k] + (double)jq[k];
     if (!valid) return;
     // J = -3 J' (J'_33 = -J'_11 - J'_22) plus the Kronecker term of
     // src/FLOWVPM_fmm.jl:148-159 (W = sum aux2 Gamma)
@@ -400,7 +357,6 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     double acc[12] = {dU[0], dU[1], dU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
     write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
-
 // --------------------------------------------------------------- launcher
 template <int K>
 static cudaError_t launch_uj_k(const UJArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
@@ -424,7 +380,8 @@ static cudaError_t launch_uj_k(const UJArgs& a, const Workspace& w, int num_sms,
                                                        a.J, a.ldJ, partial, nt_pad);
     } else {
         SrcMixed* src = (SrcMixed*)w.src_pack;
-        pack_src_mixed<K><<<(unsigned)((ns_pad + pb - 1) / pb), pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, src);
+        pack_src_mixed<K><<<(unsigned)((ns_pad + pb - 1) / pb), pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs,
+                                                                             a.self ? tgt : nullptr, src);
         uj_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
                                                          a.J, a.ldJ, partial, nt_pad);
     }

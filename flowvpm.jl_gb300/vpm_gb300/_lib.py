@@ -13,7 +13,7 @@ import threading
 import numpy as np
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG_ROOT, "lib", "libvpm_gb300.so")
+LIB_PATH = os.environ.get("VPM_GB300_LIB", os.path.join(PKG_ROOT, "lib", "libvpm_gb300.so"))
 
 # status codes, kernels, precisions and flags of include/vpm_gb300.h
 OK, ERR_ARG, ERR_CAPACITY, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NODEVICE, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
@@ -48,7 +48,32 @@ SIGNATURES = {
     "vpm_uj_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int]),
     "vpm_estr_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int]),
     "vpm_uj_dev_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp]),
+    "vpm_uj_adjoint_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int]),
+    "vpm_p2p_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int,
+                                    _vp]),
+    "vpm_leaflist_host": (_int, [_i64, _vp, _int, _dbl, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
+
+
+def leaflist_host(x: np.ndarray, leaf_size: int = 64, theta: float = 0.4):
+    """The octree leaf-pair lists of vpm_p2p_leaflist_dev (host only):
+    (perm, leaf_begin, leaf_end, row, col)."""
+    L = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n = x.shape[0]
+    sizes = np.zeros(2, dtype=np.int64)
+    rc = L.vpm_leaflist_host(n, x.ctypes.data, int(leaf_size), float(theta), None, None, None, None, None,
+                             sizes.ctypes.data)
+    if rc != OK:
+        raise VPMError(rc, L.vpm_last_error(None).decode())
+    nl, nc = int(sizes[0]), int(sizes[1])
+    perm = np.zeros(n, np.int32); lb = np.zeros(nl, np.int64); le = np.zeros(nl, np.int64)
+    row = np.zeros(nl + 1, np.int64); col = np.zeros(nc, np.int32)
+    rc = L.vpm_leaflist_host(n, x.ctypes.data, int(leaf_size), float(theta), perm.ctypes.data, lb.ctypes.data,
+                             le.ctypes.data, row.ctypes.data, col.ctypes.data, sizes.ctypes.data)
+    if rc != OK:
+        raise VPMError(rc, L.vpm_last_error(None).decode())
+    return perm, lb, le, row, col
 NOALLOC_SCRATCH_BYTES = 64 << 20   # VPM_NOALLOC_SCRATCH_BYTES
 
 
@@ -163,6 +188,32 @@ class Context:
         self._torch_stream()
         self._check(self._L.vpm_uj_dev(self._h, xt.shape[0], _ptr(xt), xs.shape[0], _ptr(xs), _ptr(gs),
                                        _ptr(sgs), _ptr(U), _ptr(J), int(kernel), int(precision)))
+
+    def uj_adjoint_dev(self, x, gam, sig, Ubar, Jbar, xbar, gbar, sbar, kernel: int, precision: int = FP64):
+        """xbar += dL/dx, gbar += dL/dGamma, sbar += dL/dsigma for dL/dU = Ubar, dL/dJ = Jbar."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(Ubar, 3); _check_dev(Jbar, 9)
+        _check_dev(xbar, 3); _check_dev(gbar, 3); _check_dev(sbar, 1)
+        self._torch_stream()
+        self._check(self._L.vpm_uj_adjoint_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(Ubar),
+                                               _ptr(Jbar), _ptr(xbar), _ptr(gbar), _ptr(sbar), int(kernel),
+                                               int(precision)))
+
+    def p2p_leaflist_dev(self, x, gam, sig, U, J, sfs_out=None, *, leaf_size: int = 64, theta: float = 0.4,
+                         kernel: int = KERNEL_GAUSSIANERF, precision: int = FP32COMP, sfs: bool = False,
+                         transposed: bool = True, static=None):
+        """Near-field P2P (UJ, and Estr into sfs_out with sfs=True) over octree leaf pairs;
+        returns (leaves, leaf pairs, particle pairs)."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(U, 3); _check_dev(J, 9)
+        if sfs:
+            _check_dev(sfs_out, 3)
+        self._torch_stream()
+        stats = np.zeros(3, dtype=np.int64)
+        flags = (SFS if sfs else 0) | (TRANSPOSED if transposed else 0)
+        self._check(self._L.vpm_p2p_leaflist_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(static),
+                                                 _ptr(U), _ptr(J), _ptr(sfs_out) if sfs else None, int(leaf_size),
+                                                 float(theta), int(kernel), int(precision), flags,
+                                                 stats.ctypes.data))
+        return tuple(int(v) for v in stats)
 
     def estr_dev(self, xt, Jt, xs, gs, sgs, Js, SFS, kernel: int, precision: int, transposed: bool = True,
                  static_t=None, static_s=None):

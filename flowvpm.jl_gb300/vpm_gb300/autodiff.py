@@ -1,0 +1,118 @@
+"""Reverse-mode differentiation through UJ and the rVPM time step.
+
+`UJFunction` is the torch.autograd.Function over the two C entry points
+`vpm_uj_dev` (forward) and `vpm_uj_adjoint_dev` (backward, the hand-written
+FP64 adjoint kernel).  It plays the role of the ChainRulesCore `rrule` that
+src/FLOWVPM_rrules.jl:179-330 sketches but never wires in; a Julia binding
+would wrap the same two calls in an rrule.
+
+`rk3_step` is the reference's rVPM low-storage RK3 step
+(src/FLOWVPM_timeintegration.jl:388-532, no SFS, inviscid, no freestream)
+with Pedrizzetti relaxation (src/FLOWVPM_relaxation.jl:62-81), written with
+torch tensor operations on device-resident state so autograd can run through
+it; every particle-to-particle evaluation goes through `UJFunction`.
+`rollout` chains steps with per-step checkpointing: only each step's input
+state is kept, and the step's forward (including its UJ evaluations) is
+recomputed during the backward pass.
+"""
+from __future__ import annotations
+
+import torch
+import torch.utils.checkpoint as ckpt
+
+from . import _lib
+
+STAGES = ((0.0, 1 / 3), (-5 / 9, 15 / 16), (-153 / 128, 8 / 15))
+
+
+class UJFunction(torch.autograd.Function):
+    """(U[n,3], J[n,9]) of one particle set (x[n,3], gamma[n,3], sigma[n]), float64 CUDA tensors."""
+
+    @staticmethod
+    def forward(ctx, x, gam, sig, kernel: int, precision: int, vctx: _lib.Context):
+        x, gam, sig = x.contiguous(), gam.contiguous(), sig.contiguous()
+        n = x.shape[0]
+        U = torch.zeros(n, 3, dtype=torch.float64, device=x.device)
+        J = torch.zeros(n, 9, dtype=torch.float64, device=x.device)
+        vctx.uj_dev(x, x, gam, sig, U, J, kernel, precision)
+        ctx.save_for_backward(x, gam, sig)
+        ctx.kernel = kernel
+        ctx.vctx = vctx
+        return U, J
+
+    @staticmethod
+    def backward(ctx, Ubar, Jbar):
+        x, gam, sig = ctx.saved_tensors
+        n = x.shape[0]
+        Ubar = torch.zeros(n, 3, dtype=torch.float64, device=x.device) if Ubar is None else Ubar.contiguous()
+        Jbar = torch.zeros(n, 9, dtype=torch.float64, device=x.device) if Jbar is None else Jbar.contiguous()
+        xb = torch.zeros_like(x)
+        gb = torch.zeros_like(gam)
+        sb = torch.zeros_like(sig)
+        ctx.vctx.uj_adjoint_dev(x, gam, sig, Ubar, Jbar, xb, gb, sb, ctx.kernel, _lib.FP64)
+        return xb, gb, sb, None, None, None
+
+
+def uj(x, gam, sig, kernel: int, precision: int = _lib.FP64, vctx: _lib.Context | None = None):
+    return UJFunction.apply(x, gam, sig, kernel, precision, vctx or _lib.default_context())
+
+
+def _stretch(J, G, transposed: bool = True):
+    """(Gamma . grad')U or (Gamma . grad)U from J[n,9] (column-major 3x3 per particle)."""
+    Jm = J.view(-1, 3, 3)                      # Jm[:, j, i] = J[i + 3j] = du_i/dx_j
+    if transposed:
+        return torch.einsum("nki,ni->nk", Jm, G)   # S_k = sum_i du_i/dx_k G_i
+    return torch.einsum("nji,nj->ni", Jm, G)       # S_i = sum_j du_i/dx_j G_j
+
+
+def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64, f: float = 0.0,
+             g: float = 0.2, relax: bool = True, rlxf: float = 0.3, transposed: bool = True,
+             vctx: _lib.Context | None = None):
+    """One rVPM RK3 step (+ Pedrizzetti relaxation) on device tensors; differentiable."""
+    vctx = vctx or _lib.default_context()
+    M0 = torch.zeros_like(x)
+    M3 = torch.zeros_like(gam)
+    M8 = torch.zeros_like(sig)
+    for a, b in STAGES:
+        U, J = UJFunction.apply(x, gam, sig, kernel, precision, vctx)
+        M0 = a * M0 + dt * U
+        x = x + b * M0
+        MM = _stretch(J, gam, transposed)
+        Gn2 = (gam * gam).sum(1)
+        pos = Gn2 > 0
+        MM4 = torch.where(pos, (f + g) / (1 + 3 * f) * (MM * gam).sum(1) / torch.where(pos, Gn2, 1.0),
+                          torch.zeros_like(Gn2))
+        M3 = a * M3 + dt * (MM - 3 * MM4[:, None] * gam)
+        M8 = a * M8 - dt * (sig * MM4)
+        gam = gam + b * M3
+        sig = sig + b * M8
+    if relax:
+        U, J = UJFunction.apply(x, gam, sig, kernel, precision, vctx)
+        w = torch.stack([J[:, 5] - J[:, 7], J[:, 6] - J[:, 2], J[:, 1] - J[:, 3]], dim=1)
+        nw = torch.sqrt((w * w).sum(1))
+        nG = torch.sqrt((gam * gam).sum(1))
+        ok = nw != 0
+        newg = (1 - rlxf) * gam + rlxf * (nG / torch.where(ok, nw, 1.0))[:, None] * w
+        gam = torch.where(ok[:, None], newg, gam)
+    return x, gam, sig
+
+
+def rollout(x, gam, sig, dt: float, nsteps: int, *, checkpoint: bool = True, **kw):
+    """nsteps of rk3_step; with checkpoint=True each step's internals are recomputed in backward."""
+    for _ in range(nsteps):
+        if checkpoint:
+            x, gam, sig = ckpt.checkpoint(lambda a, b, c: rk3_step(a, b, c, dt, **kw), x, gam, sig,
+                                          use_reentrant=False)
+        else:
+            x, gam, sig = rk3_step(x, gam, sig, dt, **kw)
+    return x, gam, sig
+
+
+def ring_loss(x, gam, sig, *, kernel: int, precision: int = _lib.FP64, vctx: _lib.Context | None = None):
+    """Kinetic-energy estimate E = 1/2 sum U_p . (x_p x Gamma_p) plus the
+    strength-weighted axial centroid sum |Gamma_p| z_p / sum |Gamma_p|."""
+    U, _ = UJFunction.apply(x, gam, sig, kernel, precision, vctx or _lib.default_context())
+    E = 0.5 * (U * torch.cross(x, gam, dim=1)).sum()
+    nG = torch.sqrt((gam * gam).sum(1))
+    Z = (nG * x[:, 2]).sum() / nG.sum()
+    return E + Z

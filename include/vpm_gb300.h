@@ -154,6 +154,40 @@ int vpm_estr_dev(vpm_ctx* ctx, int64_t nt, const double* xt, const double* Jt,
                  const double* Js, const uint8_t* static_s,
                  double* SFS, int kernel, int precision, int flags);
 
+/* Reverse mode of the self-induced UJ of one particle set (targets = sources):
+ * given Ubar[n,3] = dL/dU and Jbar[n,9] = dL/dJ, adds dL/dx to xbar[n,3],
+ * dL/dGamma to gbar[n,3] and dL/dsigma to sbar[n] (device pointers).
+ * Replaces the unwired ChainRules rrule of src/FLOWVPM_rrules.jl:179-330 (the
+ * pullback of U and J with respect to positions, strengths and core sizes).
+ * precision must be VPM_FP64.  Source-side sums are added with atomics, so
+ * their summation order (last bits) may differ between runs. */
+int vpm_uj_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                       const double* Ubar, const double* Jbar, double* xbar, double* gbar,
+                       double* sbar, int kernel, int precision);
+
+/* Near-field leg of UJ_fmm (src/FLOWVPM_UJ.jl:90-125): builds an octree of the
+ * n particles on the host (leaves of at most leaf_size <= 64 particles) and
+ * adds U[n,3], J[n,9] -- and, with VPM_SFS, Estr into SFS[n,3] -- from the
+ * direct P2P of every leaf pair that fails the multipole acceptance criterion
+ * theta * r < R1 + R2 (r: distance of the cell centres, R: cell radii;
+ * src/FLOWVPM_particlefield.jl:28-36), as FastMultipole's direct_list does.
+ * The far field is not computed.  flags: VPM_SFS, VPM_TRANSPOSED.  Device
+ * pointers; static_flags may be NULL.  stats (may be NULL) receives
+ * {leaves, leaf pairs, particle pairs}. */
+int vpm_p2p_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                         const uint8_t* static_flags, double* U, double* J, double* SFS,
+                         int leaf_size, double theta, int kernel, int precision, int flags,
+                         int64_t* stats);
+
+/* The octree leaf-pair lists vpm_p2p_leaflist_dev builds (host memory, no GPU).
+ * Call once with perm == NULL to get sizes[0] = leaves, sizes[1] = leaf pairs;
+ * then with perm[n], leaf_begin[leaves], leaf_end[leaves], row[leaves+1],
+ * col[leaf pairs]: particle i of the tree order is perm[i], leaf l holds tree
+ * positions [leaf_begin[l], leaf_end[l]), and its source leaves are
+ * col[row[l] .. row[l+1]). */
+int vpm_leaflist_host(int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
+                      int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes);
+
 /* ------------------------------------------------ allocation-free variant */
 
 /* Size of the static device scratch array behind vpm_uj_dev_noalloc (64 MiB). */

@@ -85,6 +85,9 @@ def lib():
                                                     ctypes.c_double, ctypes.c_double,
                                                     ctypes.c_double, ctypes.c_int]
         L.oracle_relax.argtypes = [_dp, _i64, _i64, ctypes.c_double, ctypes.c_int]
+        L.oracle_uj_adjoint.argtypes = [_i64, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                        ctypes.c_int]
+        L.oracle_g_d1_d2.argtypes = [ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]
         L.oracle_rk3_step.restype = ctypes.c_int
         L.oracle_rk3_step.argtypes = [_dp, _i64, _i64, ctypes.c_double, ctypes.c_int,
                                       ctypes.POINTER(StepParams)]
@@ -153,6 +156,23 @@ def estr_pairs(xt, Jt, xs, gs, sgs, Js, kernel: int, transposed: bool = True,
                             None if ss is None else ss.ctypes.data_as(_u8p),
                             _p(S), int(kernel), int(bool(transposed)), int(nthreads))
     return S[t0:t1]
+
+
+def uj_adjoint(x, gam, sig, Ubar, Jbar, kernel: int, nthreads: int = 0):
+    """(xbar[n,3], gbar[n,3], sbar[n]) = gradients of sum(Ubar*U) + sum(Jbar*J) for the
+    self-induced U, J of one particle set."""
+    x, gam, sig, Ubar, Jbar = map(_c, (x, gam, sig, Ubar, Jbar))
+    n = x.shape[0]
+    xb = np.zeros((n, 3)); gb = np.zeros((n, 3)); sb = np.zeros(n)
+    lib().oracle_uj_adjoint(n, _p(x), _p(gam), _p(sig), _p(Ubar), _p(Jbar), _p(xb), _p(gb), _p(sb),
+                            int(kernel), int(nthreads))
+    return xb, gb, sb
+
+
+def g_d1_d2(kernel: int, rho: float):
+    g, d1, d2 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    lib().oracle_g_d1_d2(int(kernel), float(rho), ctypes.byref(g), ctypes.byref(d1), ctypes.byref(d2))
+    return g.value, d1.value, d2.value
 
 
 def update_particle_states(particles, np_, a, b, dt, Uinf, f, g, zeta0, transposed=True):

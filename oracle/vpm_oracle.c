@@ -215,6 +215,110 @@ void oracle_uj_pairs(int64_t t0, int64_t t1, const double* xt,
     }
 }
 
+/* -------------------------------------------------------------- adjoint
+ * g, g' = dg/drho and g'' of each kernel (derivatives of src/FLOWVPM_kernel.jl:45-84). */
+void oracle_g_d1_d2(int kernel, double rho, double* g, double* d1, double* d2)
+{
+    switch (kernel) {
+    case VPM_KERNEL_SINGULAR: *g = 1; *d1 = 0; *d2 = 0; break;
+    case VPM_KERNEL_GAUSSIAN: {
+        const double e = exp(-rho * rho * rho);
+        *g = 1 - e; *d1 = 3 * rho * rho * e; *d2 = (6 * rho - 9 * rho * rho * rho * rho) * e; break;
+    }
+    case VPM_KERNEL_GAUSSIANERF: {
+        const double e = exp(-rho * rho / 2);
+        *g = erf(rho / sqr2) - const2 * rho * e;
+        *d1 = const2 * rho * rho * e;
+        *d2 = const2 * (2 * rho - rho * rho * rho) * e;
+        break;
+    }
+    case VPM_KERNEL_WINCKELMANS: {
+        const double q = rho * rho + 1;
+        *g = rho * rho * rho * (rho * rho + 2.5) / pow(q, 2.5);
+        *d1 = 7.5 * rho * rho / pow(q, 3.5);
+        *d2 = 7.5 * rho * (2 - 5 * rho * rho) / pow(q, 4.5);
+        break;
+    }
+    default: *g = *d1 = *d2 = NAN;
+    }
+}
+
+/* Derivatives of phi = Ubar.u + Jbar:j for one pair (u, j of src/FLOWVPM_fmm.jl:112-160)
+ * with respect to dx = x_t - x_s (out[0..2]), Gamma_s (out[3..5]) and sigma_s (out[6]).
+ * With q(r) = -g(rho)/(4 pi r^3), A = q, B = q'/r, c = dx x Gamma:
+ *   u = A c,   j_ab = B c_a dx_b + A eps_abl Gamma_l,
+ *   phi = A P + B Q,  P = Ubar.c + wbar.Gamma,  Q = c.(Jbar dx),
+ * wbar_l = eps_abl Jbar_ab. */
+static void adj_pair(const double* dx, const double* G, double sigma, const double* Ub, const double* Jb,
+                     int kernel, double* out)
+{
+    const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    for (int k = 0; k < 7; k++) out[k] = 0;
+    if (r2 == 0) return;
+    const double r = sqrt(r2), rho = r / sigma;
+    double g, g1, g2;
+    oracle_g_d1_d2(kernel, rho, &g, &g1, &g2);
+    const double r3 = r2 * r, r4 = r2 * r2, r5 = r4 * r;
+    const double A = -const4 * g / r3;
+    const double B = -const4 * (g1 / (sigma * r4) - 3 * g / r5);
+    const double qpp = -const4 * (g2 / (sigma * sigma * r3) - 6 * g1 / (sigma * r4) + 12 * g / r5);
+    const double Bpr = (qpp - B) / r2;                                  /* B'(r)/r */
+    const double dA_ds = const4 * g1 * rho / (sigma * r3);
+    const double dB_ds = -const4 * (2 * g1 - rho * g2) / (sigma * sigma * r4);
+    double c[3] = {dx[1] * G[2] - dx[2] * G[1], dx[2] * G[0] - dx[0] * G[2], dx[0] * G[1] - dx[1] * G[0]};
+    /* Jbar[a + 3b] = dL/dJ_ab ; JD = Jbar dx ; JTc = Jbar^T c */
+    double JD[3], JTc[3];
+    for (int a = 0; a < 3; a++) {
+        JD[a] = Jb[a] * dx[0] + Jb[a + 3] * dx[1] + Jb[a + 6] * dx[2];
+        JTc[a] = Jb[3 * a] * c[0] + Jb[3 * a + 1] * c[1] + Jb[3 * a + 2] * c[2];
+    }
+    const double wb[3] = {Jb[1 + 3 * 2] - Jb[2 + 3 * 1], Jb[2 + 3 * 0] - Jb[0 + 3 * 2], Jb[0 + 3 * 1] - Jb[1 + 3 * 0]};
+    const double P = Ub[0] * c[0] + Ub[1] * c[1] + Ub[2] * c[2] + wb[0] * G[0] + wb[1] * G[1] + wb[2] * G[2];
+    const double Q = c[0] * JD[0] + c[1] * JD[1] + c[2] * JD[2];
+    /* dphi/d(dx) */
+    const double s = B * P + Bpr * Q;
+    const double GxU[3] = {G[1] * Ub[2] - G[2] * Ub[1], G[2] * Ub[0] - G[0] * Ub[2], G[0] * Ub[1] - G[1] * Ub[0]};
+    const double GxJD[3] = {G[1] * JD[2] - G[2] * JD[1], G[2] * JD[0] - G[0] * JD[2], G[0] * JD[1] - G[1] * JD[0]};
+    for (int k = 0; k < 3; k++) out[k] = s * dx[k] + A * GxU[k] + B * (GxJD[k] + JTc[k]);
+    /* dphi/dGamma = A (Ubar x dx + wbar) + B (JD x dx) */
+    const double Uxd[3] = {Ub[1] * dx[2] - Ub[2] * dx[1], Ub[2] * dx[0] - Ub[0] * dx[2], Ub[0] * dx[1] - Ub[1] * dx[0]};
+    const double JDxd[3] = {JD[1] * dx[2] - JD[2] * dx[1], JD[2] * dx[0] - JD[0] * dx[2], JD[0] * dx[1] - JD[1] * dx[0]};
+    for (int k = 0; k < 3; k++) out[3 + k] = A * (Uxd[k] + wb[k]) + B * JDxd[k];
+    out[6] = dA_ds * P + dB_ds * Q;
+}
+
+void oracle_uj_adjoint(int64_t n, const double* x, const double* gam, const double* sig,
+                       const double* Ubar, const double* Jbar, double* xbar, double* gbar,
+                       double* sbar, int kernel, int nthreads)
+{
+    int nth = set_threads(nthreads);
+    (void)nth;
+    const int sing = kernel == VPM_KERNEL_SINGULAR;
+    /* target side: xbar_t += sum_s dphi/d(dx) */
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth)
+    for (int64_t t = 0; t < n; t++) {
+        double acc[3] = {0, 0, 0}, o[7];
+        for (int64_t s = 0; s < n; s++) {
+            const double dx[3] = {x[3 * t] - x[3 * s], x[3 * t + 1] - x[3 * s + 1], x[3 * t + 2] - x[3 * s + 2]};
+            adj_pair(dx, gam + 3 * s, sing ? 1.0 : sig[s], Ubar + 3 * t, Jbar + 9 * t, kernel, o);
+            for (int k = 0; k < 3; k++) acc[k] += o[k];
+        }
+        for (int k = 0; k < 3; k++) xbar[3 * t + k] += acc[k];
+    }
+    /* source side: xbar_s -= sum_t dphi/d(dx), gbar_s, sbar_s */
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth)
+    for (int64_t s = 0; s < n; s++) {
+        double acc[7] = {0, 0, 0, 0, 0, 0, 0}, o[7];
+        for (int64_t t = 0; t < n; t++) {
+            const double dx[3] = {x[3 * t] - x[3 * s], x[3 * t + 1] - x[3 * s + 1], x[3 * t + 2] - x[3 * s + 2]};
+            adj_pair(dx, gam + 3 * s, sing ? 1.0 : sig[s], Ubar + 3 * t, Jbar + 9 * t, kernel, o);
+            for (int k = 0; k < 7; k++) acc[k] += o[k];
+        }
+        for (int k = 0; k < 3; k++) { xbar[3 * s + k] -= acc[k]; gbar[3 * s + k] += acc[3 + k]; }
+        if (!sing) sbar[s] += acc[6];
+    }
+}
+
 /* ----------------------------------------------------------------- Estr
  * Estr_direct (src/FLOWVPM_subfilterscale_models.jl:16-41) inside the driver
  * loop of :61-74: non-static targets, non-static sources in index order. */

@@ -58,6 +58,19 @@ void oracle_estr_pairs(int64_t t0, int64_t t1, const double* xt, const double* J
                        const double* Js, const uint8_t* static_s,
                        double* SFS, int kernel, int transposed, int nthreads);
 
+/* Reverse mode of oracle_uj_pairs over one particle set (targets = sources,
+ * pairs with r^2 == 0 skipped): given Ubar[n*3] = dL/dU and Jbar[n*9] = dL/dJ,
+ * adds dL/dx to xbar[n*3], dL/dGamma to gbar[n*3] and dL/dsigma to sbar[n].
+ * The per-pair derivative follows from differentiating src/FLOWVPM_fmm.jl:112-160
+ * (it replaces the unwired rrule of src/FLOWVPM_rrules.jl:179-330), with the
+ * kernels' second derivatives g''(rho).  FP64, targets in parallel, sources in
+ * index order; source-side sums are accumulated per source in target order. */
+void oracle_uj_adjoint(int64_t n, const double* x, const double* gam, const double* sig,
+                       const double* Ubar, const double* Jbar, double* xbar, double* gbar,
+                       double* sbar, int kernel, int nthreads);
+/* (g, g', g'') of a kernel at rho (libm erf). */
+void oracle_g_d1_d2(int kernel, double rho, double* g, double* d1, double* d2);
+
 /* ---------------------------------------------- consumers of UJ (per particle) */
 
 /* update_particle_states, rVPM low-storage RK stage,

@@ -1,0 +1,46 @@
+"""The oracle's UJ adjoint (oracle_uj_adjoint) against central finite
+differences of the oracle's FP64 forward (CPU only).  This checks the per-pair
+derivative used by the GPU adjoint kernel: L = sum(Ubar*U) + sum(Jbar*J)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+
+
+def _loss(x, g, s, Ub, Jb, k):
+    U, J = oracle.uj_pairs(x, x, g, s, k)
+    return float((Ub * U).sum() + (Jb * J).sum())
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+def test_adjoint_matches_central_differences(k):
+    rng = np.random.default_rng(10 + k)
+    n = 14
+    x = rng.uniform(0, 0.12, (n, 3))
+    g = rng.normal(0, 1.0, (n, 3))
+    s = rng.uniform(0.03, 0.06, n)
+    Ub = rng.normal(size=(n, 3))
+    Jb = rng.normal(size=(n, 9))
+    xb, gb, sb = oracle.uj_adjoint(x, g, s, Ub, Jb, k)
+    h = 1e-6
+    for trial in range(6):
+        dx = rng.normal(size=x.shape)
+        dg = rng.normal(size=g.shape)
+        ds = rng.normal(size=s.shape) * (0 if k == 0 else 1)
+        # scale so each perturbation moves the inputs by ~h relative
+        fd = (_loss(x + h * dx, g + h * dg, s + h * 0.05 * ds, Ub, Jb, k)
+              - _loss(x - h * dx, g - h * dg, s - h * 0.05 * ds, Ub, Jb, k)) / (2 * h)
+        an = (xb * dx).sum() + (gb * dg).sum() + 0.05 * (sb * ds).sum()
+        assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (trial, fd, an)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_kernel_second_derivative(k):
+    for rho in (0.2, 0.9, 1.6, 2.5):
+        g, d1, d2 = oracle.g_d1_d2(k, rho)
+        h = 1e-5
+        fd = (oracle.g_d1_d2(k, rho + h)[1] - oracle.g_d1_d2(k, rho - h)[1]) / (2 * h)
+        assert abs(fd - d2) <= 1e-7 * max(1.0, abs(d2))
+        assert abs(g - oracle.g_dgdr(k, rho)[0]) <= 1e-15 and abs(d1 - oracle.g_dgdr(k, rho)[1]) <= 1e-15
