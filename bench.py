@@ -409,6 +409,216 @@ def run_kernel_only(args):
                       "launches": ctx.launches}))
 
 
+def _device_field(X, G, s, precision, torch, ds):
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    return ds.DeviceField(d(X), d(G), d(s), kernel=KERNEL, precision=precision)
+
+
+def _leapfrog_run(ctx, X, G, s, precision, nsteps, dt, monitor_every, torch, ds, with_sfs=True):
+    """nsteps device-resident RK3 steps with dynamic SFS (with_sfs), core
+    spreading and relaxation; impulse and energy (fresh UJ) every
+    `monitor_every` steps.  Returns (ms per step, monitor rows [(step, t, I, E)], field)."""
+    fld = _device_field(X, G, s, precision, torch, ds)
+    sfs = ds.DynamicSFSParams() if with_sfs else None
+    visc = ds.CoreSpreadingParams(nu=1e-4, sgm0=0.05)
+    mon = []
+
+    def monitor(k):
+        ds.uj(fld, ctx)
+        mon.append((k, fld.t, ds.impulse(fld).cpu().numpy().tolist(), ds.energy(fld)))
+    monitor(0)
+    step_ms = 0.0
+    for k in range(1, nsteps + 1):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        ds.rk3_step(fld, dt, ctx, sfs=sfs, viscous=visc, relax_rlxf=0.3)
+        b.record()
+        torch.cuda.synchronize()
+        step_ms += a.elapsed_time(b)
+        if k % monitor_every == 0 or k == nsteps:
+            monitor(k)
+    return step_ms / nsteps, mon, fld
+
+
+def _drift(mon):
+    I0, E0 = np.array(mon[0][2]), mon[0][3]
+    return {"impulse_rel_drift": float(np.linalg.norm(np.array(mon[-1][2]) - I0) / np.linalg.norm(I0)),
+            "energy_rel_drift": float((mon[-1][3] - E0) / abs(E0))}
+
+
+def run_leapfrog(args):
+    """Leapfrogging coaxial rings: R=1 and R=0.7, 0.3 apart axially, Gamma=1
+    each, a=0.1R, 10 particles per section, sigma=a/2 (~200k particles),
+    Gaussian-erf, rVPM, dynamic SFS (two-level, no backscatter), core spreading
+    nu=1e-4, Pedrizzetti relaxation, RK3 with dt=0.005.
+
+    * FP32-comp at full size for --lf-steps steps: ms/step, particle-steps/s,
+      impulse I = 1/2 sum x x Gamma and energy E = 1/2 sum U.(x x Gamma) drift;
+    * FP64 against FP32-comp at full size over --lf-f64-steps steps (state
+      difference), and over the whole run at --lf-small particles (monitor
+      trajectories of both precisions)."""
+    import torch
+    import vpm_gb300 as vpm
+    from vpm_gb300 import device_step as ds, workloads
+    ctx = vpm.Context(0)
+    dt = 0.005
+    X, G, s = workloads.leapfrog_rings(args.lf_n, nper=10)
+    n = X.shape[0]
+    ms32, mon32, f32 = _leapfrog_run(ctx, X, G, s, vpm.FP32COMP, args.lf_steps, dt, 20, torch, ds)
+    uj_per_step, estr_per_step = 5, 4     # dynamic SFS: test-filter UJ + 3 stages (with Estr), relaxation UJ
+    out = {"mode": "leapfrog", "n_particles": n, "steps": args.lf_steps, "dt": dt, "precision": "fp32comp",
+           "ms_per_step": ms32, "particle_steps_per_s": n / (ms32 / 1e3),
+           "pairs_per_s": (uj_per_step + estr_per_step) * float(n) * n / (ms32 / 1e3),
+           "uj_calls_per_step": uj_per_step, "estr_calls_per_step": estr_per_step,
+           "drift_fp32comp": _drift(mon32), "monitor_fp32comp": mon32}
+    # FP64 vs FP32-comp on the full-size field over a few steps
+    k64 = args.lf_f64_steps
+    if k64 > 0:
+        ms64, m64, f64 = _leapfrog_run(ctx, X, G, s, vpm.FP64, k64, dt, k64, torch, ds)
+        _, m32s, f32s = _leapfrog_run(ctx, X, G, s, vpm.FP32COMP, k64, dt, k64, torch, ds)
+        rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+        out["fp64_full_size"] = {"steps": k64, "ms_per_step_fp64": ms64, "fp32comp_speedup": ms64 / ms32,
+                                 "x_max_rel": rel(f32s.x, f64.x), "gamma_max_rel": rel(f32s.gam, f64.gam),
+                                 "sigma_max_rel": rel(f32s.sig, f64.sig), "U_max_rel": rel(f32s.U, f64.U),
+                                 "J_max_rel": rel(f32s.J, f64.J),
+                                 "energy_rel_diff": (m32s[-1][3] - m64[-1][3]) / abs(m64[-1][3])}
+    # whole run, both precisions, at reduced size, with two controls: the same
+    # comparison without the SFS model, and FP64 against FP64 started from
+    # strengths perturbed by 1e-7 (relative, seeded) -- the size of the
+    # FP32-comp UJ error
+    if args.lf_small > 0:
+        Xs, Gs, ss = workloads.leapfrog_rings(args.lf_small, nper=10)
+        Gp = Gs * (1.0 + 1e-7 * np.random.default_rng(9).standard_normal(Gs.shape))
+
+        def diff(ma, mb):
+            dI = max(np.linalg.norm(np.array(a[2]) - np.array(b[2])) / np.linalg.norm(np.array(b[2]))
+                     for a, b in zip(ma, mb))
+            dE = max(abs(a[3] - b[3]) / abs(b[3]) for a, b in zip(ma, mb))
+            return {"impulse_max_rel_diff": float(dI), "energy_max_rel_diff": float(dE)}
+        run = lambda prec, G_, sfs_: _leapfrog_run(ctx, Xs, G_, ss, prec, args.lf_steps, dt, 20, torch, ds, sfs_)
+        ms64s, mon64, _ = run(vpm.FP64, Gs, True)
+        ms32s, mon32s, _ = run(vpm.FP32COMP, Gs, True)
+        _, mon64p, _ = run(vpm.FP64, Gp, True)
+        _, mon64n, _ = run(vpm.FP64, Gs, False)
+        _, mon32n, _ = run(vpm.FP32COMP, Gs, False)
+        out["fp64_vs_fp32comp_small"] = {"n_particles": Xs.shape[0], "steps": args.lf_steps,
+                                         "ms_per_step_fp64": ms64s, "ms_per_step_fp32comp": ms32s,
+                                         "drift_fp64": _drift(mon64), "drift_fp32comp": _drift(mon32s),
+                                         "fp32comp_vs_fp64": diff(mon32s, mon64),
+                                         "control_fp64_perturbed_1e-7_vs_fp64": diff(mon64p, mon64),
+                                         "control_no_sfs_fp32comp_vs_fp64": diff(mon32n, mon64n),
+                                         "drift_no_sfs_fp64": _drift(mon64n),
+                                         "monitor_fp64": mon64, "monitor_fp32comp": mon32s}
+    print(json.dumps(out), flush=True)
+
+
+def run_jet(args):
+    """Round-jet-like cloud with the FMM near field: 2^20 particles uniform in
+    a cylinder (radius 0.5, length 4), Gamma = vol * curl A of a seeded random
+    Fourier field with a Gaussian spectrum, sigma = 0.02, Gaussian-erf.  The
+    octree (leaf size 64, theta = 0.4) and its leaf-pair lists are built on the
+    GPU at every UJ call, and every near leaf pair is evaluated by P2P in
+    FP32-comp (UJ, and Estr where the step asks for it).  The far field is not
+    computed.  Reported: the tree build alone, one UJ (+Estr) call, and whole
+    rVPM RK3 steps with dynamic SFS and relaxation (5 near-field UJ calls, 4
+    with Estr)."""
+    import torch
+    import vpm_gb300 as vpm
+    from vpm_gb300 import device_step as ds, workloads
+    ctx = vpm.Context(0)
+    X, G, s = workloads.jet_cloud(args.jet_n)
+    n = X.shape[0]
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    x, g, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    S = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    leaf, theta = 64, 0.4
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            out = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / reps, out
+    import vpm_gb300._lib as L
+    sizes = np.zeros(3, dtype=np.int64)
+
+    def tree_only():
+        rc = ctx._L.vpm_leaflist_dev(ctx._h, n, x.data_ptr(), leaf, theta, None, None, None, None, None,
+                                     sizes.ctypes.data)
+        if rc != 0:
+            raise L.VPMError(rc, ctx._L.vpm_last_error(ctx._h).decode())
+    ms_tree, _ = timed(tree_only, 5)
+    kw = dict(leaf_size=leaf, theta=theta, kernel=KERNEL, precision=vpm.FP32COMP)
+    ms_uj, st = timed(lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, **kw), 5)
+    ms_ujs, _ = timed(lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, S, sfs=True, **kw), 5)
+    ms_uj64, _ = timed(lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, leaf_size=leaf, theta=theta, kernel=KERNEL,
+                                                    precision=vpm.FP64), 1)
+    # accuracy of the FP32-comp near field against the FP64 near field over the same lists
+    U32, J32 = torch.zeros_like(U), torch.zeros_like(J)
+    U64, J64 = torch.zeros_like(U), torch.zeros_like(J)
+    ctx.p2p_leaflist_dev(x, g, sg, U32, J32, **kw)
+    ctx.p2p_leaflist_dev(x, g, sg, U64, J64, leaf_size=leaf, theta=theta, kernel=KERNEL, precision=vpm.FP64)
+    rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+    pairs = st[2]
+    # whole steps
+    fld = ds.DeviceField(x.clone(), g.clone(), sg.clone(), kernel=KERNEL, precision=vpm.FP32COMP)
+    fld.leaflist = (leaf, theta)
+    sfs = ds.DynamicSFSParams()
+    ds.rk3_step(fld, 1e-3, ctx, sfs=sfs, relax_rlxf=0.3)        # warm-up
+    torch.cuda.synchronize()
+    nst = args.jet_steps
+    t0 = time.perf_counter()
+    for _ in range(nst):
+        ds.rk3_step(fld, 1e-3, ctx, sfs=sfs, relax_rlxf=0.3)
+    torch.cuda.synchronize()
+    ms_step = (time.perf_counter() - t0) * 1e3 / nst
+    out = {"mode": "jet", "n_particles": n, "leaf_size": leaf, "theta": theta, "leaves": st[0], "leaf_pairs": st[1],
+           "particle_pairs_per_uj": pairs, "pairs_per_particle": pairs / n,
+           "tree_build_ms": ms_tree,
+           "uj_call_ms": ms_uj, "uj_pairs_per_s": pairs / (ms_uj / 1e3),
+           "uj_estr_call_ms": ms_ujs, "uj_estr_pairs_per_s": 2 * pairs / (ms_ujs / 1e3),
+           "uj_call_ms_fp64": ms_uj64, "fp32comp_over_fp64": ms_uj64 / ms_uj,
+           "err_fp32comp_vs_fp64": {"U_max_rel": rel(U32, U64), "J_max_rel": rel(J32, J64)},
+           "step_ms": ms_step, "steps_timed": nst, "particle_steps_per_s": n / (ms_step / 1e3),
+           "step": "rVPM RK3 + dynamic SFS + Pedrizzetti relaxation, 5 near-field UJ calls (4 with Estr), "
+                   "tree rebuilt at each call",
+           "far_field": "not computed (FastMultipole.jl's multipole part is outside this library)"}
+    print(json.dumps(out), flush=True)
+
+
+def run_kernel_only_jet(args):
+    """Profiling helper: `warmup` + `steps` near-field UJ (+Estr with --estr)
+    calls on the jet cloud of --n particles at the density of the 2^20 case
+    (the cylinder is shortened in proportion), nothing else."""
+    import torch
+    import vpm_gb300 as vpm
+    from vpm_gb300 import workloads
+    n = args.n
+    X, G, s = workloads.jet_cloud(n, length=4.0 * n / (1 << 20))
+    ctx = vpm.Context(0)
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    x, g, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    S = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    prec = vpm.FP64 if args.precision == "fp64" else vpm.FP32COMP
+    times, st = [], None
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st = ctx.p2p_leaflist_dev(x, g, sg, U, J, S, leaf_size=64, theta=0.4, kernel=KERNEL, precision=prec,
+                                  sfs=bool(args.estr))
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times) if times else float("nan")
+    print(json.dumps({"mode": "kernel-only-jet", "n": n, "precision": args.precision, "estr": bool(args.estr),
+                      "ms": ms, "leaves": st[0], "leaf_pairs": st[1], "pairs": st[2],
+                      "pairs_per_s": st[2] / (ms / 1e3), "launches": ctx.launches}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -421,10 +631,24 @@ def main():
     ap.add_argument("--precision", default="fp32comp", choices=["fp64", "fp32comp"])
     ap.add_argument("--kernel", default="gaussianerf", choices=["singular", "gaussian", "gaussianerf", "winckelmans"])
     ap.add_argument("--estr", action="store_true")
+    # the other workloads (one JSON line each, not the bench line)
+    ap.add_argument("--workload", default="cloud", choices=["cloud", "leapfrog", "jet"])
+    ap.add_argument("--lf-n", type=int, default=200_000)
+    ap.add_argument("--lf-steps", type=int, default=200)
+    ap.add_argument("--lf-f64-steps", type=int, default=2)
+    ap.add_argument("--lf-small", type=int, default=20_000)
+    ap.add_argument("--jet-n", type=int, default=1 << 20)
+    ap.add_argument("--jet-steps", type=int, default=3)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
-    if args.kernel_only:
+    if args.kernel_only and args.workload == "jet":
+        run_kernel_only_jet(args)
+    elif args.workload == "leapfrog":
+        run_leapfrog(args)
+    elif args.workload == "jet":
+        run_jet(args)
+    elif args.kernel_only:
         run_kernel_only(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)

@@ -21,7 +21,8 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvpm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["uj.cu", "estr.cu", "order.cu", "adjoint.cu", "leaflist.cu", "tree.cpp", "abi.cu", "noalloc.cu"]
+SOURCES = ["uj.cu", "estr.cu", "order.cu", "adjoint.cu", "nearfield.cu", "leaflist.cu", "tree.cpp", "abi.cu",
+           "noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -47,7 +48,7 @@ def build(force: bool = False, ptxas_verbose: bool = False, defines=(), lib: str
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "vpm_gb300.h"))
     cc = nvcc()
-    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr"]
     if ptxas_verbose:
         flags += ["-Xptxas", "-v"]
     flags += ["-D" + d for d in defines]

@@ -14,6 +14,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <vector>
 
 using namespace vpm;
 
@@ -21,28 +22,6 @@ namespace {
 
 // 0-based rows of the particle column, src/FLOWVPM_particlefield.jl:239-252
 enum : int { R_X = 0, R_G = 3, R_SIG = 6, R_U = 9, R_W = 12, R_J = 15, R_PSE = 24, R_SFS = 39, R_STATIC = 42 };
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t grow(size_t bytes)
-    {
-        if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = bytes + bytes / 8;  // grow with some headroom, never shrink
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
 
 thread_local std::string g_create_error;
 
@@ -65,8 +44,10 @@ struct vpm_ctx {
     DevBuf mat, mat2, x, g, s, st, xt;
     // packing and split-K scratch
     DevBuf src_pack, order, partial, flag;
-    // near-field leaf-pair lists and their packed particles
+    // near-field: packed particles, and the lists (built on the device or uploaded)
     DevBuf leaf;
+    NearScratch near;
+    int sync_rc = 0;     // VPM status of the last wait made for the list builder
 };
 
 namespace {
@@ -134,6 +115,25 @@ int bounded_wait(vpm_ctx* c)
         std::this_thread::sleep_for(std::chrono::microseconds(sleep_us));
         if (sleep_us < 1000) sleep_us *= 2;
     }
+}
+
+// SyncFn for the near-field list builder: a bounded wait whose status is kept in the context
+cudaError_t near_sync(void* p)
+{
+    vpm_ctx* c = (vpm_ctx*)p;
+    c->sync_rc = bounded_wait(c);
+    return c->sync_rc == VPM_OK ? cudaSuccess : cudaErrorLaunchTimeout;
+}
+
+// a failure of the list builder: the wait's own status, a capacity error, or a CUDA error
+int near_fail(vpm_ctx* c, cudaError_t e, const char* what)
+{
+    if (c->sync_rc != VPM_OK) return c->sync_rc;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(c, VPM_ERR_CAPACITY, "%s: out of device memory", what);
+    }
+    return cuda_fail(c, e, what);
 }
 
 bool is_device_ptr(const void* p)
@@ -311,6 +311,7 @@ int vpm_ctx_destroy(vpm_ctx* c)
         for (DevBuf* b : {&c->mat, &c->mat2, &c->x, &c->g, &c->s, &c->st, &c->xt, &c->src_pack, &c->order,
                           &c->partial, &c->flag, &c->leaf})
             b->release();
+        c->near.release_all();
         if (c->done) cudaEventDestroy(c->done);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
         cudaGetLastError();
@@ -544,47 +545,143 @@ int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, con
     return bounded_wait(c);
 }
 
+static int near_check(vpm_ctx* c, const char* fn, int64_t n, const double* x, const double* gam,
+                      const double* sig, const uint8_t* static_flags, double* U, double* J, double* SFS,
+                      int kernel, int precision, int flags)
+{
+    if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (flags & ~(VPM_SFS | VPM_TRANSPOSED))
+        return fail(c, VPM_ERR_ARG, "%s: only VPM_SFS and VPM_TRANSPOSED are accepted", fn);
+    RC(check_kernel(c, kernel, precision));
+    if (n == 0) return VPM_OK;
+    const bool sfs = (flags & VPM_SFS) != 0;
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(U) ||
+        !is_device_ptr(J) || (sfs && !is_device_ptr(SFS)) || (static_flags && !is_device_ptr(static_flags)))
+        return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
+    return VPM_OK;
+}
+
+static int near_run(vpm_ctx* c, NearLists& L, int64_t n, const double* x, const double* gam, const double* sig,
+                    const uint8_t* static_flags, double* U, double* J, double* SFS, int kernel, int precision,
+                    int flags, int64_t* stats)
+{
+    cudaError_t e = near_groups(c->near, &L, c->stream, near_sync, c, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
+    RC(grow(c, c->leaf, leaf_work_bytes(n), "near-field packs"));
+    LeafArgs a;
+    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = U; a.J = J; a.SFS = SFS; a.static_flags = static_flags;
+    a.kernel = kernel; a.precision = precision; a.sfs = (flags & VPM_SFS) != 0;
+    a.transposed = (flags & VPM_TRANSPOSED) != 0;
+    CK(launch_leaflist(a, L, c->leaf.p, c->stream, &c->launches), "near-field P2P kernels");
+    RC(bounded_wait(c));
+    if (stats) {
+        stats[0] = L.nleaves;
+        stats[1] = L.nlpairs;
+        stats[2] = L.pairs;
+    }
+    return VPM_OK;
+}
+
 int vpm_p2p_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
                          const uint8_t* static_flags, double* U, double* J, double* SFS, int leaf_size,
                          double theta, int kernel, int precision, int flags, int64_t* stats)
 {
-    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: ctx is NULL");
+    const char* fn = "vpm_p2p_leaflist_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: n out of range");
-    if (leaf_size < 1 || leaf_size > LEAF_SIZE_MAX)
-        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: leaf_size must be in 1..%d", LEAF_SIZE_MAX);
-    if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: bad theta");
-    if (flags & ~(VPM_SFS | VPM_TRANSPOSED))
-        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: only VPM_SFS and VPM_TRANSPOSED are accepted");
-    RC(check_kernel(c, kernel, precision));
     if (stats) stats[0] = stats[1] = stats[2] = 0;
-    if (n == 0) return VPM_OK;
+    if (leaf_size < 1 || leaf_size > LEAF_SIZE_MAX)
+        return fail(c, VPM_ERR_ARG, "%s: leaf_size must be in 1..%d", fn, LEAF_SIZE_MAX);
+    if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "%s: bad theta", fn);
     DeviceGuard dg(c->device);
-    const bool sfs = (flags & VPM_SFS) != 0;
-    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(U) ||
-        !is_device_ptr(J) || (sfs && !is_device_ptr(SFS)) || (static_flags && !is_device_ptr(static_flags)))
-        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: every array must be a device pointer");
-    // the host builds the octree and the leaf-pair list
-    std::vector<double> hx(3 * n);
-    CK(cudaMemcpyAsync(hx.data(), x, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H positions");
-    CK(cudaStreamSynchronize(c->stream), "D2H positions");
-    LeafLists L;
-    if (build_leaf_lists(n, hx.data(), leaf_size, theta, &L) != 0)
-        return fail(c, VPM_ERR_ARG, "vpm_p2p_leaflist_dev: octree construction failed");
-    if (L.col.size() > (size_t)INT32_MAX)
-        return fail(c, VPM_ERR_CAPACITY, "vpm_p2p_leaflist_dev: too many leaf pairs (%zu)", L.col.size());
-    RC(grow(c, c->leaf, leaf_work_bytes(n, (int64_t)L.leaf_begin.size(), (int64_t)L.col.size()), "leaf lists"));
-    LeafArgs a;
-    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = U; a.J = J; a.SFS = SFS; a.static_flags = static_flags;
-    a.kernel = kernel; a.precision = precision; a.sfs = sfs; a.transposed = (flags & VPM_TRANSPOSED) != 0;
-    CK(launch_leaflist(a, L, c->leaf.p, c->stream, &c->launches), "leaf-list P2P kernels");
-    RC(bounded_wait(c));
-    if (stats) {
-        stats[0] = (int64_t)L.leaf_begin.size();
-        stats[1] = (int64_t)L.col.size();
-        stats[2] = L.pairs;
+    RC(near_check(c, fn, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags));
+    if (n == 0) return VPM_OK;
+    NearLists L;
+    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, &L, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
+    return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags, stats);
+}
+
+int vpm_p2p_lists_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
+                      const uint8_t* static_flags, double* U, double* J, double* SFS, const int32_t* perm,
+                      int64_t nl, const int64_t* leaf_begin, const int64_t* leaf_end, const int64_t* row,
+                      const int32_t* col, int kernel, int precision, int flags, int64_t* stats)
+{
+    const char* fn = "vpm_p2p_lists_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (stats) stats[0] = stats[1] = stats[2] = 0;
+    DeviceGuard dg(c->device);
+    RC(near_check(c, fn, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags));
+    if (n == 0) return VPM_OK;
+    // the lists must describe a partition of the n tree positions into leaves
+    if (!perm || !leaf_begin || !leaf_end || !row || nl < 1 || nl > n)
+        return fail(c, VPM_ERR_ARG, "%s: missing or empty lists", fn);
+    {
+        std::vector<uint8_t> seen(n, 0);
+        for (int64_t p = 0; p < n; p++) {
+            if (perm[p] < 0 || perm[p] >= n || seen[perm[p]])
+                return fail(c, VPM_ERR_ARG, "%s: perm is not a permutation of 0..n-1", fn);
+            seen[perm[p]] = 1;
+        }
     }
+    for (int64_t l = 0; l < nl; l++)
+        if (leaf_begin[l] != (l == 0 ? 0 : leaf_end[l - 1]) || leaf_end[l] <= leaf_begin[l])
+            return fail(c, VPM_ERR_ARG, "%s: leaf %lld is not the next non-empty range", fn, (long long)l);
+    if (leaf_end[nl - 1] != n) return fail(c, VPM_ERR_ARG, "%s: the leaves do not cover 0..n-1", fn);
+    if (row[0] != 0) return fail(c, VPM_ERR_ARG, "%s: row[0] must be 0", fn);
+    for (int64_t l = 0; l < nl; l++)
+        if (row[l + 1] < row[l]) return fail(c, VPM_ERR_ARG, "%s: row is not monotone", fn);
+    if (row[nl] > (int64_t)INT32_MAX) return fail(c, VPM_ERR_CAPACITY, "%s: more than 2^31 leaf pairs", fn);
+    if (row[nl] > 0 && !col) return fail(c, VPM_ERR_ARG, "%s: col is NULL", fn);
+    std::vector<int32_t> cs(col, col + row[nl]);
+    for (int64_t l = 0; l < nl; l++) {
+        std::sort(cs.begin() + row[l], cs.begin() + row[l + 1]);
+        for (int64_t j = row[l]; j < row[l + 1]; j++) {
+            if (cs[j] < 0 || cs[j] >= nl) return fail(c, VPM_ERR_ARG, "%s: source leaf out of range", fn);
+            if (j > row[l] && cs[j] == cs[j - 1])
+                return fail(c, VPM_ERR_ARG, "%s: leaf %lld lists source leaf %d twice", fn, (long long)l, cs[j]);
+        }
+    }
+    NearLists L;
+    cudaError_t e = near_upload(c->near, n, perm, nl, leaf_begin, leaf_end, row, cs.data(), c->stream, near_sync, c,
+                                &L, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "leaf-pair lists");
+    return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags, stats);
+}
+
+int vpm_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
+                     int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes)
+{
+    const char* fn = "vpm_leaflist_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (!sizes || n <= 0 || n > (int64_t)1 << 30 || leaf_size < 1 || leaf_size > LEAF_SIZE_MAX ||
+        !(theta >= 0.0 && theta <= 1.0e6))
+        return fail(c, VPM_ERR_ARG, "%s: bad arguments", fn);
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x)) return fail(c, VPM_ERR_ARG, "%s: x must be a device pointer", fn);
+    NearLists L;
+    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, &L, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
+    sizes[0] = L.nleaves;
+    sizes[1] = L.nlpairs;
+    sizes[2] = L.pairs;
+    if (!perm) return VPM_OK;
+    if (!leaf_begin || !leaf_end || !row || !col) return fail(c, VPM_ERR_ARG, "%s: NULL output", fn);
+    const int64_t nl = L.nleaves, m = L.nlpairs;
+    std::vector<int32_t> b(nl), en(nl), r(nl + 1);
+    CK(cudaMemcpyAsync(perm, L.perm, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream), "D2H lists");
+    CK(cudaMemcpyAsync(b.data(), L.leaf_begin, nl * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream), "D2H lists");
+    CK(cudaMemcpyAsync(en.data(), L.leaf_end, nl * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream), "D2H lists");
+    CK(cudaMemcpyAsync(r.data(), L.row, (nl + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream), "D2H lists");
+    if (m > 0) CK(cudaMemcpyAsync(col, L.col, m * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream), "D2H lists");
+    RC(bounded_wait(c));
+    for (int64_t l = 0; l < nl; l++) { leaf_begin[l] = b[l]; leaf_end[l] = en[l]; }
+    for (int64_t l = 0; l <= nl; l++) row[l] = r[l];
     return VPM_OK;
 }
 

@@ -106,9 +106,78 @@ cudaError_t launch_estr(const EstrArgs& a, const Workspace& w, int num_sms, cuda
 cudaError_t launch_uj_adjoint(const AdjArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
                               int64_t* launches);
 
-struct LeafLists;
-constexpr int LEAF_SIZE_MAX = 64;
-size_t leaf_work_bytes(int64_t n, int64_t nleaves, int64_t nleafpairs);
-cudaError_t launch_leaflist(const LeafArgs& a, const LeafLists& L, void* work, cudaStream_t st, int64_t* launches);
+// ------------------------------------------------------------------ near field
+// A device allocation that grows on demand and never shrinks.
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t grow(size_t bytes)
+    {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = bytes + bytes / 8;   // some headroom
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+// Leaf-pair lists on the device.  Particles are numbered by their Morton
+// position p (perm[p] = caller index); leaves are Morton-ordered ranges
+// [leaf_begin[l], leaf_end[l]); row/col is the CSR list of the source leaves
+// of every target leaf.  For the kernels, targets are cut into warp groups of
+// 32 consecutive Morton positions; group g's sources are the intervals
+// ivs[grp_row[g] .. grp_row[g+1]) = (p0, p1, mask, 0): particle range [p0, p1)
+// needed by the target leaves whose bit (leaf - leaf_of[32 g]) is set in mask.
+struct NearLists {
+    int64_t n = 0, nleaves = 0, nlpairs = 0, ngroups = 0, nivs = 0;
+    int64_t pairs = 0;                 // particle pairs over all leaf pairs
+    int64_t nodes = 0;                 // octree nodes (0 for lists given by the caller)
+    const int32_t* perm = nullptr;     // [n]
+    const int32_t* leaf_of = nullptr;  // [n]
+    const int32_t* leaf_begin = nullptr;
+    const int32_t* leaf_end = nullptr; // [nleaves]
+    const int32_t* row = nullptr;      // [nleaves + 1]
+    const int32_t* col = nullptr;      // [nlpairs]
+    const int32_t* grp_row = nullptr;  // [ngroups + 1]
+    const int4* ivs = nullptr;         // [nivs]
+};
+
+// Device scratch of the list builder (owned by the context).
+struct NearScratch {
+    DevBuf keys, keys2, idx, perm, xs, part, nodes, node_lvl, node_box, node_cr, node_leaf, ctr;
+    DevBuf flag, leaf_of, lb, le, row, col, fr0, fr1, near0, near1, grp_cnt, grp_row, ivs, cub;
+    int64_t* hctr = nullptr;          // pinned host copy of the builder's counters
+    size_t capF = 0, capN = 0;        // traversal capacities (pairs)
+    void release_all();
+};
+
+// A bounded wait for the stream, supplied by the ABI layer (cudaSuccess or an error).
+typedef cudaError_t (*SyncFn)(void* ctx);
+
+// Octree (leaf size, Morton keys of 21 bits per axis) and near leaf pairs
+// (theta |c_A - c_B| < R_A + R_B) of the n device positions x[n,3].
+cudaError_t near_build(NearScratch& s, int64_t n, const double* x, int leaf_size, double theta, cudaStream_t st,
+                       SyncFn sync, void* sync_ctx, NearLists* out, int64_t* launches);
+// Lists supplied by the caller on the host (checked there): copied to the device.
+cudaError_t near_upload(NearScratch& s, int64_t n, const int32_t* perm, int64_t nleaves, const int64_t* leaf_begin,
+                        const int64_t* leaf_end, const int64_t* row, const int32_t* col, cudaStream_t st,
+                        SyncFn sync, void* sync_ctx, NearLists* out, int64_t* launches);
+// The warp-group source intervals of lists built or uploaded above.
+cudaError_t near_groups(NearScratch& s, NearLists* L, cudaStream_t st, SyncFn sync, void* sync_ctx,
+                        int64_t* launches);
+
+constexpr int LEAF_SIZE_MAX = 4096;
+size_t leaf_work_bytes(int64_t n);
+cudaError_t launch_leaflist(const LeafArgs& a, const NearLists& L, void* work, cudaStream_t st, int64_t* launches);
 
 }  // namespace vpm

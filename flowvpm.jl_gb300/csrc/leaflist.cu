@@ -2,24 +2,27 @@
 // UJ_fmm (FastMultipole's direct_list, src/FLOWVPM_UJ.jl:90-100) and the Estr
 // pass over the same list (Estr_fmm!, src/FLOWVPM_subfilterscale_models.jl:94-188).
 //
-// The host builds the octree and the leaf-pair list (tree.cpp); particles are
-// processed in the tree's Morton order, so every leaf is a contiguous range.
-// One block per target leaf, one target per thread (leaves hold at most
-// LEAF_MAX particles); the block walks its list of source leaves, staging each
-// source leaf in shared memory.  Pair math is that of the all-pairs kernels
-// (uj_pair.cuh for FP32-comp, the reference formula for FP64); Estr uses the
-// same factored form as estr.cu with the self pair excluded by position.
+// Particles are processed in the tree's Morton order (nearfield.cu), so every
+// leaf is a contiguous range.  Leaves are small (leaf_size is a maximum; a
+// uniform cloud at leaf_size 64 averages ~11 particles a leaf), so work is not
+// cut per leaf: one warp takes 32 consecutive Morton positions -- a few
+// neighbouring leaves -- and walks the union of their source lists as
+// particle intervals, each with the mask of the warp's leaves that need it.
+// Sources are staged 32 at a time in the warp's shared memory; a lane whose
+// leaf is not in an interval's mask computes with zero weight.  Pair math is
+// that of the all-pairs kernels (uj_pair.cuh for FP32-comp, the reference
+// formula for FP64); Estr uses the factored form of estr.cu with the self
+// pair excluded by position.
 #include "internal.h"
-#include "tree.h"
 #include "uj_pair.cuh"
 #include "vpm_math.cuh"
 
 namespace vpm {
 
-constexpr int LEAF_MAX = LEAF_SIZE_MAX;   // threads per block = largest leaf
-constexpr int MID_LEAVES = 4;      // source leaves summed in FP32 before the FP64 add
-
-static_assert(LEAF_MAX % 32 == 0 && LEAF_MAX % 4 == 0, "whole warps, 4-source groups");
+constexpr int NF_WARPS = 4;                  // warp groups per block
+constexpr int NF_THREADS = 32 * NF_WARPS;
+constexpr int NF_BLK_TILES = 2;              // 32-source tiles summed in FP32 per block
+constexpr int NF_MID_BLKS = 4;               // blocks summed in FP32 before the FP64 add
 
 __global__ void tgt_from_perm(int64_t n, const double* __restrict__ x, const int32_t* __restrict__ perm,
                               TgtPos* __restrict__ out)
@@ -109,37 +112,50 @@ __global__ void leaf_pack_estr(int64_t n, const double* __restrict__ x, const do
     }
 }
 
+// Warp-group geometry shared by the mixed kernels: this lane's target (FP64
+// position, caller index), its leaf relative to the group's first leaf, and
+// the FP32 offsets from the group origin (the group's first target).
+struct GroupTarget {
+    double tx, ty, tz;
+    int32_t idx;
+    int local;
+    bool valid;
+};
+
+__device__ __forceinline__ GroupTarget group_target(int64_t n, int64_t p0, int lane, const TgtPos* __restrict__ tgt,
+                                                    const int32_t* __restrict__ leaf_of)
+{
+    GroupTarget g;
+    const int64_t t = p0 + lane;
+    g.valid = t < n;
+    const TgtPos p = tgt[g.valid ? t : p0];
+    g.tx = p.x; g.ty = p.y; g.tz = p.z; g.idx = p.idx;
+    g.local = leaf_of[g.valid ? t : p0] - leaf_of[p0];
+    return g;
+}
+
 // ------------------------------------------------------------- UJ, FP32-comp
 template <int K>
-__global__ void __launch_bounds__(LEAF_MAX)
-leaf_uj_mixed(const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb, const int32_t* __restrict__ le,
-              const int32_t* __restrict__ row, const int32_t* __restrict__ col,
-              const SrcMixed* __restrict__ src, double* U, double* J)
+__global__ void __launch_bounds__(NF_THREADS)
+nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
+            const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const SrcMixed* __restrict__ src,
+            double* U, double* J)
 {
-    __shared__ SrcMixed tile[LEAF_MAX];
-    __shared__ float4 off[LEAF_MAX / 32][LEAF_MAX];
+    __shared__ SrcMixed tile[NF_WARPS][32];
+    __shared__ float4 off[NF_WARPS][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int leaf = blockIdx.x;
-    const int64_t t = (int64_t)lb[leaf] + threadIdx.x;
-    const bool valid = t < le[leaf];
-    double tx = 3.0e4, ty = 3.0e4, tz = 3.0e4;
-    int32_t idx = 0;
-    if (valid) {
-        const TgtPos p = tgt[t];
-        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
-    }
-    // warp origin: lane 0's target if valid, else the leaf's first target
-    const int64_t t0 = (int64_t)lb[leaf] + warp * 32;
-    const bool w_any = t0 < le[leaf];
-    const TgtPos p0 = tgt[w_any ? t0 : (int64_t)lb[leaf]];
-    const double ox = p0.x, oy = p0.y, oz = p0.z;
-    const float3 th = make_float3((float)tx, (float)ty, (float)tz);
-    const float3 tl = make_float3((float)(tx - (double)th.x), (float)(ty - (double)th.y), (float)(tz - (double)th.z));
-    const float3 oh = make_float3((float)ox, (float)oy, (float)oz);
-    const float3 ol = make_float3((float)(ox - (double)oh.x), (float)(oy - (double)oh.y), (float)(oz - (double)oh.z));
-    const float3 to = valid ? make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz))
-                            : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
-    float b2 = valid ? fmaf(to.x, to.x, fmaf(to.y, to.y, to.z * to.z)) : 0.0f;
+    const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
+    if (grp >= ngroups) return;
+    const int64_t p0 = 32 * grp;
+    const GroupTarget me = group_target(n, p0, lane, tgt, leaf_of);
+    const TgtPos o = tgt[p0];
+    const float3 th = make_float3((float)me.tx, (float)me.ty, (float)me.tz);
+    const float3 tl = make_float3((float)(me.tx - (double)th.x), (float)(me.ty - (double)th.y),
+                                  (float)(me.tz - (double)th.z));
+    const float3 oh = make_float3((float)o.x, (float)o.y, (float)o.z);
+    const float3 ol = make_float3((float)(o.x - (double)oh.x), (float)(o.y - (double)oh.y), (float)(o.z - (double)oh.z));
+    const float3 to = make_float3((float)(me.tx - o.x), (float)(me.ty - o.y), (float)(me.tz - o.z));
+    float b2 = fmaf(to.x, to.x, fmaf(to.y, to.y, to.z * to.z));
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
     const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
@@ -147,57 +163,63 @@ leaf_uj_mixed(const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb, co
 
     double dU[3] = {0.0, 0.0, 0.0}, dW[3] = {0.0, 0.0, 0.0}, dJ[8];
     float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
+    float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) { dJ[k] = 0.0; mj[k] = 0.f; }
-    int in_mid = 0;
-    const int e0 = row[leaf], e1 = row[leaf + 1];
-    for (int e = e0; e < e1; e++) {
-        const int sl = col[e];
-        const int64_t sb = lb[sl];
-        const int cnt = le[sl] - lb[sl];
-        __syncthreads();
-        if (threadIdx.x < cnt) {
-            tile[threadIdx.x] = src[sb + threadIdx.x];
-        } else {   // padding: far away, no strength
-            tile[threadIdx.x].a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
-            tile[threadIdx.x].b = make_float4(0.f, 0.f, 0.f, 1.f);
-            tile[threadIdx.x].gam = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        __syncthreads();
-        const int ng = (cnt + 3) / 4;
-        for (int j = lane; j < 4 * ng; j += 32) {
-            const float4 a = tile[j].a, b = tile[j].b;
-            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : b.w * b.w;
-            off[warp][j] = make_float4((a.x - oh.x) + (b.x - ol.x), (a.y - oh.y) + (b.y - ol.y),
-                                       (a.z - oh.z) + (b.z - ol.z), thr);
-        }
-        __syncwarp();
-        float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
+    for (int k = 0; k < 8; k++) { dJ[k] = 0.0; mj[k] = 0.f; jq[k] = 0.f; }
+    int tiles = 0, blks = 0;
+    const int e1 = grp_row[grp + 1];
+    for (int e = grp_row[grp]; e < e1; e++) {
+        const int4 iv = ivs[e];
+        const float act = (me.valid && ((unsigned)iv.z >> me.local) & 1u) ? 1.0f : 0.0f;
+        for (int base = iv.x; base < iv.y; base += 32) {
+            const int cnt = min(32, iv.y - base);
+            SrcMixed sj;
+            if (lane < cnt) {
+                sj = src[base + lane];
+            } else {   // padding: far away, no strength
+                sj.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+                sj.b = make_float4(0.f, 0.f, 0.f, 1.f);
+                sj.gam = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            const float thr = singular_tail<K>() ? fmaxf(sfar * sj.a.w, r2n) : sj.b.w * sj.b.w;
+            __syncwarp();
+            tile[warp][lane] = sj;
+            off[warp][lane] = make_float4((sj.a.x - oh.x) + (sj.b.x - ol.x), (sj.a.y - oh.y) + (sj.b.y - ol.y),
+                                          (sj.a.z - oh.z) + (sj.b.z - ol.z), thr);
+            __syncwarp();
+            const int ng = (cnt + 3) >> 2;
+            for (int q = 0; q < ng; q++)
+                pair4_mixed<K, true>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, act);
+            if (++tiles == NF_BLK_TILES) {
+                tiles = 0;
 #pragma unroll
-        for (int k = 0; k < 8; k++) jq[k] = 0.f;
-        for (int g = 0; g < ng; g++) pair4_mixed<K>(to, th, tl, r2n, off[warp], tile, 4 * g, u, jq, w);
+                for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }
 #pragma unroll
-        for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; }
+                for (int k = 0; k < 8; k++) { mj[k] += jq[k]; jq[k] = 0.f; }
+                if (++blks == NF_MID_BLKS) {
+                    blks = 0;
 #pragma unroll
-        for (int k = 0; k < 8; k++) mj[k] += jq[k];
-        if (++in_mid == MID_LEAVES || e + 1 == e1) {
+                    for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
 #pragma unroll
-            for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
-#pragma unroll
-            for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
-            in_mid = 0;
+                    for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
+                }
+            }
         }
     }
-    if (!valid) return;
+#pragma unroll
+    for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k] + (double)u[k]; dW[k] += (double)mw[k] + (double)w[k]; }
+#pragma unroll
+    for (int k = 0; k < 8; k++) dJ[k] += (double)mj[k] + (double)jq[k];
+    if (!me.valid) return;
     double j9[9];
 #pragma unroll
     for (int k = 0; k < 8; k++) j9[k] = -3.0 * dJ[k];
     j9[8] = 3.0 * (dJ[0] + dJ[4]);
     j9[1] -= dW[2]; j9[2] += dW[1]; j9[3] += dW[2]; j9[5] -= dW[0]; j9[6] -= dW[1]; j9[7] += dW[0];
 #pragma unroll
-    for (int k = 0; k < 3; k++) U[3 * (int64_t)idx + k] += dU[k];
+    for (int k = 0; k < 3; k++) U[3 * (int64_t)me.idx + k] += dU[k];
 #pragma unroll
-    for (int k = 0; k < 9; k++) J[9 * (int64_t)idx + k] += j9[k];
+    for (int k = 0; k < 9; k++) J[9 * (int64_t)me.idx + k] += j9[k];
 }
 
 // --------------------------------------------------------------------- UJ, FP64
@@ -226,107 +248,126 @@ __device__ __forceinline__ void leaf_pair_f64(double tx, double ty, double tz, c
 }
 
 template <int K>
-__global__ void __launch_bounds__(LEAF_MAX)
-leaf_uj_f64(const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb, const int32_t* __restrict__ le,
-            const int32_t* __restrict__ row, const int32_t* __restrict__ col,
-            const SrcF64* __restrict__ src, double* U, double* J)
+__global__ void __launch_bounds__(NF_THREADS)
+nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
+          const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const SrcF64* __restrict__ src,
+          double* U, double* J)
 {
-    __shared__ SrcF64 tile[LEAF_MAX];
-    const int leaf = blockIdx.x;
-    const int64_t t = (int64_t)lb[leaf] + threadIdx.x;
-    const bool valid = t < le[leaf];
-    double tx = 1.0e3, ty = 1.0e3, tz = 1.0e3;
-    int32_t idx = 0;
-    if (valid) {
-        const TgtPos p = tgt[t];
-        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
-    }
+    __shared__ SrcF64 tile[NF_WARPS][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
+    if (grp >= ngroups) return;
+    const GroupTarget me = group_target(n, 32 * grp, lane, tgt, leaf_of);
     double acc[12];
 #pragma unroll
     for (int k = 0; k < 12; k++) acc[k] = 0.0;
-    for (int e = row[leaf]; e < row[leaf + 1]; e++) {
-        const int sl = col[e];
-        const int cnt = le[sl] - lb[sl];
-        __syncthreads();
-        if (threadIdx.x < cnt) tile[threadIdx.x] = src[(int64_t)lb[sl] + threadIdx.x];
-        __syncthreads();
-        for (int j = 0; j < cnt; j++) leaf_pair_f64<K>(tx, ty, tz, tile[j], acc);
+    const int e1 = grp_row[grp + 1];
+    for (int e = grp_row[grp]; e < e1; e++) {
+        const int4 iv = ivs[e];
+        const bool act = me.valid && (((unsigned)iv.z >> me.local) & 1u);
+        for (int base = iv.x; base < iv.y; base += 32) {
+            const int cnt = min(32, iv.y - base);
+            __syncwarp();
+            if (lane < cnt) tile[warp][lane] = src[base + lane];
+            __syncwarp();
+            if (act)
+                for (int j = 0; j < cnt; j++) leaf_pair_f64<K>(me.tx, me.ty, me.tz, tile[warp][j], acc);
+        }
     }
-    if (!valid) return;
+    if (!me.valid) return;
 #pragma unroll
-    for (int k = 0; k < 3; k++) U[3 * (int64_t)idx + k] += acc[k];
+    for (int k = 0; k < 3; k++) U[3 * (int64_t)me.idx + k] += acc[k];
 #pragma unroll
-    for (int k = 0; k < 9; k++) J[9 * (int64_t)idx + k] += acc[3 + k];
+    for (int k = 0; k < 9; k++) J[9 * (int64_t)me.idx + k] += acc[3 + k];
 }
 
 // ------------------------------------------------------------------------- Estr
+// SFS_t += J_t^T sum_s z_s g_s - sum_s z_s v_s  (z = zeta(r/sigma_s), g and v
+// pre-scaled by ZNORM / sigma_s^3 in the pack), over the group's intervals,
+// skipping the self pair, for non-static targets.
 template <int K, bool MIXED>
-__global__ void __launch_bounds__(LEAF_MAX)
-leaf_estr(const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb, const int32_t* __restrict__ le,
-          const int32_t* __restrict__ row, const int32_t* __restrict__ col, const void* __restrict__ srcv,
-          const double* __restrict__ Jt, const uint8_t* __restrict__ static_t, bool transposed, double* SFS)
+__global__ void __launch_bounds__(NF_THREADS)
+nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
+        const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const void* __restrict__ srcv,
+        const double* __restrict__ Jt, const uint8_t* __restrict__ static_t, bool transposed, double* SFS)
 {
-    __shared__ __align__(16) unsigned char tile_raw[LEAF_MAX * (MIXED ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64))];
-    __shared__ float4 s_hi[LEAF_MAX], s_lo[LEAF_MAX];   // mixed: double-float source positions
-    const int leaf = blockIdx.x;
-    const int64_t t = (int64_t)lb[leaf] + threadIdx.x;
-    const bool in = t < le[leaf];
-    double tx = 1.0e3, ty = 1.0e3, tz = 1.0e3;
-    int32_t idx = 0;
-    if (in) {
-        const TgtPos p = tgt[t];
-        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
-    }
-    const bool valid = in && !(static_t && static_t[idx]);
-    const float3 th = make_float3((float)tx, (float)ty, (float)tz);
-    const float3 tl = make_float3((float)(tx - (double)th.x), (float)(ty - (double)th.y), (float)(tz - (double)th.z));
+    constexpr size_t SZ = MIXED ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64);
+    __shared__ __align__(16) unsigned char tile_raw[NF_WARPS][32 * SZ];
+    __shared__ float4 s_hi[NF_WARPS][32], s_lo[NF_WARPS][32];   // mixed: double-float source positions
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
+    if (grp >= ngroups) return;
+    const int64_t p0 = 32 * grp;
+    const GroupTarget me = group_target(n, p0, lane, tgt, leaf_of);
+    const bool live = me.valid && !(static_t && static_t[me.idx]);
+    const int64_t t = p0 + lane;
+    const float3 th = make_float3((float)me.tx, (float)me.ty, (float)me.tz);
+    const float3 tl = make_float3((float)(me.tx - (double)th.x), (float)(me.ty - (double)th.y),
+                                  (float)(me.tz - (double)th.z));
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
-    for (int e = row[leaf]; e < row[leaf + 1]; e++) {
-        const int sl = col[e];
-        const int64_t sb = lb[sl];
-        const int cnt = le[sl] - lb[sl];
-        __syncthreads();
-        if (threadIdx.x < cnt) {
-            if (MIXED) {
-                const SrcEstrMixed p = ((const SrcEstrMixed*)srcv)[sb + threadIdx.x];
-                ((SrcEstrMixed*)tile_raw)[threadIdx.x] = p;
-                const float xh = (float)p.x, yh = (float)p.y, zh = (float)p.z;
-                s_hi[threadIdx.x] = make_float4(xh, yh, zh, p.isig2);
-                s_lo[threadIdx.x] = make_float4((float)(p.x - (double)xh), (float)(p.y - (double)yh),
-                                                (float)(p.z - (double)zh), 0.f);
-            } else {
-                ((SrcEstrF64*)tile_raw)[threadIdx.x] = ((const SrcEstrF64*)srcv)[sb + threadIdx.x];
+    float mg[3] = {0.f, 0.f, 0.f}, mv[3] = {0.f, 0.f, 0.f};
+    int tiles = 0;
+    const int e1 = grp_row[grp + 1];
+    for (int e = grp_row[grp]; e < e1; e++) {
+        const int4 iv = ivs[e];
+        const bool act = live && (((unsigned)iv.z >> me.local) & 1u);
+        for (int base = iv.x; base < iv.y; base += 32) {
+            const int cnt = min(32, iv.y - base);
+            __syncwarp();
+            if (lane < cnt) {
+                if (MIXED) {
+                    const SrcEstrMixed p = ((const SrcEstrMixed*)srcv)[base + lane];
+                    ((SrcEstrMixed*)tile_raw[warp])[lane] = p;
+                    const float xh = (float)p.x, yh = (float)p.y, zh = (float)p.z;
+                    s_hi[warp][lane] = make_float4(xh, yh, zh, p.isig2);
+                    s_lo[warp][lane] = make_float4((float)(p.x - (double)xh), (float)(p.y - (double)yh),
+                                                   (float)(p.z - (double)zh), 0.f);
+                } else {
+                    ((SrcEstrF64*)tile_raw[warp])[lane] = ((const SrcEstrF64*)srcv)[base + lane];
+                }
             }
-        }
-        __syncthreads();
-        float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
-        for (int j = 0; j < cnt; j++) {
-            if (sb + j == t) continue;   // the self pair (sources and targets share the order)
+            __syncwarp();
+            if (!act) continue;
+            const int jself = (int)(t - base);   // the self pair's slot in this tile, if any
             if (MIXED) {
-                const SrcEstrMixed& p = ((const SrcEstrMixed*)tile_raw)[j];
-                const float4 h = s_hi[j], l = s_lo[j];
-                const float dx = (th.x - h.x) + (tl.x - l.x);
-                const float dy = (th.y - h.y) + (tl.y - l.y);
-                const float dz = (th.z - h.z) + (tl.z - l.z);
-                const float z = zhat_f32<K>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * h.w);
-                fg[0] = fmaf(z, p.g.x, fg[0]); fg[1] = fmaf(z, p.g.y, fg[1]); fg[2] = fmaf(z, p.g.z, fg[2]);
-                fv[0] = fmaf(z, p.v.x, fv[0]); fv[1] = fmaf(z, p.v.y, fv[1]); fv[2] = fmaf(z, p.v.z, fv[2]);
-            } else {
-                const SrcEstrF64& p = ((const SrcEstrF64*)tile_raw)[j];
-                const double dx = p.xy.x - tx, dy = p.xy.y - ty, dz = p.z_isig.x - tz;
-                const double isig = p.z_isig.y;
-                const double z = zeta_f64<K>(sqrt(dx * dx + dy * dy + dz * dz) * isig) * isig * isig * isig;
-                zg[0] += z * p.gxy.x; zg[1] += z * p.gxy.y; zg[2] += z * p.gz_vx.x;
-                zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y;
-            }
-        }
-        if (MIXED) {
+                float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
+                for (int j = 0; j < cnt; j++) {
+                    const SrcEstrMixed& p = ((const SrcEstrMixed*)tile_raw[warp])[j];
+                    const float4 h = s_hi[warp][j], l = s_lo[warp][j];
+                    const float dx = (th.x - h.x) + (tl.x - l.x);
+                    const float dy = (th.y - h.y) + (tl.y - l.y);
+                    const float dz = (th.z - h.z) + (tl.z - l.z);
+                    float z = zhat_f32<K>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * h.w);
+                    z = (j == jself) ? 0.0f : z;
+                    fg[0] = fmaf(z, p.g.x, fg[0]); fg[1] = fmaf(z, p.g.y, fg[1]); fg[2] = fmaf(z, p.g.z, fg[2]);
+                    fv[0] = fmaf(z, p.v.x, fv[0]); fv[1] = fmaf(z, p.v.y, fv[1]); fv[2] = fmaf(z, p.v.z, fv[2]);
+                }
 #pragma unroll
-            for (int k = 0; k < 3; k++) { zg[k] += (double)fg[k]; zv[k] += (double)fv[k]; }
+                for (int k = 0; k < 3; k++) { mg[k] += fg[k]; mv[k] += fv[k]; }
+                if (++tiles == NF_BLK_TILES * NF_MID_BLKS) {
+                    tiles = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) { zg[k] += (double)mg[k]; zv[k] += (double)mv[k]; mg[k] = 0.f; mv[k] = 0.f; }
+                }
+            } else {
+                for (int j = 0; j < cnt; j++) {
+                    if (j == jself) continue;
+                    const SrcEstrF64& p = ((const SrcEstrF64*)tile_raw[warp])[j];
+                    const double dx = p.xy.x - me.tx, dy = p.xy.y - me.ty, dz = p.z_isig.x - me.tz;
+                    const double isig = p.z_isig.y;
+                    const double z = zeta_f64<K>(sqrt(dx * dx + dy * dy + dz * dz) * isig) * isig * isig * isig;
+                    zg[0] += z * p.gxy.x; zg[1] += z * p.gxy.y; zg[2] += z * p.gz_vx.x;
+                    zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y;
+                }
+            }
         }
     }
-    if (!valid) return;
-    const double* Jp = Jt + 9 * (int64_t)idx;
+    if (MIXED) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) { zg[k] += (double)mg[k]; zv[k] += (double)mv[k]; }
+    }
+    if (!live) return;
+    const double* Jp = Jt + 9 * (int64_t)me.idx;
     double s[3];
     if (transposed) {
         s[0] = Jp[0] * zg[0] + Jp[1] * zg[1] + Jp[2] * zg[2];
@@ -338,70 +379,53 @@ leaf_estr(const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb, const 
         s[2] = Jp[2] * zg[0] + Jp[5] * zg[1] + Jp[8] * zg[2];
     }
 #pragma unroll
-    for (int k = 0; k < 3; k++) SFS[3 * (int64_t)idx + k] += s[k] - zv[k];
+    for (int k = 0; k < 3; k++) SFS[3 * (int64_t)me.idx + k] += s[k] - zv[k];
 }
 
 // ---------------------------------------------------------------------- launcher
-size_t leaf_work_bytes(int64_t n, int64_t nleaves, int64_t npairs_leaf)
+size_t leaf_work_bytes(int64_t n)
 {
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-    return al(n * sizeof(TgtPos)) + al(n * sizeof(SrcEstrF64)) + al(n * sizeof(int32_t)) +
-           2 * al(nleaves * sizeof(int32_t)) + al((nleaves + 1) * sizeof(int32_t)) + al(npairs_leaf * sizeof(int32_t));
+    return al(n * sizeof(TgtPos)) + al(n * sizeof(SrcEstrF64));
 }
 
 template <int K>
-static cudaError_t launch_leaf_k(const LeafArgs& a, const LeafLists& L, void* work, cudaStream_t st,
+static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* work, cudaStream_t st,
                                  int64_t* launches)
 {
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
     const int64_t n = a.n;
-    const int64_t nl = (int64_t)L.leaf_begin.size();
     char* p = (char*)work;
     TgtPos* tgt = (TgtPos*)p;            p += al(n * sizeof(TgtPos));
-    void* src = p;                       p += al(n * sizeof(SrcEstrF64));
-    int32_t* perm = (int32_t*)p;         p += al(n * sizeof(int32_t));
-    int32_t* lb = (int32_t*)p;           p += al(nl * sizeof(int32_t));
-    int32_t* le = (int32_t*)p;           p += al(nl * sizeof(int32_t));
-    int32_t* row = (int32_t*)p;          p += al((nl + 1) * sizeof(int32_t));
-    int32_t* col = (int32_t*)p;
-    // host -> device copies of the lists (narrowed to int32: n < 2^31)
-    std::vector<int32_t> hb(nl), he(nl), hr(nl + 1);
-    for (int64_t l = 0; l < nl; l++) { hb[l] = (int32_t)L.leaf_begin[l]; he[l] = (int32_t)L.leaf_end[l]; }
-    for (int64_t l = 0; l <= nl; l++) hr[l] = (int32_t)L.row[l];
-    cudaError_t e;
-    if ((e = cudaMemcpyAsync(perm, L.perm.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(lb, hb.data(), nl * sizeof(int32_t), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(le, he.data(), nl * sizeof(int32_t), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(row, hr.data(), (nl + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(col, L.col.data(), L.col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st)))
-        return e;
-    // the host vectors must outlive the copies
-    if ((e = cudaStreamSynchronize(st))) return e;
+    void* src = p;
     const unsigned g = (unsigned)((n + 255) / 256);
-    tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, perm, tgt);
+    const unsigned gb = (unsigned)((L.ngroups + NF_WARPS - 1) / NF_WARPS);
+    tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
     if (a.precision) {
-        leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, perm, (SrcMixed*)src);
-        leaf_uj_mixed<K><<<(unsigned)nl, LEAF_MAX, 0, st>>>(tgt, lb, le, row, col, (const SrcMixed*)src, a.U, a.J);
+        leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
+        nf_uj_mixed<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                  (const SrcMixed*)src, a.U, a.J);
     } else {
-        leaf_pack_f64<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, perm, (SrcF64*)src);
-        leaf_uj_f64<K><<<(unsigned)nl, LEAF_MAX, 0, st>>>(tgt, lb, le, row, col, (const SrcF64*)src, a.U, a.J);
+        leaf_pack_f64<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcF64*)src);
+        nf_uj_f64<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                (const SrcF64*)src, a.U, a.J);
     }
     *launches += 3;
     if (a.sfs) {
-        leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, perm,
+        leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm,
                                               a.precision, src);
         if (a.precision)
-            leaf_estr<K, true><<<(unsigned)nl, LEAF_MAX, 0, st>>>(tgt, lb, le, row, col, src, a.J, a.static_flags,
-                                                                  a.transposed, a.SFS);
+            nf_estr<K, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
+                                                        a.static_flags, a.transposed, a.SFS);
         else
-            leaf_estr<K, false><<<(unsigned)nl, LEAF_MAX, 0, st>>>(tgt, lb, le, row, col, src, a.J, a.static_flags,
-                                                                   a.transposed, a.SFS);
+            nf_estr<K, false><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
+                                                         a.static_flags, a.transposed, a.SFS);
         *launches += 2;
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_leaflist(const LeafArgs& a, const LeafLists& L, void* work, cudaStream_t st, int64_t* launches)
+cudaError_t launch_leaflist(const LeafArgs& a, const NearLists& L, void* work, cudaStream_t st, int64_t* launches)
 {
     if (a.n <= 0) return cudaSuccess;
     switch (a.kernel) {

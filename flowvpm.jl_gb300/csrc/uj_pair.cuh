@@ -1,5 +1,5 @@
 // uj_pair.cuh -- the mixed (FP32-comp) UJ pair machinery shared by the all-pairs
-// kernel (uj.cu) and the near-field leaf-pair kernel (leaflist.cu).
+// kernel (uj.cu) and the near-field warp-group kernel (leaflist.cu).
 #pragma once
 #include "internal.h"
 #include "vpm_math.cuh"
@@ -41,10 +41,12 @@ __device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float G
 //   to      : target offset from the warp origin (FP32)
 //   th, tl  : target double-float position
 //   r2n     : (2 b)^2, b = the warp's extent around its origin
-template <int K>
+//   act     : with MASK, 1 when this lane's target takes these sources, else 0
+//             (every lane still votes and computes: the sum is multiplied by act)
+template <int K, bool MASK = false>
 __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, const float3& tl, float r2n,
                                             const float4* __restrict__ off, const SrcMixed* __restrict__ tile,
-                                            int j0, float (&u)[3], float (&jq)[8], float (&w)[3])
+                                            int j0, float (&u)[3], float (&jq)[8], float (&w)[3], float act = 1.0f)
 {
     float dx[4], dy[4], dz[4], r2[4], hw[4];
     bool far = true;
@@ -70,6 +72,7 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             } else {
                 near_GQ<K>(r2[q] * hw[q], hw[q], G, Q);
             }
+            if constexpr (MASK) { G *= act; Q *= act; }
             accum_pair(dx[q], dy[q], dz[q], G, Q, tile[j0 + q].gam, u, jq, w);
         }
     } else {
@@ -93,6 +96,7 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             const bool nz = e2 > 0.0f;
             G = nz ? G : 0.0f;
             Q = nz ? Q : 0.0f;
+            if constexpr (MASK) { G *= act; Q *= act; }
             accum_pair(ex, ey, ez, G, Q, tile[j0 + q].gam, u, jq, w);
         }
     }

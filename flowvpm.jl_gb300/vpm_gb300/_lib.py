@@ -51,7 +51,10 @@ SIGNATURES = {
     "vpm_uj_adjoint_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int]),
     "vpm_p2p_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int,
                                     _vp]),
+    "vpm_p2p_lists_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
+                                 _int, _int, _int, _vp]),
     "vpm_leaflist_host": (_int, [_i64, _vp, _int, _dbl, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "vpm_leaflist_dev": (_int, [_vp, _i64, _vp, _int, _dbl, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 
@@ -214,6 +217,43 @@ class Context:
                                                  float(theta), int(kernel), int(precision), flags,
                                                  stats.ctypes.data))
         return tuple(int(v) for v in stats)
+
+    def p2p_lists_dev(self, x, gam, sig, U, J, lists, sfs_out=None, *, kernel: int = KERNEL_GAUSSIANERF,
+                      precision: int = FP32COMP, sfs: bool = False, transposed: bool = True, static=None):
+        """Near-field P2P over caller-supplied host lists (perm, leaf_begin, leaf_end, row, col);
+        returns (leaves, leaf pairs, particle pairs)."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(U, 3); _check_dev(J, 9)
+        if sfs:
+            _check_dev(sfs_out, 3)
+        perm, lb, le, row, col = (np.ascontiguousarray(lists[0], np.int32), np.ascontiguousarray(lists[1], np.int64),
+                                  np.ascontiguousarray(lists[2], np.int64), np.ascontiguousarray(lists[3], np.int64),
+                                  np.ascontiguousarray(lists[4], np.int32))
+        self._torch_stream()
+        stats = np.zeros(3, dtype=np.int64)
+        flags = (SFS if sfs else 0) | (TRANSPOSED if transposed else 0)
+        self._check(self._L.vpm_p2p_lists_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(static),
+                                              _ptr(U), _ptr(J), _ptr(sfs_out) if sfs else None, perm.ctypes.data,
+                                              lb.shape[0], lb.ctypes.data, le.ctypes.data, row.ctypes.data,
+                                              col.ctypes.data if col.size else None, int(kernel), int(precision),
+                                              flags, stats.ctypes.data))
+        return tuple(int(v) for v in stats)
+
+    def leaflist_dev(self, x, leaf_size: int = 64, theta: float = 0.4):
+        """The leaf-pair lists built on the GPU from device positions x[n,3]:
+        (perm, leaf_begin, leaf_end, row, col, particle pairs)."""
+        _check_dev(x, 3)
+        self._torch_stream()
+        n = x.shape[0]
+        sizes = np.zeros(3, dtype=np.int64)
+        self._check(self._L.vpm_leaflist_dev(self._h, n, _ptr(x), int(leaf_size), float(theta), None, None, None,
+                                             None, None, sizes.ctypes.data))
+        nl, nc = int(sizes[0]), int(sizes[1])
+        perm = np.zeros(n, np.int32); lb = np.zeros(nl, np.int64); le = np.zeros(nl, np.int64)
+        row = np.zeros(nl + 1, np.int64); col = np.zeros(max(nc, 1), np.int32)
+        self._check(self._L.vpm_leaflist_dev(self._h, n, _ptr(x), int(leaf_size), float(theta), perm.ctypes.data,
+                                             lb.ctypes.data, le.ctypes.data, row.ctypes.data, col.ctypes.data,
+                                             sizes.ctypes.data))
+        return perm, lb, le, row, col[:nc], int(sizes[2])
 
     def estr_dev(self, xt, Jt, xs, gs, sgs, Js, SFS, kernel: int, precision: int, transposed: bool = True,
                  static_t=None, static_s=None):

@@ -1,0 +1,210 @@
+"""Device-resident rVPM time step: the particle state stays in GPU memory
+across a step and between steps, and every particle-to-particle evaluation is a
+call into libvpm_gb300 (all pairs, or the near-field leaf pairs).
+
+The per-particle work around UJ is the reference's, restated on float64 CUDA
+tensors in the reference's operation order:
+  * rVPM low-storage RK3, src/FLOWVPM_timeintegration.jl:388-532;
+  * the pseudo-three-level dynamic SFS procedure with Lagrangian averaging,
+    bounds and the NaN check, src/FLOWVPM_subfilterscale.jl:447-673, and
+    backscatter clipping, :287-296;
+  * core spreading (RK3 branch), src/FLOWVPM_viscous.jl:175-220;
+  * Pedrizzetti relaxation, src/FLOWVPM_relaxation.jl:62-81.
+Static particles are not supported in this form (the host mirror has them).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import torch
+
+from . import _lib
+from .autodiff import STAGES, _stretch
+
+EPS = 2.220446049250313e-16
+
+
+@dataclass
+class DeviceField:
+    """SoA particle state on the device (float64), the rows of the reference's
+    particle matrix that the step uses."""
+    x: torch.Tensor            # [n,3]  X
+    gam: torch.Tensor          # [n,3]  Gamma
+    sig: torch.Tensor          # [n]    sigma
+    kernel: int = _lib.KERNEL_GAUSSIANERF
+    precision: int = _lib.FP32COMP
+    f: float = 0.0             # ReformulatedVPM(f, g)
+    g: float = 0.2
+    transposed: bool = True
+    t: float = 0.0
+    nt: int = 0
+    U: torch.Tensor = None     # [n,3]
+    J: torch.Tensor = None     # [n,9]
+    SFS: torch.Tensor = None   # [n,3]
+    C: torch.Tensor = None     # [n,3]  C_INDEX rows (coefficient, Lagrangian numerator, denominator)
+    M: torch.Tensor = None     # [n,9]  M_INDEX rows
+    # near-field evaluation instead of all pairs (FMM near field: leaf size, theta)
+    leaflist: tuple | None = None
+
+    def __post_init__(self):
+        n = self.x.shape[0]
+        z = lambda k: torch.zeros(n, k, dtype=torch.float64, device=self.x.device)
+        self.U = z(3) if self.U is None else self.U
+        self.J = z(9) if self.J is None else self.J
+        self.SFS = z(3) if self.SFS is None else self.SFS
+        self.C = z(3) if self.C is None else self.C
+        self.M = z(9) if self.M is None else self.M
+
+    @property
+    def n(self) -> int:
+        return self.x.shape[0]
+
+
+def uj(fld: DeviceField, ctx: _lib.Context, *, sfs: bool = False, reset: bool = True, reset_sfs: bool = False):
+    """UJ_direct semantics on the device state (no static particles)."""
+    if reset:
+        fld.U.zero_()
+        fld.J.zero_()
+    if reset_sfs:
+        fld.SFS.zero_()
+    if fld.leaflist is None:
+        ctx.uj_dev(fld.x, fld.x, fld.gam, fld.sig, fld.U, fld.J, fld.kernel, fld.precision)
+        if sfs:
+            ctx.estr_dev(fld.x, fld.J, fld.x, fld.gam, fld.sig, fld.J, fld.SFS, fld.kernel, fld.precision,
+                         fld.transposed)
+    else:
+        leaf_size, theta = fld.leaflist
+        ctx.p2p_leaflist_dev(fld.x, fld.gam, fld.sig, fld.U, fld.J, fld.SFS if sfs else None, leaf_size=leaf_size,
+                             theta=theta, kernel=fld.kernel, precision=fld.precision, sfs=sfs,
+                             transposed=fld.transposed)
+
+
+@dataclass
+class DynamicSFSParams:
+    """DynamicSFS settings; defaults = SFS_Cd_twolevel_nobackscatter (src/FLOWVPM.jl:223)."""
+    alpha: float = 0.999
+    rlxf: float = 0.005
+    minC: float = 0.0
+    maxC: float = 1.0
+    force_positive: bool = True
+    clip_backscatter: bool = True
+
+
+@dataclass
+class CoreSpreadingParams:
+    nu: float
+    sgm0: float
+    beta: float = 1.5
+    t_sgm: float = 0.0
+
+
+def _zeta0(kernel: int) -> float:
+    from .particlefield import standard_kernels
+    return standard_kernels[kernel].zeta(0.0)
+
+
+def _dynamic_before(fld, ctx, p: DynamicSFSParams):
+    fld.sig *= p.alpha
+    uj(fld, ctx, sfs=True, reset=True, reset_sfs=True)
+    fld.M.zero_()
+    fld.M[:, 0:3] = _stretch(fld.J, fld.gam, fld.transposed)
+    fld.M[:, 3:6] = fld.SFS
+    fld.sig /= p.alpha
+
+
+def _dynamic_after(fld, p: DynamicSFSParams, zeta0: float):
+    G = fld.gam
+    M = fld.M
+    M[:, 0:3] -= _stretch(fld.J, G, fld.transposed)
+    M[:, 3:6] -= fld.SFS
+    s = fld.sig
+    nume = (M[:, 0] * G[:, 0] + M[:, 1] * G[:, 1] + M[:, 2] * G[:, 2]) * (3 * p.alpha - 2)
+    deno = (M[:, 3] * G[:, 0] + M[:, 4] * G[:, 1] + M[:, 5] * G[:, 2]) / (zeta0 / (s * s * s))
+    Cp = fld.C
+    C3 = torch.where(Cp[:, 2] == 0, deno, Cp[:, 2])
+    C3 = torch.where(C3 == 0, torch.full_like(C3, EPS), C3)
+    nume = p.rlxf * nume + (1 - p.rlxf) * Cp[:, 1]
+    deno = p.rlxf * deno + (1 - p.rlxf) * C3
+    ratio = (nume / deno).abs()
+    big = ratio > p.maxC
+    deno = torch.where(big & (deno.abs() < C3.abs()), torch.sign(deno) * C3.abs(), deno)
+    nume = torch.where(big & ((nume / deno).abs() >= p.maxC), torch.sign(nume) * deno.abs() * p.maxC, nume)
+    small = (~big) & (ratio < p.minC)
+    nume = torch.where(small, torch.sign(nume) * deno.abs() * p.minC, nume)
+    C1 = nume / deno
+    if bool(torch.isnan(C1).any()):
+        raise FloatingPointError("NaN in dynamicprocedure_pseudo3level_afterUJ")
+    if p.force_positive:
+        C1 = C1 * torch.sign(C1)
+    Cp[:, 0] = C1
+    Cp[:, 1] = nume
+    Cp[:, 2] = deno
+    M.zero_()
+    if p.clip_backscatter:
+        clip = Cp[:, 0] * (G * fld.SFS).sum(1) < 0
+        Cp[:, 0] = torch.where(clip, Cp[:, 0] * 0, Cp[:, 0])
+
+
+def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSParams | None = None,
+             viscous: CoreSpreadingParams | None = None, relax_rlxf: float | None = None,
+             Uinf=(0.0, 0.0, 0.0)):
+    """One rungekutta3 step (+ relaxation when relax_rlxf is given) of the device state."""
+    zeta0 = _zeta0(fld.kernel)
+    f, g = fld.f, fld.g
+    Uinf = torch.tensor(Uinf, dtype=torch.float64, device=fld.x.device)
+    fld.M.zero_()
+    for a, b in STAGES:
+        first = (a == 1 or a == 0)
+        if sfs is not None and first:
+            _dynamic_before(fld, ctx, sfs)
+        uj(fld, ctx, sfs=sfs is not None, reset=True, reset_sfs=sfs is not None)
+        if sfs is not None and first:
+            _dynamic_after(fld, sfs, zeta0)
+        # update_particle_states (src/FLOWVPM_timeintegration.jl:463-532)
+        M, G, s = fld.M, fld.gam, fld.sig
+        C = fld.C[:, 0]
+        S = fld.SFS
+        M[:, 0:3] = a * M[:, 0:3] + dt * (fld.U + Uinf)
+        fld.x += b * M[:, 0:3]
+        MM = _stretch(fld.J, G, fld.transposed)
+        Gn2 = (G * G).sum(1)
+        s3 = s * s * s
+        MM4 = (f + g) / (1 + 3 * f) * (MM * G).sum(1)
+        MM4 = MM4 - f / (1 + 3 * f) * (C * S[:, 0] * G[:, 0] + C * S[:, 1] * G[:, 1] + C * S[:, 2] * G[:, 2]) * s3 / zeta0
+        pos = Gn2 > 0
+        MM4 = torch.where(pos, MM4 / torch.where(pos, Gn2, torch.ones_like(Gn2)), torch.zeros_like(Gn2))
+        M[:, 3:6] = a * M[:, 3:6] + dt * (MM - 3 * MM4[:, None] * G - C[:, None] * S * s3[:, None] / zeta0)
+        M[:, 7] = a * M[:, 7] - dt * (s * MM4)
+        G += b * M[:, 3:6]
+        s += b * M[:, 7]
+        # core spreading (src/FLOWVPM_viscous.jl:175-220)
+        if viscous is not None:
+            M[:, 6] = a * M[:, 6] + dt * 2 * viscous.nu
+            fld.sig.copy_(torch.sqrt(fld.sig ** 2 + b * M[:, 6]))
+            if abs(b - 8 / 15) <= 1e-7:
+                viscous.t_sgm += dt
+                beta = math.sqrt(2 * viscous.nu * viscous.t_sgm / viscous.sgm0 ** 2 + 1)
+                if beta >= viscous.beta:
+                    raise NotImplementedError("core-spreading reset (zeta/RBF) is not part of this library")
+    if relax_rlxf is not None:
+        uj(fld, ctx)
+        J = fld.J
+        w = torch.stack([J[:, 5] - J[:, 7], J[:, 6] - J[:, 2], J[:, 1] - J[:, 3]], dim=1)
+        nw = torch.sqrt((w * w).sum(1))
+        nG = torch.sqrt((fld.gam * fld.gam).sum(1))
+        ok = nw != 0
+        newg = (1 - relax_rlxf) * fld.gam + relax_rlxf * (nG / torch.where(ok, nw, torch.ones_like(nw)))[:, None] * w
+        fld.gam.copy_(torch.where(ok[:, None], newg, fld.gam))
+    fld.t += dt
+    fld.nt += 1
+
+
+def impulse(fld: DeviceField) -> torch.Tensor:
+    """Linear impulse I = 1/2 sum x_p x Gamma_p."""
+    return 0.5 * torch.cross(fld.x, fld.gam, dim=1).sum(0)
+
+
+def energy(fld: DeviceField) -> float:
+    """Kinetic-energy estimate E = 1/2 sum U_p . (x_p x Gamma_p), from the U of the last evaluation."""
+    return float(0.5 * (fld.U * torch.cross(fld.x, fld.gam, dim=1)).sum())

@@ -166,27 +166,49 @@ int vpm_uj_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* g
                        double* sbar, int kernel, int precision);
 
 /* Near-field leg of UJ_fmm (src/FLOWVPM_UJ.jl:90-125): builds an octree of the
- * n particles on the host (leaves of at most leaf_size <= 64 particles) and
- * adds U[n,3], J[n,9] -- and, with VPM_SFS, Estr into SFS[n,3] -- from the
- * direct P2P of every leaf pair that fails the multipole acceptance criterion
- * theta * r < R1 + R2 (r: distance of the cell centres, R: cell radii;
- * src/FLOWVPM_particlefield.jl:28-36), as FastMultipole's direct_list does.
- * The far field is not computed.  flags: VPM_SFS, VPM_TRANSPOSED.  Device
- * pointers; static_flags may be NULL.  stats (may be NULL) receives
- * {leaves, leaf pairs, particle pairs}. */
+ * n particles on the GPU (leaves of at most leaf_size particles,
+ * 1 <= leaf_size <= 4096) and adds U[n,3], J[n,9] -- and, with VPM_SFS, Estr
+ * into SFS[n,3] -- from the direct P2P of every leaf pair that fails the
+ * multipole acceptance criterion theta * r < R1 + R2 (r: distance of the cell
+ * centres, R: cell radii; src/FLOWVPM_particlefield.jl:28-36), as
+ * FastMultipole's direct_list does.  The far field is not computed.  flags:
+ * VPM_SFS, VPM_TRANSPOSED.  Device pointers; static_flags may be NULL.  stats
+ * (may be NULL) receives {leaves, leaf pairs, particle pairs}.  The lists are
+ * the ones vpm_leaflist_host builds, entry for entry. */
 int vpm_p2p_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
                          const uint8_t* static_flags, double* U, double* J, double* SFS,
                          int leaf_size, double theta, int kernel, int precision, int flags,
                          int64_t* stats);
 
-/* The octree leaf-pair lists vpm_p2p_leaflist_dev builds (host memory, no GPU).
+/* The same near-field P2P over leaf-pair lists the caller supplies in host
+ * memory (for instance FastMultipole's direct_list of the reference's own
+ * tree): particle perm[p] is at tree position p (perm a permutation of
+ * 0..n-1), leaf l holds the positions [leaf_begin[l], leaf_end[l]) (leaves
+ * contiguous, non-empty, in order, covering 0..n-1), and its source leaves are
+ * col[row[l] .. row[l+1]) (each row is sorted here; a repeated entry is an
+ * error).  Other arguments as vpm_p2p_leaflist_dev; stats[2] receives the
+ * particle pairs. */
+int vpm_p2p_lists_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                      const uint8_t* static_flags, double* U, double* J, double* SFS,
+                      const int32_t* perm, int64_t nleaves, const int64_t* leaf_begin,
+                      const int64_t* leaf_end, const int64_t* row, const int32_t* col,
+                      int kernel, int precision, int flags, int64_t* stats);
+
+/* The octree leaf-pair lists of n positions, built on the host (no GPU).
  * Call once with perm == NULL to get sizes[0] = leaves, sizes[1] = leaf pairs;
  * then with perm[n], leaf_begin[leaves], leaf_end[leaves], row[leaves+1],
  * col[leaf pairs]: particle i of the tree order is perm[i], leaf l holds tree
  * positions [leaf_begin[l], leaf_end[l]), and its source leaves are
- * col[row[l] .. row[l+1]). */
+ * col[row[l] .. row[l+1]) in increasing order. */
 int vpm_leaflist_host(int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
                       int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes);
+
+/* The same lists built on the GPU from device positions x[n,3] (what
+ * vpm_p2p_leaflist_dev uses), copied to the host arrays as vpm_leaflist_host
+ * fills them.  sizes[0..2] = leaves, leaf pairs, particle pairs; with
+ * perm == NULL only the sizes are returned. */
+int vpm_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
+                     int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes);
 
 /* ------------------------------------------------ allocation-free variant */
 
