@@ -354,16 +354,21 @@ def adjoint_ratio(ctx, vpm, torch, n=32000):
         with torch.no_grad():
             ad.ring_loss(*ad.rollout(x, g, sg, 0.01, steps, checkpoint=False, **kw), **kw)
 
-    def roll_grad():
-        xx, gg, ss = x.clone().requires_grad_(), g.clone().requires_grad_(), sg.clone().requires_grad_()
-        ad.ring_loss(*ad.rollout(xx, gg, ss, 0.01, steps, checkpoint=True, **kw), **kw).backward()
+    def roll_grad(mode):
+        def run():
+            xx, gg, ss = x.clone().requires_grad_(), g.clone().requires_grad_(), sg.clone().requires_grad_()
+            ad.ring_loss(*ad.rollout(xx, gg, ss, 0.01, steps, checkpoint=mode, **kw), **kw).backward()
+        return run
     t_roll = timed(roll_fwd)
-    t_grad = timed(roll_grad)
+    t_grad = timed(roll_grad(True))
+    t_grad_rc = timed(roll_grad("recompute"))
     return {"n_particles": n, "uj_fwd_ms": fwd, "uj_adjoint_ms": adj, "uj_adjoint_over_fwd": adj / fwd,
             "rollout_steps": steps, "rollout_fwd_ms": t_roll, "rollout_grad_ms": t_grad,
-            "rollout_grad_over_fwd": t_grad / t_roll,
-            "note": "FP64 forward and adjoint, Gaussian-erf; rollout_grad includes the forward pass and the "
-                    "per-step recompute of checkpointing"}
+            "rollout_grad_over_fwd": t_grad / t_roll, "rollout_backward_over_fwd": (t_grad - t_roll) / t_roll,
+            "rollout_grad_recompute_ms": t_grad_rc, "rollout_grad_recompute_over_fwd": t_grad_rc / t_roll,
+            "note": "FP64 forward and adjoint, Gaussian-erf.  rollout_grad = forward + backward with per-step "
+                    "checkpointing that keeps each step's UJ values; backward = rollout_grad - forward; "
+                    "_recompute re-runs each step's UJ evaluations in the backward pass"}
 
 
 def measure_ffma_peak(ctx) -> float:
@@ -462,17 +467,18 @@ def run_leapfrog(args):
     from vpm_gb300 import device_step as ds, workloads
     ctx = vpm.Context(0)
     dt = 0.005
-    X, G, s = workloads.leapfrog_rings(args.lf_n, nper=10)
-    n = X.shape[0]
-    ms32, mon32, f32 = _leapfrog_run(ctx, X, G, s, vpm.FP32COMP, args.lf_steps, dt, 20, torch, ds)
+    out = {"mode": "leapfrog", "steps": args.lf_steps, "dt": dt, "precision": "fp32comp"}
     uj_per_step, estr_per_step = 5, 4     # dynamic SFS: test-filter UJ + 3 stages (with Estr), relaxation UJ
-    out = {"mode": "leapfrog", "n_particles": n, "steps": args.lf_steps, "dt": dt, "precision": "fp32comp",
-           "ms_per_step": ms32, "particle_steps_per_s": n / (ms32 / 1e3),
-           "pairs_per_s": (uj_per_step + estr_per_step) * float(n) * n / (ms32 / 1e3),
-           "uj_calls_per_step": uj_per_step, "estr_calls_per_step": estr_per_step,
-           "drift_fp32comp": _drift(mon32), "monitor_fp32comp": mon32}
+    if args.lf_n > 0:
+        X, G, s = workloads.leapfrog_rings(args.lf_n, nper=10)
+        n = X.shape[0]
+        ms32, mon32, f32 = _leapfrog_run(ctx, X, G, s, vpm.FP32COMP, args.lf_steps, dt, 20, torch, ds)
+        out.update({"n_particles": n, "ms_per_step": ms32, "particle_steps_per_s": n / (ms32 / 1e3),
+                    "pairs_per_s": (uj_per_step + estr_per_step) * float(n) * n / (ms32 / 1e3),
+                    "uj_calls_per_step": uj_per_step, "estr_calls_per_step": estr_per_step,
+                    "drift_fp32comp": _drift(mon32), "monitor_fp32comp": mon32})
     # FP64 vs FP32-comp on the full-size field over a few steps
-    k64 = args.lf_f64_steps
+    k64 = args.lf_f64_steps if args.lf_n > 0 else 0
     if k64 > 0:
         ms64, m64, f64 = _leapfrog_run(ctx, X, G, s, vpm.FP64, k64, dt, k64, torch, ds)
         _, m32s, f32s = _leapfrog_run(ctx, X, G, s, vpm.FP32COMP, k64, dt, k64, torch, ds)

@@ -176,6 +176,14 @@ __global__ void positions_of_matrix(int64_t np, const double* __restrict__ mat, 
 }
 
 // Sets *flag if any of rows [r0, r1) of the first np columns is not finite.
+// rows [r0, r1) of every column set to zero
+__global__ void zero_rows(int64_t np, double* __restrict__ mat, int r0, int r1)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    for (int r = r0; r < r1; r++) mat[i * VPM_NFIELDS + r] = 0.0;
+}
+
 __global__ void check_rows_finite(int64_t np, const double* __restrict__ mat, int r0, int r1, int* flag)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -542,6 +550,73 @@ int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, con
     e.transposed = (flags & VPM_TRANSPOSED) != 0;
     e.self = (xt == xs) && (nt == ns);
     CK(launch_estr(e, w, c->num_sms, c->stream, &c->launches), "Estr kernels");
+    return bounded_wait(c);
+}
+
+// --------------------------------------------------------------- zeta (RBF basis)
+int vpm_zeta_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const double* xs, const double* gs,
+                 const double* sgs, double* W, int kernel, int precision)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_zeta_dev: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+        return fail(c, VPM_ERR_ARG, "vpm_zeta_dev: sizes out of range");
+    RC(check_kernel(c, kernel, precision));
+    if (nt == 0 || ns == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(xt) || !is_device_ptr(xs) || !is_device_ptr(gs) || !is_device_ptr(sgs) || !is_device_ptr(W))
+        return fail(c, VPM_ERR_ARG, "vpm_zeta_dev: every array must be a device pointer");
+    Workspace w;
+    RC(ensure_work(c, nt, ns, precision, true, &w));
+    EstrArgs e;
+    e.nt = nt; e.ns = ns; e.xt = xt; e.Jt = nullptr; e.ldJt = 9; e.static_t = nullptr;
+    e.xs = xs; e.gs = gs; e.sgs = sgs; e.Js = nullptr; e.ldJs = 9; e.static_s = nullptr;
+    e.SFS = W; e.ldS = 3; e.kernel = kernel; e.precision = precision;
+    e.transposed = true; e.self = (xt == xs) && (nt == ns); e.zeta = true;
+    CK(launch_estr(e, w, c->num_sms, c->stream, &c->launches), "zeta kernels");
+    return bounded_wait(c);
+}
+
+int vpm_zeta(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, int precision)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_zeta: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (!particles && np > 0) return fail(c, VPM_ERR_ARG, "vpm_zeta: particles is NULL");
+    if (ld != VPM_NFIELDS) return fail(c, VPM_ERR_ARG, "vpm_zeta: ld must be %d (got %lld)", VPM_NFIELDS, (long long)ld);
+    if (np < 0 || np > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_zeta: np=%lld out of range", (long long)np);
+    RC(check_kernel(c, kernel, precision));
+    if (np == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    cudaStream_t st = c->stream;
+    const size_t mat_bytes = (size_t)VPM_NFIELDS * np * sizeof(double);
+    RC(grow(c, c->mat, mat_bytes, "particle matrix"));
+    RC(grow(c, c->x, 3 * np * sizeof(double), "positions"));
+    RC(grow(c, c->g, 3 * np * sizeof(double), "strengths"));
+    RC(grow(c, c->s, np * sizeof(double), "core sizes"));
+    RC(grow(c, c->st, np, "static flags"));
+    Workspace w;
+    RC(ensure_work(c, np, np, precision, true, &w));
+    double* mat = (double*)c->mat.p;
+    double* x = (double*)c->x.p;
+    double* g = (double*)c->g.p;
+    double* s = (double*)c->s.p;
+    CK(cudaMemcpyAsync(mat, particles, mat_bytes, cudaMemcpyHostToDevice, st), "H2D particle matrix");
+    unpack_matrix<<<nblk(np), EB, 0, st>>>(np, mat, 0, x, g, s, (uint8_t*)c->st.p);
+    zero_rows<<<nblk(np), EB, 0, st>>>(np, mat, R_J, R_J + 3);   // J[1:3] of every particle, statics included
+    c->launches += 2;
+    CK(cudaGetLastError(), "unpack_matrix");
+    EstrArgs e;
+    e.nt = np; e.ns = np; e.xt = x; e.Jt = nullptr; e.ldJt = VPM_NFIELDS; e.static_t = nullptr;
+    e.xs = x; e.gs = g; e.sgs = s; e.Js = nullptr; e.ldJs = VPM_NFIELDS; e.static_s = nullptr;
+    e.SFS = mat + R_J; e.ldS = VPM_NFIELDS; e.kernel = kernel; e.precision = precision;
+    e.transposed = true; e.self = true; e.zeta = true;
+    CK(launch_estr(e, w, c->num_sms, st, &c->launches), "zeta kernels");
+    RC(bounded_wait(c));
+    const size_t pitch = VPM_NFIELDS * sizeof(double);
+    CK(cudaMemcpy2DAsync(particles + R_J, pitch, mat + R_J, pitch, 3 * sizeof(double), (size_t)np,
+                         cudaMemcpyDeviceToHost, st), "D2H rows 16:18");
     return bounded_wait(c);
 }
 

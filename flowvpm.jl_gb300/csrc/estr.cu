@@ -12,13 +12,24 @@
 // zero strength; static targets are left untouched.  Targets run in Morton
 // order (order.cu) like the UJ kernels.  The FP64 kernel keeps the reference's
 // zeta formula; the mixed kernel uses FP32 pair math on per-warp FP32 offsets
-// (see uj.cu) and FP64 accumulation of FP32 blocks.
+// (see uj.cu) and FP64 accumulation of FP32 blocks, and skips every pair at
+// r = 0 (the self pair, and coincident particles, whose J are equal so that
+// their reference term is zero; in the factored form their two terms would
+// only cancel to FP32 rounding, at the largest weight zeta(0)).
 #include "internal.h"
 #include "vpm_math.cuh"
 
 namespace vpm {
 
 static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// Sources summed in plain FP32 before a compensated add.  J_t^T Zg - Zv is a
+// difference of two sums far larger than itself (by |J| / |J_t - J_s| and by
+// the cancellation of neighbours on either side of a target), so their FP32
+// rounding is what limits the mixed Estr; sums of 8 added with compensation
+// bring it from ~1e-5 to ~2e-6 of max |SFS| on a smooth field.
+constexpr int ESTR_SUB = 8;
+static_assert(UJ_BLOCK % ESTR_SUB == 0, "whole sub-blocks");
 
 size_t estr_src_pack_bytes(int64_t ns, int precision)
 {
@@ -62,8 +73,8 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
         const bool off = static_s && static_s[i];
         const double k = off ? 0.0 : zeta_norm(K) * isig2 * isig;
         const double gx = gs[3 * i], gy = gs[3 * i + 1], gz = gs[3 * i + 2];
-        double vx, vy, vz;
-        stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
+        double vx = 0.0, vy = 0.0, vz = 0.0;   // the zeta field (Js null) needs no v
+        if (Js) stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
         p.g = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), 0.f);
         p.v = make_float4((float)(k * vx), (float)(k * vy), (float)(k * vz), 0.f);
     } else {
@@ -87,8 +98,8 @@ __global__ void pack_estr_f64(int64_t ns, int64_t ns_pad, const double* __restri
     if (i < ns) {
         const bool off = static_s && static_s[i];
         const double gx = off ? 0.0 : gs[3 * i], gy = off ? 0.0 : gs[3 * i + 1], gz = off ? 0.0 : gs[3 * i + 2];
-        double vx, vy, vz;
-        stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
+        double vx = 0.0, vy = 0.0, vz = 0.0;
+        if (Js) stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
         p.xy = make_double2(xs[3 * i], xs[3 * i + 1]);
         p.z_isig = make_double2(xs[3 * i + 2], 1.0 / sgs[i]);
         p.gxy = make_double2(gx, gy);
@@ -139,7 +150,10 @@ __global__ void estr_reduce(int64_t nt, int nsplit, const double* __restrict__ p
     }
 }
 
-template <int K>
+// With ZETA the kernels evaluate zeta_direct instead (src/FLOWVPM_viscous.jl:467-488):
+// W_t += sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s over every source and target, the
+// self pair included, written to the SFS output.
+template <int K, bool ZETA>
 __global__ void __launch_bounds__(UJ_THREADS)
 estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
                 const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrF64* __restrict__ src,
@@ -154,8 +168,8 @@ estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __rest
         const TgtPos p = tgt[t];
         tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
     }
-    const bool valid = t < nt && !(static_t && static_t[idx]);
-    const int64_t self_idx = self ? idx : -1;
+    const bool valid = t < nt && (ZETA || !(static_t && static_t[idx]));
+    const int64_t self_idx = (self && !ZETA) ? idx : -1;
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
@@ -172,16 +186,17 @@ estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __rest
             const double isig = p.z_isig.y;
             const double z = zeta_f64<K>(r * isig) * isig * isig * isig;
             zg[0] += z * p.gxy.x; zg[1] += z * p.gxy.y; zg[2] += z * p.gz_vx.x;
-            zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y;
+            if constexpr (!ZETA) { zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y; }
         }
     }
     if (!valid) return;
     double o[3];
-    estr_combine(Jt + idx * ldJt, zg, zv, transposed, o);
+    if constexpr (ZETA) { o[0] = zg[0]; o[1] = zg[1]; o[2] = zg[2]; }
+    else estr_combine(Jt + idx * ldJt, zg, zv, transposed, o);
     write_estr(t, idx, o, SFS, ldS, partial, nt_pad);
 }
 
-template <int K>
+template <int K, bool ZETA>
 __global__ void __launch_bounds__(UJ_THREADS)
 estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
                   const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrMixed* __restrict__ src,
@@ -198,7 +213,7 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
         const TgtPos p = tgt[t];
         tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
     }
-    const bool valid = t < nt && !(static_t && static_t[idx]);
+    const bool valid = t < nt && (ZETA || !(static_t && static_t[idx]));
     const double ox = __shfl_sync(0xffffffffu, tx, 0);
     const double oy = __shfl_sync(0xffffffffu, ty, 0);
     const double oz = __shfl_sync(0xffffffffu, tz, 0);
@@ -218,36 +233,58 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
                                        (float)(tile[j].z - oz), tile[j].isig2);
         }
         __syncwarp();
-        // sources follow the targets' Morton order: the self pair is source position t
-        const int64_t jself = self ? t - base : -1;
 #pragma unroll 1
         for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
-            float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
-#pragma unroll 4
-            for (int j = 0; j < UJ_BLOCK; j++) {
-                const float4 a = off[warp][sb + j];
-                const float dx = to.x - a.x, dy = to.y - a.y, dz = to.z - a.z;
-                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * a.w;
-                if constexpr (zeta_skip_s<K>() > 0.0f) {
-                    if (__all_sync(0xffffffffu, s > zeta_skip_s<K>())) continue;
+            // compensated FP32 sums over the block (see comp_add), FP64 across blocks
+            float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+            for (int sub = 0; sub < UJ_BLOCK; sub += ESTR_SUB) {
+                float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
+                bool any = false;   // warp-uniform: some source of the sub-block was not skipped
+#pragma unroll
+                for (int jj = 0; jj < ESTR_SUB; jj++) {
+                    const int j = sb + sub + jj;
+                    const float4 a = off[warp][j];
+                    const float dx = to.x - a.x, dy = to.y - a.y, dz = to.z - a.z;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float s = r2 * a.w;
+                    if constexpr (zeta_skip_s<K>() > 0.0f) {
+                        if (__all_sync(0xffffffffu, s > zeta_skip_s<K>())) continue;
+                    }
+                    any = true;
+                    float z = zhat_f32<K>(s);
+                    if constexpr (!ZETA) z = (r2 == 0.0f) ? 0.0f : z;
+                    const float4 g = tile[j].g;
+                    fg[0] = fmaf(z, g.x, fg[0]);
+                    fg[1] = fmaf(z, g.y, fg[1]);
+                    fg[2] = fmaf(z, g.z, fg[2]);
+                    if constexpr (!ZETA) {
+                        const float4 v = tile[j].v;
+                        fv[0] = fmaf(z, v.x, fv[0]);
+                        fv[1] = fmaf(z, v.y, fv[1]);
+                        fv[2] = fmaf(z, v.z, fv[2]);
+                    }
                 }
-                float z = zhat_f32<K>(s);
-                z = (sb + j == jself) ? 0.0f : z;
-                const float4 g = tile[sb + j].g, v = tile[sb + j].v;
-                fg[0] = fmaf(z, g.x, fg[0]);
-                fg[1] = fmaf(z, g.y, fg[1]);
-                fg[2] = fmaf(z, g.z, fg[2]);
-                fv[0] = fmaf(z, v.x, fv[0]);
-                fv[1] = fmaf(z, v.y, fv[1]);
-                fv[2] = fmaf(z, v.z, fv[2]);
+                if (any) {
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        comp_add(sg[k], cg[k], fg[k]);
+                        if constexpr (!ZETA) comp_add(sv[k], cv[k], fv[k]);
+                    }
+                }
             }
 #pragma unroll
-            for (int k = 0; k < 3; k++) { zg[k] += (double)fg[k]; zv[k] += (double)fv[k]; }
+            for (int k = 0; k < 3; k++) {
+                zg[k] += (double)sg[k] + (double)cg[k];
+                if constexpr (!ZETA) zv[k] += (double)sv[k] + (double)cv[k];
+            }
         }
+        __syncwarp();
     }
     if (!valid) return;
     double o[3];
-    estr_combine(Jt + idx * ldJt, zg, zv, transposed, o);
+    if constexpr (ZETA) { o[0] = zg[0]; o[1] = zg[1]; o[2] = zg[2]; }
+    else estr_combine(Jt + idx * ldJt, zg, zv, transposed, o);
     write_estr(t, idx, o, SFS, ldS, partial, nt_pad);
 }
 
@@ -267,25 +304,37 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
     const TgtPos* tgt = nullptr;
     cudaError_t e = order_targets(a.nt, a.xt, w.order, w.order_bytes, st, launches, &tgt);
     if (e != cudaSuccess) return e;
+    const uint8_t* static_s = a.zeta ? nullptr : a.static_s;
+    const uint8_t* static_t = a.zeta ? nullptr : a.static_t;
     if (a.precision == 0) {
         SrcEstrF64* src = (SrcEstrF64*)w.src_pack;
-        pack_estr_f64<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
-                                                a.transposed, src);
-        estr_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
-                                                        per_split, a.self, a.transposed, a.SFS, a.ldS,
-                                                        partial, nt_pad);
+        pack_estr_f64<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.zeta ? nullptr : a.Js, a.ldJs,
+                                                static_s, a.transposed, src);
+        if (a.zeta)
+            estr_f64_kernel<K, true><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
+                                                                  per_split, a.self, a.transposed, a.SFS, a.ldS,
+                                                                  partial, nt_pad);
+        else
+            estr_f64_kernel<K, false><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
+                                                                   per_split, a.self, a.transposed, a.SFS, a.ldS,
+                                                                   partial, nt_pad);
     } else {
         SrcEstrMixed* src = (SrcEstrMixed*)w.src_pack;
-        pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.Js, a.ldJs, a.static_s,
-                                                  a.transposed, a.self ? tgt : nullptr, src);
-        estr_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, a.static_t, ns_pad, src,
-                                                          per_split, a.self, a.transposed, a.SFS, a.ldS,
-                                                          partial, nt_pad);
+        pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.zeta ? nullptr : a.Js, a.ldJs,
+                                                  static_s, a.transposed, a.self ? tgt : nullptr, src);
+        if (a.zeta)
+            estr_mixed_kernel<K, true><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
+                                                                    per_split, a.self, a.transposed, a.SFS, a.ldS,
+                                                                    partial, nt_pad);
+        else
+            estr_mixed_kernel<K, false><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
+                                                                     per_split, a.self, a.transposed, a.SFS, a.ldS,
+                                                                     partial, nt_pad);
     }
     *launches += 2;
     if (partial) {
         estr_reduce<<<(unsigned)((a.nt + pb - 1) / pb), pb, 0, st>>>(a.nt, nsplit, partial, nt_pad, tgt,
-                                                                   a.static_t, a.SFS, a.ldS);
+                                                                   static_t, a.SFS, a.ldS);
         *launches += 1;
     }
     return cudaGetLastError();

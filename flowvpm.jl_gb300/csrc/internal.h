@@ -20,7 +20,7 @@ struct __align__(16) SrcMixed { float4 a, b, gam; };
 // Packed source of the FP64 UJ kernel, 64 B.
 struct __align__(16) SrcF64 { double2 xy, z_isig, gxy, gz_sig; };
 
-// Packed source of the mixed Estr kernel, 64 B: FP64 position, 1/sigma^2,
+// Packed source of the mixed Estr kernels, 64 B: FP64 position, 1/sigma^2,
 // g = ZNORM Gamma / sigma^3 and v = ZNORM (J^T Gamma) / sigma^3 (or J Gamma), in
 // FP32; g = v = 0 for static sources.
 struct __align__(16) SrcEstrMixed { double x, y, z; float isig2, pad; float4 g; float4 v; };
@@ -57,6 +57,7 @@ struct EstrArgs {
     double* SFS; int64_t ldS;
     int kernel, precision;
     bool transposed, self;
+    bool zeta = false;    // zeta_direct instead: SFS receives W = sum zeta Gamma (J unused, statics included)
 };
 
 // Reverse mode of the self-induced UJ of one particle set.

@@ -8,8 +8,10 @@
 // cut per leaf: one warp takes 32 consecutive Morton positions -- a few
 // neighbouring leaves -- and walks the union of their source lists as
 // particle intervals, each with the mask of the warp's leaves that need it.
-// Sources are staged 32 at a time in the warp's shared memory; a lane whose
-// leaf is not in an interval's mask computes with zero weight.  Pair math is
+// Sources are staged 32 at a time in the warp's shared memory, the tiles
+// running on across interval boundaries so that they are full, each source
+// carrying its interval's mask; a lane whose leaf is not in a source's mask
+// computes that pair with zero weight.  Pair math is
 // that of the all-pairs kernels (uj_pair.cuh for FP32-comp, the reference
 // formula for FP64); Estr uses the factored form of estr.cu with the self
 // pair excluded by position.
@@ -112,13 +114,13 @@ __global__ void leaf_pack_estr(int64_t n, const double* __restrict__ x, const do
     }
 }
 
-// Warp-group geometry shared by the mixed kernels: this lane's target (FP64
-// position, caller index), its leaf relative to the group's first leaf, and
-// the FP32 offsets from the group origin (the group's first target).
+// Warp-group geometry shared by the kernels: this lane's target (FP64
+// position, caller index) and its bit in the interval masks (its leaf relative
+// to the group's first leaf; 0 for the padding lanes of the last group).
 struct GroupTarget {
     double tx, ty, tz;
     int32_t idx;
-    int local;
+    unsigned bit;
     bool valid;
 };
 
@@ -130,9 +132,50 @@ __device__ __forceinline__ GroupTarget group_target(int64_t n, int64_t p0, int l
     g.valid = t < n;
     const TgtPos p = tgt[g.valid ? t : p0];
     g.tx = p.x; g.ty = p.y; g.tz = p.z; g.idx = p.idx;
-    g.local = leaf_of[g.valid ? t : p0] - leaf_of[p0];
+    g.bit = g.valid ? 1u << (leaf_of[t] - leaf_of[p0]) : 0u;
     return g;
 }
+
+// Walks a group's intervals 32 sources at a time, across interval boundaries,
+// so that tiles are full.  Lane i keeps interval wbase + i of a 32-interval
+// window in registers; the walk itself is warp-uniform.
+struct IntervalWalk {
+    const int4* ivs;
+    int e, e1, off, wbase;
+    int4 win;
+
+    __device__ __forceinline__ void init(const int4* v, int e0, int e_end, int lane)
+    {
+        ivs = v; e = e0; e1 = e_end; off = 0; wbase = e0;
+        win = (e0 + lane < e_end) ? ivs[e0 + lane] : make_int4(0, 0, 0, 0);
+    }
+    // Next tile: this lane's source position (-1 for none) and target mask; returns the tile's size.
+    __device__ __forceinline__ int next(int lane, int& my_p, unsigned& my_mask)
+    {
+        int filled = 0;
+        my_p = -1;
+        my_mask = 0u;
+        while (filled < 32 && e < e1) {
+            if (e - wbase >= 32) {
+                wbase = e;
+                win = (wbase + lane < e1) ? ivs[wbase + lane] : make_int4(0, 0, 0, 0);
+            }
+            const int k = e - wbase;
+            const int p0 = __shfl_sync(0xffffffffu, win.x, k);
+            const int p1 = __shfl_sync(0xffffffffu, win.y, k);
+            const unsigned m = (unsigned)__shfl_sync(0xffffffffu, win.z, k);
+            const int take = min(p1 - p0 - off, 32 - filled);
+            if (lane >= filled && lane < filled + take) {
+                my_p = p0 + off + (lane - filled);
+                my_mask = m;
+            }
+            filled += take;
+            off += take;
+            if (off == p1 - p0) { e++; off = 0; }
+        }
+        return filled;
+    }
+};
 
 // ------------------------------------------------------------- UJ, FP32-comp
 template <int K>
@@ -167,42 +210,43 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
 #pragma unroll
     for (int k = 0; k < 8; k++) { dJ[k] = 0.0; mj[k] = 0.f; jq[k] = 0.f; }
     int tiles = 0, blks = 0;
-    const int e1 = grp_row[grp + 1];
-    for (int e = grp_row[grp]; e < e1; e++) {
-        const int4 iv = ivs[e];
-        const float act = (me.valid && ((unsigned)iv.z >> me.local) & 1u) ? 1.0f : 0.0f;
-        for (int base = iv.x; base < iv.y; base += 32) {
-            const int cnt = min(32, iv.y - base);
-            SrcMixed sj;
-            if (lane < cnt) {
-                sj = src[base + lane];
-            } else {   // padding: far away, no strength
-                sj.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
-                sj.b = make_float4(0.f, 0.f, 0.f, 1.f);
-                sj.gam = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            const float thr = singular_tail<K>() ? fmaxf(sfar * sj.a.w, r2n) : sj.b.w * sj.b.w;
-            __syncwarp();
-            tile[warp][lane] = sj;
-            off[warp][lane] = make_float4((sj.a.x - oh.x) + (sj.b.x - ol.x), (sj.a.y - oh.y) + (sj.b.y - ol.y),
-                                          (sj.a.z - oh.z) + (sj.b.z - ol.z), thr);
-            __syncwarp();
-            const int ng = (cnt + 3) >> 2;
-            for (int q = 0; q < ng; q++)
-                pair4_mixed<K, true>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, act);
-            if (++tiles == NF_BLK_TILES) {
-                tiles = 0;
+    IntervalWalk walk;
+    walk.init(ivs, grp_row[grp], grp_row[grp + 1], lane);
+    for (;;) {
+        int sp;
+        unsigned smask;
+        const int cnt = walk.next(lane, sp, smask);
+        if (cnt == 0) break;
+        SrcMixed sj;
+        if (sp >= 0) {
+            sj = src[sp];
+        } else {   // padding: far away, no strength, no target
+            sj.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+            sj.b = make_float4(0.f, 0.f, 0.f, 1.f);
+            sj.gam = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        sj.gam.w = __uint_as_float(smask);
+        const float thr = singular_tail<K>() ? fmaxf(sfar * sj.a.w, r2n) : sj.b.w * sj.b.w;
+        __syncwarp();
+        tile[warp][lane] = sj;
+        off[warp][lane] = make_float4((sj.a.x - oh.x) + (sj.b.x - ol.x), (sj.a.y - oh.y) + (sj.b.y - ol.y),
+                                      (sj.a.z - oh.z) + (sj.b.z - ol.z), thr);
+        __syncwarp();
+        const int ng = (cnt + 3) >> 2;
+        for (int q = 0; q < ng; q++)
+            pair4_mixed<K, true>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, me.bit);
+        if (++tiles == NF_BLK_TILES) {
+            tiles = 0;
 #pragma unroll
-                for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }
+            for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }
 #pragma unroll
-                for (int k = 0; k < 8; k++) { mj[k] += jq[k]; jq[k] = 0.f; }
-                if (++blks == NF_MID_BLKS) {
-                    blks = 0;
+            for (int k = 0; k < 8; k++) { mj[k] += jq[k]; jq[k] = 0.f; }
+            if (++blks == NF_MID_BLKS) {
+                blks = 0;
 #pragma unroll
-                    for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
+                for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
 #pragma unroll
-                    for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
-                }
+                for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
             }
         }
     }
@@ -254,6 +298,7 @@ nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int3
           double* U, double* J)
 {
     __shared__ SrcF64 tile[NF_WARPS][32];
+    __shared__ unsigned tmask[NF_WARPS][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
     if (grp >= ngroups) return;
@@ -261,18 +306,19 @@ nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int3
     double acc[12];
 #pragma unroll
     for (int k = 0; k < 12; k++) acc[k] = 0.0;
-    const int e1 = grp_row[grp + 1];
-    for (int e = grp_row[grp]; e < e1; e++) {
-        const int4 iv = ivs[e];
-        const bool act = me.valid && (((unsigned)iv.z >> me.local) & 1u);
-        for (int base = iv.x; base < iv.y; base += 32) {
-            const int cnt = min(32, iv.y - base);
-            __syncwarp();
-            if (lane < cnt) tile[warp][lane] = src[base + lane];
-            __syncwarp();
-            if (act)
-                for (int j = 0; j < cnt; j++) leaf_pair_f64<K>(me.tx, me.ty, me.tz, tile[warp][j], acc);
-        }
+    IntervalWalk walk;
+    walk.init(ivs, grp_row[grp], grp_row[grp + 1], lane);
+    for (;;) {
+        int sp;
+        unsigned smask;
+        const int cnt = walk.next(lane, sp, smask);
+        if (cnt == 0) break;
+        __syncwarp();
+        if (sp >= 0) tile[warp][lane] = src[sp];
+        tmask[warp][lane] = smask;
+        __syncwarp();
+        for (int j = 0; j < cnt; j++)
+            if (tmask[warp][j] & me.bit) leaf_pair_f64<K>(me.tx, me.ty, me.tz, tile[warp][j], acc);
     }
     if (!me.valid) return;
 #pragma unroll
@@ -284,109 +330,125 @@ nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int3
 // ------------------------------------------------------------------------- Estr
 // SFS_t += J_t^T sum_s z_s g_s - sum_s z_s v_s  (z = zeta(r/sigma_s), g and v
 // pre-scaled by ZNORM / sigma_s^3 in the pack), over the group's intervals,
-// skipping the self pair, for non-static targets.
+// skipping the self pair (mixed: every pair at r = 0, as in estr.cu), for
+// non-static targets.
 template <int K, bool MIXED>
 __global__ void __launch_bounds__(NF_THREADS)
 nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
         const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const void* __restrict__ srcv,
         const double* __restrict__ Jt, const uint8_t* __restrict__ static_t, bool transposed, double* SFS)
 {
-    constexpr size_t SZ = MIXED ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64);
-    __shared__ __align__(16) unsigned char tile_raw[NF_WARPS][32 * SZ];
-    __shared__ float4 s_hi[NF_WARPS][32], s_lo[NF_WARPS][32];   // mixed: double-float source positions
+    // mixed: per source (x_hi, 1/sigma^2), (x_lo), g, v;  FP64: the packed source
+    __shared__ __align__(16) float4 mtile[MIXED ? NF_WARPS : 1][4][32];
+    __shared__ SrcEstrF64 dtile[MIXED ? 1 : NF_WARPS][32];
+    __shared__ int spos[NF_WARPS][32];                          // source position, -1 for padding
+    __shared__ unsigned tmask[NF_WARPS][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
     if (grp >= ngroups) return;
     const int64_t p0 = 32 * grp;
     const GroupTarget me = group_target(n, p0, lane, tgt, leaf_of);
     const bool live = me.valid && !(static_t && static_t[me.idx]);
-    const int64_t t = p0 + lane;
+    const unsigned bit = live ? me.bit : 0u;
+    const int tpos = (int)(p0 + lane);
     const float3 th = make_float3((float)me.tx, (float)me.ty, (float)me.tz);
     const float3 tl = make_float3((float)(me.tx - (double)th.x), (float)(me.ty - (double)th.y),
                                   (float)(me.tz - (double)th.z));
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
-    float mg[3] = {0.f, 0.f, 0.f}, mv[3] = {0.f, 0.f, 0.f};
+    // mixed: compensated FP32 sums of 8-source partial sums (comp_add), FP64 every NF_BLK_TILES tiles
+    float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
     int tiles = 0;
-    const int e1 = grp_row[grp + 1];
-    for (int e = grp_row[grp]; e < e1; e++) {
-        const int4 iv = ivs[e];
-        const bool act = live && (((unsigned)iv.z >> me.local) & 1u);
-        for (int base = iv.x; base < iv.y; base += 32) {
-            const int cnt = min(32, iv.y - base);
-            __syncwarp();
-            if (lane < cnt) {
-                if (MIXED) {
-                    const SrcEstrMixed p = ((const SrcEstrMixed*)srcv)[base + lane];
-                    ((SrcEstrMixed*)tile_raw[warp])[lane] = p;
-                    const float xh = (float)p.x, yh = (float)p.y, zh = (float)p.z;
-                    s_hi[warp][lane] = make_float4(xh, yh, zh, p.isig2);
-                    s_lo[warp][lane] = make_float4((float)(p.x - (double)xh), (float)(p.y - (double)yh),
+    IntervalWalk walk;
+    walk.init(ivs, grp_row[grp], grp_row[grp + 1], lane);
+    for (;;) {
+        int sp;
+        unsigned smask;
+        const int cnt = walk.next(lane, sp, smask);
+        if (cnt == 0) break;
+        __syncwarp();
+        if (sp >= 0) {
+            if constexpr (MIXED) {
+                const SrcEstrMixed p = ((const SrcEstrMixed*)srcv)[sp];
+                const float xh = (float)p.x, yh = (float)p.y, zh = (float)p.z;
+                mtile[warp][0][lane] = make_float4(xh, yh, zh, p.isig2);
+                mtile[warp][1][lane] = make_float4((float)(p.x - (double)xh), (float)(p.y - (double)yh),
                                                    (float)(p.z - (double)zh), 0.f);
-                } else {
-                    ((SrcEstrF64*)tile_raw[warp])[lane] = ((const SrcEstrF64*)srcv)[base + lane];
-                }
+                mtile[warp][2][lane] = p.g;
+                mtile[warp][3][lane] = p.v;
+            } else {
+                dtile[warp][lane] = ((const SrcEstrF64*)srcv)[sp];
             }
-            __syncwarp();
-            if (!act) continue;
-            const int jself = (int)(t - base);   // the self pair's slot in this tile, if any
-            if (MIXED) {
+        }
+        spos[warp][lane] = sp;
+        tmask[warp][lane] = smask;
+        __syncwarp();
+        if constexpr (MIXED) {
+            for (int j0 = 0; j0 < cnt; j0 += 8) {
                 float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
-                for (int j = 0; j < cnt; j++) {
-                    const SrcEstrMixed& p = ((const SrcEstrMixed*)tile_raw[warp])[j];
-                    const float4 h = s_hi[warp][j], l = s_lo[warp][j];
+                const int j1 = min(j0 + 8, cnt);
+                for (int j = j0; j < j1; j++) {
+                    const float4 h = mtile[warp][0][j], l = mtile[warp][1][j];
                     const float dx = (th.x - h.x) + (tl.x - l.x);
                     const float dy = (th.y - h.y) + (tl.y - l.y);
                     const float dz = (th.z - h.z) + (tl.z - l.z);
-                    float z = zhat_f32<K>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * h.w);
-                    z = (j == jself) ? 0.0f : z;
-                    fg[0] = fmaf(z, p.g.x, fg[0]); fg[1] = fmaf(z, p.g.y, fg[1]); fg[2] = fmaf(z, p.g.z, fg[2]);
-                    fv[0] = fmaf(z, p.v.x, fv[0]); fv[1] = fmaf(z, p.v.y, fv[1]); fv[2] = fmaf(z, p.v.z, fv[2]);
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    float z = zhat_f32<K>(r2 * h.w);
+                    const bool on = (tmask[warp][j] & bit) != 0u && r2 != 0.0f;   // pairs at r = 0 are skipped
+                    z = on ? z : 0.0f;
+                    const float4 g = mtile[warp][2][j], v = mtile[warp][3][j];
+                    fg[0] = fmaf(z, g.x, fg[0]); fg[1] = fmaf(z, g.y, fg[1]); fg[2] = fmaf(z, g.z, fg[2]);
+                    fv[0] = fmaf(z, v.x, fv[0]); fv[1] = fmaf(z, v.y, fv[1]); fv[2] = fmaf(z, v.z, fv[2]);
                 }
 #pragma unroll
-                for (int k = 0; k < 3; k++) { mg[k] += fg[k]; mv[k] += fv[k]; }
-                if (++tiles == NF_BLK_TILES * NF_MID_BLKS) {
-                    tiles = 0;
+                for (int k = 0; k < 3; k++) { comp_add(sg[k], cg[k], fg[k]); comp_add(sv[k], cv[k], fv[k]); }
+            }
+            if (++tiles == NF_BLK_TILES) {
+                tiles = 0;
 #pragma unroll
-                    for (int k = 0; k < 3; k++) { zg[k] += (double)mg[k]; zv[k] += (double)mv[k]; mg[k] = 0.f; mv[k] = 0.f; }
+                for (int k = 0; k < 3; k++) {
+                    zg[k] += (double)sg[k] + (double)cg[k];
+                    zv[k] += (double)sv[k] + (double)cv[k];
+                    sg[k] = cg[k] = sv[k] = cv[k] = 0.f;
                 }
-            } else {
-                for (int j = 0; j < cnt; j++) {
-                    if (j == jself) continue;
-                    const SrcEstrF64& p = ((const SrcEstrF64*)tile_raw[warp])[j];
-                    const double dx = p.xy.x - me.tx, dy = p.xy.y - me.ty, dz = p.z_isig.x - me.tz;
-                    const double isig = p.z_isig.y;
-                    const double z = zeta_f64<K>(sqrt(dx * dx + dy * dy + dz * dz) * isig) * isig * isig * isig;
-                    zg[0] += z * p.gxy.x; zg[1] += z * p.gxy.y; zg[2] += z * p.gz_vx.x;
-                    zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y;
-                }
+            }
+        } else {
+            for (int j = 0; j < cnt; j++) {
+                if (!(tmask[warp][j] & bit) || spos[warp][j] == tpos) continue;
+                const SrcEstrF64& p = dtile[warp][j];
+                const double dx = p.xy.x - me.tx, dy = p.xy.y - me.ty, dz = p.z_isig.x - me.tz;
+                const double isig = p.z_isig.y;
+                const double z = zeta_f64<K>(sqrt(dx * dx + dy * dy + dz * dz) * isig) * isig * isig * isig;
+                zg[0] += z * p.gxy.x; zg[1] += z * p.gxy.y; zg[2] += z * p.gz_vx.x;
+                zv[0] += z * p.gz_vx.y; zv[1] += z * p.vyz.x; zv[2] += z * p.vyz.y;
             }
         }
     }
-    if (MIXED) {
+    if constexpr (MIXED) {
 #pragma unroll
-        for (int k = 0; k < 3; k++) { zg[k] += (double)mg[k]; zv[k] += (double)mv[k]; }
+        for (int k = 0; k < 3; k++) { zg[k] += (double)sg[k] + (double)cg[k]; zv[k] += (double)sv[k] + (double)cv[k]; }
     }
     if (!live) return;
     const double* Jp = Jt + 9 * (int64_t)me.idx;
-    double s[3];
+    double o[3];
     if (transposed) {
-        s[0] = Jp[0] * zg[0] + Jp[1] * zg[1] + Jp[2] * zg[2];
-        s[1] = Jp[3] * zg[0] + Jp[4] * zg[1] + Jp[5] * zg[2];
-        s[2] = Jp[6] * zg[0] + Jp[7] * zg[1] + Jp[8] * zg[2];
+        o[0] = Jp[0] * zg[0] + Jp[1] * zg[1] + Jp[2] * zg[2] - zv[0];
+        o[1] = Jp[3] * zg[0] + Jp[4] * zg[1] + Jp[5] * zg[2] - zv[1];
+        o[2] = Jp[6] * zg[0] + Jp[7] * zg[1] + Jp[8] * zg[2] - zv[2];
     } else {
-        s[0] = Jp[0] * zg[0] + Jp[3] * zg[1] + Jp[6] * zg[2];
-        s[1] = Jp[1] * zg[0] + Jp[4] * zg[1] + Jp[7] * zg[2];
-        s[2] = Jp[2] * zg[0] + Jp[5] * zg[1] + Jp[8] * zg[2];
+        o[0] = Jp[0] * zg[0] + Jp[3] * zg[1] + Jp[6] * zg[2] - zv[0];
+        o[1] = Jp[1] * zg[0] + Jp[4] * zg[1] + Jp[7] * zg[2] - zv[1];
+        o[2] = Jp[2] * zg[0] + Jp[5] * zg[1] + Jp[8] * zg[2] - zv[2];
     }
 #pragma unroll
-    for (int k = 0; k < 3; k++) SFS[3 * (int64_t)me.idx + k] += s[k] - zv[k];
+    for (int k = 0; k < 3; k++) SFS[3 * (int64_t)me.idx + k] += o[k];
 }
 
 // ---------------------------------------------------------------------- launcher
 size_t leaf_work_bytes(int64_t n)
 {
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-    return al(n * sizeof(TgtPos)) + al(n * sizeof(SrcEstrF64));
+    const size_t src = sizeof(SrcEstrMixed) > sizeof(SrcEstrF64) ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64);
+    return al(n * sizeof(TgtPos)) + al(n * src);
 }
 
 template <int K>

@@ -118,20 +118,31 @@ __global__ void nt_bbox_partial(int64_t n, const double* __restrict__ x, double*
         for (int k = 0; k < 6; k++) part[6 * blockIdx.x + k] = s[k][0];
 }
 
-// box = (lo_x, lo_y, lo_z, ext): the cube of side ext = the largest extent
+// box = (lo_x, lo_y, lo_z, ext): the cube of side ext = the largest extent (one block of GS_THREADS)
 __global__ void nt_bbox_final(int nb, const double* __restrict__ part, double* __restrict__ box)
 {
-    if (threadIdx.x != 0) return;
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int b = 0; b < nb; b++)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
         for (int k = 0; k < 3; k++) {
             lo[k] = fmin(lo[k], part[6 * b + k]);
             hi[k] = fmax(hi[k], part[6 * b + 3 + k]);
         }
+    __shared__ double s[6][GS_THREADS];
+    for (int k = 0; k < 3; k++) { s[k][threadIdx.x] = lo[k]; s[3 + k][threadIdx.x] = hi[k]; }
+    __syncthreads();
+    for (int m = GS_THREADS / 2; m > 0; m >>= 1) {
+        if ((int)threadIdx.x < m)
+            for (int k = 0; k < 3; k++) {
+                s[k][threadIdx.x] = fmin(s[k][threadIdx.x], s[k][threadIdx.x + m]);
+                s[3 + k][threadIdx.x] = fmax(s[3 + k][threadIdx.x], s[3 + k][threadIdx.x + m]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
     double ext = 0.0;
-    for (int k = 0; k < 3; k++) ext = fmax(ext, __dsub_rn(hi[k], lo[k]));
+    for (int k = 0; k < 3; k++) ext = fmax(ext, __dsub_rn(s[3 + k][0], s[k][0]));
     if (!(ext > 0.0)) ext = 1.0;
-    box[0] = lo[0]; box[1] = lo[1]; box[2] = lo[2]; box[3] = ext;
+    box[0] = s[0][0]; box[1] = s[1][0]; box[2] = s[2][0]; box[3] = ext;
 }
 
 __global__ void nt_keys(int64_t n, const double* __restrict__ x, const double* __restrict__ box,
@@ -538,7 +549,7 @@ cudaError_t near_build(NearScratch& s, int64_t n, const double* x, int leaf_size
     // 1. keys and the Morton order
     const unsigned gb = gs_blocks(n);
     nt_bbox_partial<<<gb, GS_THREADS, 0, st>>>(n, x, s.part.as<double>());
-    nt_bbox_final<<<1, 32, 0, st>>>((int)gb, s.part.as<double>(), box);
+    nt_bbox_final<<<1, GS_THREADS, 0, st>>>((int)gb, s.part.as<double>(), box);
     nt_keys<<<gb, GS_THREADS, 0, st>>>(n, x, box, s.keys.as<uint64_t>(), s.idx.as<int32_t>());
     size_t tb = 0;
     NT_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, s.keys.as<uint64_t>(), s.keys2.as<uint64_t>(),

@@ -236,6 +236,10 @@ constexpr int MID_BLOCKS = 4;               // FP32 blocks per FP32 mid-level su
 #ifndef VPM_UJ_MIN_BLOCKS
 #define VPM_UJ_MIN_BLOCKS 5                 // resident blocks per SM the register budget targets
 #endif
+#ifndef VPM_UJ_UNROLL
+#define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
+#endif
+constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
 
 // Each warp streams the sources on its own: 32 per tile, double-buffered with
 // cp.async, so warps never wait for each other (no block-wide barrier).
@@ -317,7 +321,7 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
                                                 (a.z - oh.z) + (b.z - ol.z), thr);
         }
         __syncwarp();
-#pragma unroll 2
+#pragma unroll (UJ_UNROLL)
         for (int j = 0; j < WT; j += 4)
             pair4_mixed<K>(to, th, tl, r2n, offs[warp][buf], stage[warp][buf], j, u, jq, w);
         if (++in_block == BLOCK_TILES) {

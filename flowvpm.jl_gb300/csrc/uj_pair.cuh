@@ -41,12 +41,14 @@ __device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float G
 //   to      : target offset from the warp origin (FP32)
 //   th, tl  : target double-float position
 //   r2n     : (2 b)^2, b = the warp's extent around its origin
-//   act     : with MASK, 1 when this lane's target takes these sources, else 0
-//             (every lane still votes and computes: the sum is multiplied by act)
+//   mybit   : with MASK, this lane's bit in each source's target mask (the bits
+//             of gam.w): a source whose mask lacks it contributes nothing (every
+//             lane still votes and computes)
 template <int K, bool MASK = false>
 __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, const float3& tl, float r2n,
                                             const float4* __restrict__ off, const SrcMixed* __restrict__ tile,
-                                            int j0, float (&u)[3], float (&jq)[8], float (&w)[3], float act = 1.0f)
+                                            int j0, float (&u)[3], float (&jq)[8], float (&w)[3],
+                                            unsigned mybit = 0u)
 {
     float dx[4], dy[4], dz[4], r2[4], hw[4];
     bool far = true;
@@ -72,8 +74,13 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             } else {
                 near_GQ<K>(r2[q] * hw[q], hw[q], G, Q);
             }
-            if constexpr (MASK) { G *= act; Q *= act; }
-            accum_pair(dx[q], dy[q], dz[q], G, Q, tile[j0 + q].gam, u, jq, w);
+            const float4 gq = tile[j0 + q].gam;
+            if constexpr (MASK) {
+                const bool on = (__float_as_uint(gq.w) & mybit) != 0u;
+                G = on ? G : 0.0f;
+                Q = on ? Q : 0.0f;
+            }
+            accum_pair(dx[q], dy[q], dz[q], G, Q, gq, u, jq, w);
         }
     } else {
 #pragma unroll
@@ -96,8 +103,13 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             const bool nz = e2 > 0.0f;
             G = nz ? G : 0.0f;
             Q = nz ? Q : 0.0f;
-            if constexpr (MASK) { G *= act; Q *= act; }
-            accum_pair(ex, ey, ez, G, Q, tile[j0 + q].gam, u, jq, w);
+            const float4 gq = tile[j0 + q].gam;
+            if constexpr (MASK) {
+                const bool on = (__float_as_uint(gq.w) & mybit) != 0u;
+                G = on ? G : 0.0f;
+                Q = on ? Q : 0.0f;
+            }
+            accum_pair(ex, ey, ez, G, Q, gq, u, jq, w);
         }
     }
 }

@@ -246,6 +246,16 @@ __device__ __forceinline__ void pair_GQ(float r2, float s, float isig2, float& G
     }
 }
 
+// s += y, with the rounding error of the addition accumulated in c (Fast2Sum;
+// exact when |s| >= |y|, which a running sum of like terms keeps after its
+// first additions).  s + c is the compensated sum.
+__device__ __forceinline__ void comp_add(float& s, float& c, float y)
+{
+    const float t = s + y;
+    c += (s - t) + y;
+    s = t;
+}
+
 // zeta(rho)/ZNORM as a function of s = rho^2 (FP32).
 template <int K>
 __device__ __forceinline__ float zhat_f32(float s)

@@ -14,8 +14,9 @@ from .particlefield import (ParticleField, ClassicVPM, ReformulatedVPM, Kernel, 
 from .timeintegration import (AfterUJ, BeforeUJ, ConstantSFS, CoreSpreading, DynamicSFS, Inviscid,
                               NoSFS, Relaxation, SFS_Cd_twolevel_nobackscatter, SFS_Cs_nobackscatter,
                               clipping_backscatter, correctedpedrizzetti, isSFSenabled, noSFS,
-                              norelaxation, pedrizzetti, rungekutta3, run_vpm, update_particle_states)
-from .uj import UJ_gb300, UJ_gb300_cross, UJ_gb300_mixed
+                              norelaxation, pedrizzetti, rbf_conjugategradient, rungekutta3, run_vpm,
+                              update_particle_states)
+from .uj import UJ_gb300, UJ_gb300_cross, UJ_gb300_mixed, zeta_gb300, zeta_gb300_mixed
 from . import rings
 
 __all__ = [n for n in dir() if not n.startswith("_")]

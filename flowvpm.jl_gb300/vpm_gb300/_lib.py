@@ -49,6 +49,8 @@ SIGNATURES = {
     "vpm_estr_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int]),
     "vpm_uj_dev_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp]),
     "vpm_uj_adjoint_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int]),
+    "vpm_zeta": (_int, [_vp, _vp, _i64, _i64, _int, _int]),
+    "vpm_zeta_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _int, _int]),
     "vpm_p2p_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int,
                                     _vp]),
     "vpm_p2p_lists_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
@@ -170,6 +172,22 @@ class Context:
             raise ValueError(f"np={np_} exceeds maxparticles={particles.shape[1]}")
         self._check(self._L.vpm_uj(self._h, _ptr(particles), NFIELDS, int(np_), int(kernel),
                                    int(precision), int(flags)))
+
+    def zeta(self, particles: np.ndarray, np_: int, kernel: int, precision: int):
+        """vpm_zeta (zeta_direct) on a Fortran-ordered (46, maxparticles) matrix: rows 16:18."""
+        if not (isinstance(particles, np.ndarray) and particles.dtype == np.float64
+                and particles.flags.f_contiguous and particles.shape[0] == NFIELDS):
+            raise TypeError("particles must be a Fortran-ordered float64 array of shape (46, maxparticles)")
+        if np_ > particles.shape[1]:
+            raise ValueError(f"np={np_} exceeds maxparticles={particles.shape[1]}")
+        self._check(self._L.vpm_zeta(self._h, _ptr(particles), NFIELDS, int(np_), int(kernel), int(precision)))
+
+    def zeta_dev(self, xt, xs, gs, sgs, W, kernel: int, precision: int):
+        """W[nt,3] += sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s (device tensors)."""
+        _check_dev(xt, 3); _check_dev(xs, 3); _check_dev(gs, 3); _check_dev(sgs, 1); _check_dev(W, 3)
+        self._torch_stream()
+        self._check(self._L.vpm_zeta_dev(self._h, xt.shape[0], _ptr(xt), xs.shape[0], _ptr(xs), _ptr(gs),
+                                         _ptr(sgs), _ptr(W), int(kernel), int(precision)))
 
     def uj_cross(self, src: np.ndarray, ns: int, tgt: np.ndarray, nt: int, kernel: int, precision: int):
         for m in (src, tgt):

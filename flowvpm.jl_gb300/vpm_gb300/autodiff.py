@@ -11,9 +11,13 @@ would wrap the same two calls in an rrule.
 with Pedrizzetti relaxation (src/FLOWVPM_relaxation.jl:62-81), written with
 torch tensor operations on device-resident state so autograd can run through
 it; every particle-to-particle evaluation goes through `UJFunction`.
-`rollout` chains steps with per-step checkpointing: only each step's input
-state is kept, and the step's forward (including its UJ evaluations) is
-recomputed during the backward pass.
+`rollout` chains steps with per-step checkpointing.  The default keeps, per
+step, its input state and the U, J of its UJ evaluations (O(N) each); the
+backward pass re-runs the step's O(N) tensor algebra with autograd on those
+kept values, so the O(N^2) pair sums are not evaluated again: their reverse
+mode is the adjoint kernel, which recomputes the pair terms tile by tile.
+checkpoint="recompute" keeps only each step's input state and re-runs the
+whole step, UJ evaluations included (torch.utils.checkpoint).
 """
 from __future__ import annotations
 
@@ -65,16 +69,39 @@ def _stretch(J, G, transposed: bool = True):
     return torch.einsum("nji,nj->ni", Jm, G)       # S_i = sum_j du_i/dx_j G_j
 
 
+class _KeptUJ(torch.autograd.Function):
+    """UJ whose forward values were kept from an earlier evaluation on the same
+    inputs; its backward is the adjoint kernel, as for UJFunction."""
+
+    @staticmethod
+    def forward(ctx, x, gam, sig, U, J, kernel: int, vctx: _lib.Context):
+        ctx.save_for_backward(x, gam, sig)
+        ctx.kernel = kernel
+        ctx.vctx = vctx
+        return U.clone(), J.clone()
+
+    @staticmethod
+    def backward(ctx, Ubar, Jbar):
+        xb, gb, sb, *_ = UJFunction.backward(ctx, Ubar, Jbar)
+        return xb, gb, sb, None, None, None, None
+
+
+def _uj_default(x, gam, sig, kernel, precision, vctx):
+    return UJFunction.apply(x, gam, sig, kernel, precision, vctx)
+
+
 def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64, f: float = 0.0,
              g: float = 0.2, relax: bool = True, rlxf: float = 0.3, transposed: bool = True,
-             vctx: _lib.Context | None = None):
-    """One rVPM RK3 step (+ Pedrizzetti relaxation) on device tensors; differentiable."""
+             vctx: _lib.Context | None = None, uj_fn=None):
+    """One rVPM RK3 step (+ Pedrizzetti relaxation) on device tensors; differentiable.
+    uj_fn(x, gam, sig, kernel, precision, vctx) -> (U, J) replaces UJFunction (checkpointing)."""
     vctx = vctx or _lib.default_context()
+    uj_fn = uj_fn or _uj_default
     M0 = torch.zeros_like(x)
     M3 = torch.zeros_like(gam)
     M8 = torch.zeros_like(sig)
     for a, b in STAGES:
-        U, J = UJFunction.apply(x, gam, sig, kernel, precision, vctx)
+        U, J = uj_fn(x, gam, sig, kernel, precision, vctx)
         M0 = a * M0 + dt * U
         x = x + b * M0
         MM = _stretch(J, gam, transposed)
@@ -87,7 +114,7 @@ def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64,
         gam = gam + b * M3
         sig = sig + b * M8
     if relax:
-        U, J = UJFunction.apply(x, gam, sig, kernel, precision, vctx)
+        U, J = uj_fn(x, gam, sig, kernel, precision, vctx)
         w = torch.stack([J[:, 5] - J[:, 7], J[:, 6] - J[:, 2], J[:, 1] - J[:, 3]], dim=1)
         nw = torch.sqrt((w * w).sum(1))
         nG = torch.sqrt((gam * gam).sum(1))
@@ -97,12 +124,50 @@ def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64,
     return x, gam, sig
 
 
-def rollout(x, gam, sig, dt: float, nsteps: int, *, checkpoint: bool = True, **kw):
-    """nsteps of rk3_step; with checkpoint=True each step's internals are recomputed in backward."""
+class _StepKeepUJ(torch.autograd.Function):
+    """One rk3_step with per-step checkpointing that keeps the step's U, J values."""
+
+    @staticmethod
+    def forward(ctx, x, gam, sig, dt, kw):
+        kept = []
+
+        def record(x_, g_, s_, kernel, precision, vctx):
+            U, J = UJFunction.apply(x_, g_, s_, kernel, precision, vctx)
+            kept.append((U, J))
+            return U, J
+        with torch.no_grad():
+            out = rk3_step(x, gam, sig, dt, uj_fn=record, **kw)
+        ctx.save_for_backward(x, gam, sig)
+        ctx.kept, ctx.dt, ctx.kw = kept, dt, kw
+        return out
+
+    @staticmethod
+    def backward(ctx, gx, gg, gs):
+        x, gam, sig = (t.detach().requires_grad_() for t in ctx.saved_tensors)
+        kept = iter(ctx.kept)
+
+        def replay(x_, g_, s_, kernel, precision, vctx):
+            U, J = next(kept)
+            return _KeptUJ.apply(x_, g_, s_, U, J, kernel, vctx)
+        with torch.enable_grad():
+            out = rk3_step(x, gam, sig, ctx.dt, uj_fn=replay, **ctx.kw)
+        grads = [gx, gg, gs]
+        outs = [o for o, gr in zip(out, grads) if gr is not None]
+        torch.autograd.backward(outs, [gr for gr in grads if gr is not None])
+        return x.grad, gam.grad, sig.grad, None, None
+
+
+def rollout(x, gam, sig, dt: float, nsteps: int, *, checkpoint=True, **kw):
+    """nsteps of rk3_step.  checkpoint=True: per-step checkpointing that keeps
+    each step's UJ values (no pair sum is evaluated twice); "recompute": per-step
+    checkpointing that re-runs each step in the backward pass; False: autograd
+    keeps every intermediate."""
     for _ in range(nsteps):
-        if checkpoint:
+        if checkpoint == "recompute":
             x, gam, sig = ckpt.checkpoint(lambda a, b, c: rk3_step(a, b, c, dt, **kw), x, gam, sig,
                                           use_reentrant=False)
+        elif checkpoint:
+            x, gam, sig = _StepKeepUJ.apply(x, gam, sig, dt, kw)
         else:
             x, gam, sig = rk3_step(x, gam, sig, dt, **kw)
     return x, gam, sig

@@ -8,7 +8,9 @@ tensors in the reference's operation order:
   * the pseudo-three-level dynamic SFS procedure with Lagrangian averaging,
     bounds and the NaN check, src/FLOWVPM_subfilterscale.jl:447-673, and
     backscatter clipping, :287-296;
-  * core spreading (RK3 branch), src/FLOWVPM_viscous.jl:175-220;
+  * core spreading (RK3 branch), src/FLOWVPM_viscous.jl:175-220, with the
+    core-size reset: zeta_direct (src/FLOWVPM_viscous.jl:467-488, through
+    vpm_zeta_dev) and the RBF conjugate gradient (:314-454);
   * Pedrizzetti relaxation, src/FLOWVPM_relaxation.jl:62-81.
 Static particles are not supported in this form (the host mirror has them).
 """
@@ -44,6 +46,7 @@ class DeviceField:
     SFS: torch.Tensor = None   # [n,3]
     C: torch.Tensor = None     # [n,3]  C_INDEX rows (coefficient, Lagrangian numerator, denominator)
     M: torch.Tensor = None     # [n,9]  M_INDEX rows
+    vol: torch.Tensor = None   # [n]    particle volumes (the RBF initial guess of a core-size reset)
     # near-field evaluation instead of all pairs (FMM near field: leaf size, theta)
     leaflist: tuple | None = None
 
@@ -93,10 +96,55 @@ class DynamicSFSParams:
 
 @dataclass
 class CoreSpreadingParams:
+    """CoreSpreading(nu, sgm0; beta, itmax, tol, iterror), src/FLOWVPM_viscous.jl:62-112."""
     nu: float
     sgm0: float
     beta: float = 1.5
     t_sgm: float = 0.0
+    itmax: int = 15
+    tol: float = 1e-3
+    iterror: bool = True
+
+
+def zeta(fld: DeviceField, ctx: _lib.Context) -> torch.Tensor:
+    """zeta_direct: W[n,3] = sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s (self pair included)."""
+    W = torch.zeros_like(fld.gam)
+    ctx.zeta_dev(fld.x, fld.x, fld.gam, fld.sig, W, fld.kernel, fld.precision)
+    return W
+
+
+def rbf_conjugategradient(fld: DeviceField, ctx: _lib.Context, target: torch.Tensor, p: CoreSpreadingParams):
+    """src/FLOWVPM_viscous.jl:314-454 per component on device tensors: new
+    strengths whose basis field reproduces `target` (to the relative residual tol)."""
+    if fld.vol is None:
+        raise ValueError("a core-size reset needs the particle volumes (DeviceField.vol)")
+    tiny = 2 * EPS
+    x = target * fld.vol[:, None]                 # x0 = omega_targ * vol
+    fld.gam.copy_(x)
+    r = target - zeta(fld, ctx)                   # r0 = b - A x0
+    fld.gam.copy_(r)                              # p0 = r0
+    rr0s = (r * r).sum(0).tolist()
+    rrs = list(rr0s)
+    flags = [math.sqrt(a) > p.tol or (a != 0 and math.sqrt(b / a) > p.tol) for a, b in zip(rr0s, rrs)]
+    for it in range(1, int(p.itmax) + 1):
+        if not any(flags):
+            break
+        Ap = zeta(fld, ctx)
+        pAps = (fld.gam * Ap).sum(0).tolist()
+        alphas = torch.tensor([rrs[i] / pAps[i] * flags[i] if flags[i] else 0.0 for i in range(3)],
+                              dtype=torch.float64, device=x.device)
+        prev_rrs = rrs
+        x += alphas * fld.gam
+        r -= alphas * Ap
+        rrs = (r * r).sum(0).tolist()
+        betas = [1.0 if abs(prev_rrs[i]) <= tiny else rrs[i] / prev_rrs[i] for i in range(3)]
+        fld.gam.copy_(r + torch.tensor(betas, dtype=torch.float64, device=x.device) * fld.gam)
+        flags = [flags[i] and (False if abs(rr0s[i]) <= tiny else math.sqrt(rrs[i] / rr0s[i]) > p.tol)
+                 for i in range(3)]
+        if it == p.itmax and any(flags) and p.iterror:
+            raise RuntimeError(f"Maximum number of iterations {p.itmax} reached before convergence. "
+                               f"Errors: {[math.sqrt(a / b) for a, b in zip(rrs, rr0s)]}, tolerance:{p.tol}")
+    fld.gam.copy_(x)
 
 
 def _zeta0(kernel: int) -> float:
@@ -185,8 +233,11 @@ def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSP
             if abs(b - 8 / 15) <= 1e-7:
                 viscous.t_sgm += dt
                 beta = math.sqrt(2 * viscous.nu * viscous.t_sgm / viscous.sgm0 ** 2 + 1)
-                if beta >= viscous.beta:
-                    raise NotImplementedError("core-spreading reset (zeta/RBF) is not part of this library")
+                if beta >= viscous.beta:   # core-size reset (src/FLOWVPM_viscous.jl:199-219)
+                    target = zeta(fld, ctx)
+                    fld.sig.fill_(viscous.sgm0)
+                    rbf_conjugategradient(fld, ctx, target, viscous)
+                    viscous.t_sgm = 0.0
     if relax_rlxf is not None:
         uj(fld, ctx)
         J = fld.J

@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .particlefield import (C_INDEX, GAMMA_INDEX, J_INDEX, M_INDEX, SFS_INDEX, SIGMA_INDEX,
-                            STATIC_INDEX, U_INDEX, X_INDEX, ParticleField, ReformulatedVPM,
+                            STATIC_INDEX, U_INDEX, VOL_INDEX, X_INDEX, ParticleField, ReformulatedVPM,
                             _reset_particles)
 
 EPS = 2.220446049250313e-16  # Julia eps()
@@ -47,13 +47,65 @@ class Inviscid:
 
 @dataclass
 class CoreSpreading:
-    """Core spreading, src/FLOWVPM_viscous.jl:62-223.  The RK3 spreading of the
-    core sizes is mirrored; the core-size reset (zeta evaluation + RBF
-    conjugate-gradient) is not part of this library and raises if reached."""
+    """Core spreading, src/FLOWVPM_viscous.jl:62-223: RK3 spreading of the core
+    sizes and, once sigma/sgm0 reaches beta, the core-size reset -- the basis
+    field of the current strengths (`zeta`, default zeta_gb300 = zeta_direct on
+    the GB300) becomes the target vorticity, sigma returns to sgm0 and new
+    strengths come from the RBF conjugate gradient (rbf_conjugategradient)."""
     nu: float
     sgm0: float
     beta: float = 1.5
     t_sgm: float = 0.0
+    zeta: object = None
+    itmax: int = 15
+    tol: float = 1e-3
+    iterror: bool = True
+
+
+def rbf_conjugategradient(pfield: ParticleField, cs: CoreSpreading):
+    """src/FLOWVPM_viscous.jl:314-454, per component, over the non-static
+    particles: the solution is built in M[1:3], the residual in M[4:6], the
+    target vorticity is M[7:9]; Gamma holds the search direction while the
+    basis field of it (zeta) lands in J[1:3]."""
+    zeta = cs.zeta if cs.zeta is not None else _default_zeta()
+    P = pfield.particles
+    idx = _live(pfield)
+    tiny = 2 * EPS
+    P[27:30, idx] = P[33:36, idx] * P[VOL_INDEX, idx]          # x0 = omega_targ * vol
+    P[GAMMA_INDEX, idx] = P[27:30, idx]
+    zeta(pfield)
+    P[30:33, idx] = P[33:36, idx] - P[15:18, idx]               # r0 = b - A x0
+    P[GAMMA_INDEX, idx] = P[30:33, idx]                         # p0 = r0
+    rr0s = (P[30:33, idx] ** 2).sum(1)
+    rrs = rr0s.copy()
+    with np.errstate(divide="ignore", invalid="ignore"):
+        flags = (np.sqrt(rr0s) > cs.tol) | (np.sqrt(rrs / rr0s) > cs.tol)
+    for it in range(1, int(cs.itmax) + 1):
+        if not flags.any():
+            break
+        zeta(pfield)
+        pAps = (P[GAMMA_INDEX, idx] * P[15:18, idx]).sum(1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            alphas = rrs / pAps * flags
+        prev_rrs = rrs
+        P[27:30, idx] += alphas[:, None] * P[GAMMA_INDEX, idx]
+        P[30:33, idx] -= alphas[:, None] * P[15:18, idx]
+        rrs = (P[30:33, idx] ** 2).sum(1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            betas = rrs / prev_rrs
+        betas = np.where(np.abs(prev_rrs) <= tiny, 1.0, betas)
+        P[GAMMA_INDEX, idx] = P[30:33, idx] + betas[:, None] * P[GAMMA_INDEX, idx]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            flags = flags & np.where(np.abs(rr0s) <= tiny, False, np.sqrt(rrs / rr0s) > cs.tol)
+        if it == cs.itmax and flags.any() and cs.iterror:
+            raise RuntimeError(f"Maximum number of iterations {cs.itmax} reached before convergence. "
+                               f"Errors: {np.sqrt(rrs / rr0s)}, tolerance:{cs.tol}")
+    P[GAMMA_INDEX, idx] = P[27:30, idx]
+
+
+def _default_zeta():
+    from .uj import zeta_gb300
+    return zeta_gb300
 
 
 def viscousdiffusion(pfield: ParticleField, dt: float, aux1: float = 0.0, aux2: float = 0.0):
@@ -74,9 +126,12 @@ def viscousdiffusion(pfield: ParticleField, dt: float, aux1: float = 0.0, aux2: 
         scheme.t_sgm += dt
         beta_cur = math.sqrt(2 * scheme.nu * scheme.t_sgm / scheme.sgm0 ** 2 + 1)
         if beta_cur >= scheme.beta:
-            raise NotImplementedError(
-                f"core-spreading reset reached (sigma growth {beta_cur:.4f} >= {scheme.beta}); "
-                "the zeta/RBF reset is not part of this library")
+            zeta = scheme.zeta if scheme.zeta is not None else _default_zeta()
+            zeta(pfield)                                        # basis field of the current strengths
+            P[33:36, idx] = P[15:18, idx]                       # target vorticity in M[7:9]
+            P[SIGMA_INDEX, idx] = scheme.sgm0                   # reset core sizes
+            rbf_conjugategradient(pfield, scheme)
+            scheme.t_sgm = 0.0
 
 
 # ----------------------------------------------------------------- relaxation

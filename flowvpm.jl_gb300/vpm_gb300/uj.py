@@ -58,3 +58,16 @@ def UJ_gb300_cross(source: ParticleField, target: ParticleField, *, precision: i
     """UJ_direct(source, target), src/FLOWVPM_UJ.jl:48-50: accumulate, no reset."""
     c = ctx if ctx is not None else _lib.default_context()
     c.uj_cross(source.particles, source.np, target.particles, target.np, _kernel_id(source), precision)
+
+
+def zeta_gb300(pfield: ParticleField, *, ctx: _lib.Context | None = None) -> None:
+    """zeta_direct(pfield) (src/FLOWVPM_viscous.jl:467-488) on the GB300 in FP64:
+    rows 16:18 (J[1:3]) of every particle receive the RBF basis field."""
+    c = ctx if ctx is not None else _lib.default_context()
+    c.zeta(pfield.particles, pfield.np, _kernel_id(pfield), _lib.FP64)
+
+
+def zeta_gb300_mixed(pfield: ParticleField, *, ctx: _lib.Context | None = None) -> None:
+    """zeta_direct on the GB300 with FP32 pair math and FP64 block reduction."""
+    c = ctx if ctx is not None else _lib.default_context()
+    c.zeta(pfield.particles, pfield.np, _kernel_id(pfield), _lib.FP32COMP)

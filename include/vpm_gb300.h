@@ -165,6 +165,16 @@ int vpm_uj_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* g
                        const double* Ubar, const double* Jbar, double* xbar, double* gbar,
                        double* sbar, int kernel, int precision);
 
+/* zeta_direct(pfield) (src/FLOWVPM_viscous.jl:467-488), the RBF basis field of
+ * core spreading: rows 16:18 (J[1:3]) of every particle, statics included, are
+ * set to sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s over every source, the self
+ * pair included.  Host 46-row matrix as vpm_uj; only rows 16:18 are written. */
+int vpm_zeta(vpm_ctx* ctx, double* particles, int64_t ld_rows, int64_t np, int kernel, int precision);
+
+/* The same sum on device arrays: W[nt,3] += sum_s zeta(|xt - xs|/sigma_s)/sigma_s^3 Gamma_s. */
+int vpm_zeta_dev(vpm_ctx* ctx, int64_t nt, const double* xt, int64_t ns, const double* xs, const double* gs,
+                 const double* sgs, double* W, int kernel, int precision);
+
 /* Near-field leg of UJ_fmm (src/FLOWVPM_UJ.jl:90-125): builds an octree of the
  * n particles on the GPU (leaves of at most leaf_size particles,
  * 1 <= leaf_size <= 4096) and adds U[n,3], J[n,9] -- and, with VPM_SFS, Estr

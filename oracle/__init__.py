@@ -80,6 +80,7 @@ def lib():
                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_estr_pairs.argtypes = [_i64, _i64, _dp, _dp, _u8p, _i64, _dp, _dp, _dp,
                                         _dp, _u8p, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_zeta_pairs.argtypes = [_i64, _i64, _dp, _i64, _dp, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int]
         L.oracle_update_particle_states.argtypes = [_dp, _i64, _i64, ctypes.c_double,
                                                     ctypes.c_double, ctypes.c_double, _dp,
                                                     ctypes.c_double, ctypes.c_double,
@@ -139,6 +140,17 @@ def uj_pairs(xt, xs, gs, sgs, kernel: int, targets=None, erf_mode: int = 0,
     lib().oracle_uj_pairs(t0, t1, _p(xt), xs.shape[0], _p(xs), _p(gs), _p(sgs), _p(U), _p(J),
                           int(kernel), int(erf_mode), int(bool(compensated)), int(nthreads))
     return U[t0:t1], J[t0:t1]
+
+
+def zeta_pairs(xt, xs, gs, sgs, kernel: int, targets=None, nthreads: int = 0):
+    """Return W[nt,3] = zeta_direct of the sources on the targets (self pairs included)."""
+    xt, xs, gs, sgs = _c(xt), _c(xs), _c(gs), _c(sgs)
+    nt = xt.shape[0]
+    t0, t1 = targets if targets is not None else (0, nt)
+    W = np.zeros((nt, 3))
+    lib().oracle_zeta_pairs(t0, t1, _p(xt), xs.shape[0], _p(xs), _p(gs), _p(sgs), _p(W), int(kernel),
+                            int(nthreads))
+    return W[t0:t1]
 
 
 def estr_pairs(xt, Jt, xs, gs, sgs, Js, kernel: int, transposed: bool = True,

@@ -362,6 +362,31 @@ void oracle_estr_pairs(int64_t t0, int64_t t1, const double* xt, const double* J
     }
 }
 
+/* zeta_direct(sources, targets, zeta), src/FLOWVPM_viscous.jl:467-488: the
+ * basis-function (vorticity) field W_t += sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s
+ * over every source, the self pair (r = 0) included; statics take part. */
+void oracle_zeta_pairs(int64_t t0, int64_t t1, const double* xt, int64_t ns, const double* xs,
+                       const double* gs, const double* sgs, double* W, int kernel, int nthreads)
+{
+    int nth = set_threads(nthreads);
+    (void)nth;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth)
+    for (int64_t t = t0; t < t1; t++) {
+        double w0 = W[3 * t], w1 = W[3 * t + 1], w2 = W[3 * t + 2];
+        for (int64_t s = 0; s < ns; s++) {
+            const double dX1 = xt[3 * t] - xs[3 * s];
+            const double dX2 = xt[3 * t + 1] - xs[3 * s + 1];
+            const double dX3 = xt[3 * t + 2] - xs[3 * s + 2];
+            const double r = sqrt(dX1 * dX1 + dX2 * dX2 + dX3 * dX3);
+            const double zeta_sgm = 1.0 / (sgs[s] * sgs[s] * sgs[s]) * oracle_zeta(kernel, r / sgs[s]);
+            w0 += gs[3 * s] * zeta_sgm;
+            w1 += gs[3 * s + 1] * zeta_sgm;
+            w2 += gs[3 * s + 2] * zeta_sgm;
+        }
+        W[3 * t] = w0; W[3 * t + 1] = w1; W[3 * t + 2] = w2;
+    }
+}
+
 /* ------------------------------------------------------- UJ_direct (46 rows) */
 static int is_static(const double* p) { return p[RSTATIC] != 0; }
 

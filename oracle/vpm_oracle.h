@@ -58,6 +58,11 @@ void oracle_estr_pairs(int64_t t0, int64_t t1, const double* xt, const double* J
                        const double* Js, const uint8_t* static_s,
                        double* SFS, int kernel, int transposed, int nthreads);
 
+/* zeta_direct: W_t += sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s, self pair included
+ * (src/FLOWVPM_viscous.jl:467-488). */
+void oracle_zeta_pairs(int64_t t0, int64_t t1, const double* xt, int64_t ns, const double* xs,
+                       const double* gs, const double* sgs, double* W, int kernel, int nthreads);
+
 /* Reverse mode of oracle_uj_pairs over one particle set (targets = sources,
  * pairs with r^2 == 0 skipped): given Ubar[n*3] = dL/dU and Jbar[n*9] = dL/dJ,
  * adds dL/dx to xbar[n*3], dL/dGamma to gbar[n*3] and dL/dsigma to sbar[n].

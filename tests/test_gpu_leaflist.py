@@ -125,7 +125,7 @@ def test_leaflist_estr_with_statics(ctx, prec):
     Jg = J.cpu().numpy()
     # the oracle's Estr uses the GPU's J (as UJ_fmm's Estr uses the J just computed)
     _, _, Sr = _oracle_over_lists(X, G, s, Jg, static, lists, 2, True)
-    assert normwise(S.cpu().numpy(), Sr)[0] <= (1e-12 if prec == 0 else 1e-5)
+    assert normwise(S.cpu().numpy(), Sr)[0] <= (1e-12 if prec == 0 else 2e-6)
     assert not S.cpu().numpy()[static].any()
 
 

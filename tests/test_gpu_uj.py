@@ -2,7 +2,10 @@
 
 Tolerances (normwise: max|err| / max|ref| per quantity, over all targets):
   FP64 kernels      <= 1e-12 for U, J and SFS
-  FP32-comp kernels <= 1e-6 for U and J, <= 1e-5 for SFS
+  FP32-comp kernels <= 1e-6 for U and J; <= 2e-6 for SFS computed from the
+  FP32-comp J (the J error propagates: SFS sums differences of J), <= 3e-6 for
+  SFS from an exact J on a smooth field (limited by the FP32 sums of the
+  factored form, which cancel)
 """
 import os
 
@@ -17,7 +20,7 @@ pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FP64, FP32COMP = 0, 1
 TOL_UJ = {FP64: 1e-12, FP32COMP: 1e-6}
-TOL_SFS = {FP64: 1e-12, FP32COMP: 1e-5}
+TOL_SFS = {FP64: 1e-12, FP32COMP: 2e-6}
 ALL_FLAGS = oracle.RESET | oracle.RESET_SFS | oracle.SFS | oracle.TRANSPOSED
 
 
@@ -120,6 +123,34 @@ def test_estr_dev_parity(ctx, prec, transposed):
     assert normwise(SFS.cpu().numpy(), ref)[0] <= TOL_SFS[prec]
 
 
+@pytest.mark.parametrize("transposed", [True, False])
+def test_mixed_estr_on_a_smooth_field(ctx, transposed):
+    """On two coaxial rings J varies slowly from particle to particle, so each
+    Estr term z (J_t - J_s)^T g is a difference of nearly equal J, and the sum
+    over a target's neighbours cancels further.  With an exact J the FP32-comp
+    Estr keeps 3e-6 there; the difference of SFS between the dynamic
+    procedure's two filter widths (sigma and 0.999 sigma, each with its own J)
+    -- a difference of nearly equal SFS -- keeps 5e-3."""
+    import torch
+    from vpm_gb300 import workloads
+    X, G, s = workloads.leapfrog_rings(4000, nper=10)
+    n = X.shape[0]
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    out = {}
+    for alpha in (1.0, 0.999):
+        sa = s * alpha
+        _, J = oracle.uj_pairs(X, X, G, sa, 2)
+        ref = oracle.estr_pairs(X, J, X, G, sa, J, 2, transposed)
+        SFS = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+        ctx.estr_dev(d(X), d(J), d(X), d(G), d(sa), d(J), SFS, 2, FP32COMP, transposed)
+        got = SFS.cpu().numpy()
+        assert normwise(got, ref)[0] <= 3e-6, alpha
+        out[alpha] = (got, ref)
+    diff_got = out[0.999][0] - out[1.0][0]
+    diff_ref = out[0.999][1] - out[1.0][1]
+    assert normwise(diff_got, diff_ref)[0] <= 5e-3
+
+
 @pytest.mark.parametrize("prec", [FP64, FP32COMP])
 def test_uj_cross_matrix(ctx, prec):
     Xs, Gs, ss = random_cloud(500, seed=31, box=0.2)
@@ -201,3 +232,35 @@ def test_nonfinite_outputs_are_reported(ctx):
     with pytest.raises(vpm_gb300.VPMError) as ei:
         ctx.uj(P, 50, 2, FP64, oracle.RESET | vpm_gb300._lib.CHECK_FINITE)
     assert ei.value.code == vpm_gb300._lib.ERR_NONFINITE
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32COMP])
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+def test_zeta_dev_parity(ctx, k, prec):
+    """zeta_direct (src/FLOWVPM_viscous.jl:467-488), self pairs included."""
+    import torch
+    X, G, s = random_cloud(1500, seed=40 + k, box=0.3)
+    X[7] = X[3]                              # a coincident pair
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    W = torch.zeros(X.shape[0], 3, device="cuda", dtype=torch.float64)
+    x = d(X)
+    ctx.zeta_dev(x, x, d(G), d(s), W, k, prec)
+    ref = oracle.zeta_pairs(X, X, G, s, k)
+    assert normwise(W.cpu().numpy(), ref)[0] <= TOL_UJ[prec]
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32COMP])
+def test_zeta_matrix_writes_rows_16_18_of_every_particle(ctx, prec):
+    n = 700
+    X, G, s = random_cloud(n, seed=44, box=0.3)
+    static = np.zeros(n, bool)
+    static[::11] = True
+    P = matrix_of(X, G, s, static=static, extra=5)
+    P[15:18, :] = 7.0                        # overwritten, statics included
+    Q = P.copy(order="F")
+    ctx.zeta(P, n, 2, prec)
+    ref = oracle.zeta_pairs(X, X, G, s, 2)
+    assert normwise(P[15:18, :n].T, ref)[0] <= TOL_UJ[prec]
+    other = [r for r in range(46) if r not in (15, 16, 17)]
+    assert np.array_equal(P[other, :], Q[other, :])
+    assert np.array_equal(P[:, n:], Q[:, n:])

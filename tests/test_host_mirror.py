@@ -86,9 +86,44 @@ def test_dynamic_sfs_sets_coefficients_and_clips():
     assert np.all(C * (G * S).sum(axis=0) >= 0)   # backscatter clipped
 
 
-def test_corespreading_reset_is_reported():
-    pf = _ring_field(kernel=vpm.gaussianerf, viscous=vpm.CoreSpreading(nu=1.0, sgm0=0.05))
-    with pytest.raises(NotImplementedError, match="reset"):
+def zeta_oracle(pfield):
+    """zeta_direct through the oracle: rows 16:18 of every particle (statics included)."""
+    n = pfield.np
+    P = pfield.particles
+    X = np.ascontiguousarray(P[0:3, :n].T)
+    P[15:18, :n] = oracle.zeta_pairs(X, X, np.ascontiguousarray(P[3:6, :n].T), P[6, :n], pfield.kernel.kid).T
+
+
+def test_corespreading_reset_rebuilds_strengths():
+    """The core-size reset of src/FLOWVPM_viscous.jl:194-219: sigma returns to
+    sgm0 on the non-static particles, the growth timer restarts, and the RBF
+    conjugate gradient leaves strengths whose basis field matches the target
+    vorticity to the CG tolerance; the static particle is left alone."""
+    pf = _ring_field(kernel=vpm.gaussianerf, static=True, relaxation=vpm.norelaxation,
+                     viscous=vpm.CoreSpreading(1e-3, 0.05, beta=1.0001, zeta=zeta_oracle))
+    n = pf.np
+    st_before = pf.particles[:, n - 1].copy()
+    pf.nextstep(0.01)
+    P = pf.particles
+    assert pf.viscous.t_sgm == 0.0
+    assert np.all(P[6, :n - 1] == 0.05)
+    assert np.array_equal(P[0:7, n - 1], st_before[0:7])
+    # the reference's stopping rule: |b - A x| <= tol |b - A x0| per component, x0 = b vol
+    targ = P[33:36, :n - 1].T.copy()
+    zeta_oracle(pf)
+    W = P[15:18, :n - 1].T.copy()
+    P[3:6, :n - 1] = (targ * P[7, :n - 1][:, None]).T
+    zeta_oracle(pf)
+    r0 = targ - P[15:18, :n - 1].T
+    live = (targ ** 2).sum(0) > 1e-12 * (targ ** 2).sum()      # the ring's axial component is zero
+    res = np.sqrt(((W - targ) ** 2).sum(0)[live] / (r0 ** 2).sum(0)[live])
+    assert live.any() and (res <= 1e-3).all(), res
+
+
+def test_corespreading_reset_reports_non_convergence():
+    pf = _ring_field(kernel=vpm.gaussianerf, relaxation=vpm.norelaxation,
+                     viscous=vpm.CoreSpreading(1e-3, 0.05, beta=1.0001, zeta=zeta_oracle, itmax=1, tol=1e-14))
+    with pytest.raises(RuntimeError, match="Maximum number of iterations"):
         pf.nextstep(0.01)
 
 
