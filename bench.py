@@ -274,8 +274,8 @@ def run_gpu(args, rank, world):
                        "precision": "fp32comp", "pairs_per_step": pairs_per_step,
                        "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single"},
-            "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": 46 * 8 * n,
-                    "d2h_bytes_per_step": 18 * 8 * n, "ms_per_step": 1e3 * statistics.mean(e2e_times),
+            "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": 8 * 8 * n,
+                    "d2h_bytes_per_step": 12 * 8 * n, "ms_per_step": 1e3 * statistics.mean(e2e_times),
                     "call": "vpm_uj(ctx, host 46xN matrix, RESET) = UJ_gb300_mixed(pfield)"},
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops,
                          "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops, "traffic": None,

@@ -7,6 +7,8 @@
 #include "tree.h"
 
 #include <algorithm>
+#include <atomic>
+#include <cmath>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -22,6 +24,29 @@ namespace {
 
 // 0-based rows of the particle column, src/FLOWVPM_particlefield.jl:239-252
 enum : int { R_X = 0, R_G = 3, R_SIG = 6, R_U = 9, R_W = 12, R_J = 15, R_PSE = 24, R_SFS = 39, R_STATIC = 42 };
+
+// Page-locked host staging memory that grows on demand.
+struct PinBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t grow(size_t bytes)
+    {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = bytes + bytes / 8;
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
 
 thread_local std::string g_create_error;
 
@@ -42,6 +67,9 @@ struct vpm_ctx {
     int64_t launches = 0;
     // device copies of host matrices and SoA views of them
     DevBuf mat, mat2, x, g, s, st, xt;
+    // compact staging of the drop-in call: per particle X, Gamma, sigma, static in; U, J, SFS out
+    PinBuf hin, hout;
+    DevBuf din, dout;
     // packing and split-K scratch
     DevBuf src_pack, order, partial, flag;
     // near-field: packed particles, and the lists (built on the device or uploaded)
@@ -168,6 +196,18 @@ __global__ void unpack_matrix(int64_t np, double* __restrict__ mat, int flags, d
     }
 }
 
+// the compact input rows (X, Gamma, sigma, static: 8 doubles a particle) to SoA
+__global__ void unpack_compact(int64_t np, const double* __restrict__ in, double* __restrict__ x,
+                               double* __restrict__ g, double* __restrict__ s, uint8_t* __restrict__ st)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const double* p = in + 8 * i;
+    for (int k = 0; k < 3; k++) { x[3 * i + k] = p[k]; g[3 * i + k] = p[3 + k]; }
+    s[i] = p[6];
+    st[i] = p[7] != 0.0 ? 1 : 0;
+}
+
 __global__ void positions_of_matrix(int64_t np, const double* __restrict__ mat, double* __restrict__ x)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -175,7 +215,20 @@ __global__ void positions_of_matrix(int64_t np, const double* __restrict__ mat, 
     for (int k = 0; k < 3; k++) x[3 * i + k] = mat[(int64_t)VPM_NFIELDS * i + R_X + k];
 }
 
-// Sets *flag if any of rows [r0, r1) of the first np columns is not finite.
+// out[i] = a * in[i] (core sizes of the test filter)
+__global__ void scale_copy(int64_t n, const double* __restrict__ in, double a, double* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a * in[i];
+}
+
+// out[i] = a[i] - b[i]
+__global__ void sub_arrays(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
+}
+
 // rows [r0, r1) of every column set to zero
 __global__ void zero_rows(int64_t np, double* __restrict__ mat, int r0, int r1)
 {
@@ -184,6 +237,7 @@ __global__ void zero_rows(int64_t np, double* __restrict__ mat, int r0, int r1)
     for (int r = r0; r < r1; r++) mat[i * VPM_NFIELDS + r] = 0.0;
 }
 
+// Sets *flag if any of rows [r0, r1) of the first np columns is not finite.
 __global__ void check_rows_finite(int64_t np, const double* __restrict__ mat, int r0, int r1, int* flag)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -268,6 +322,23 @@ int enter(vpm_ctx* c)
 }  // namespace
 
 // =================================================================== ABI
+// Host rows <-> compact staging, split over host threads.
+template <class F>
+static void host_parallel(int64_t n, F f)
+{
+    const unsigned hw = std::thread::hardware_concurrency();
+    int nth = (int)std::min<int64_t>(hw ? hw : 1, 16);
+    if (n < (1 << 15)) nth = 1;
+    if (nth <= 1) { f(0, n); return; }
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nth - 1) / nth;
+    for (int t = 0; t < nth; t++) {
+        const int64_t a = t * chunk, b = std::min(n, a + chunk);
+        if (a < b) th.emplace_back(f, a, b);
+    }
+    for (auto& x : th) x.join();
+}
+
 extern "C" {
 
 int vpm_abi_version(void) { return VPM_ABI_VERSION; }
@@ -320,6 +391,9 @@ int vpm_ctx_destroy(vpm_ctx* c)
                           &c->partial, &c->flag, &c->leaf})
             b->release();
         c->near.release_all();
+        for (DevBuf* b : {&c->din, &c->dout}) b->release();
+        c->hin.release();
+        c->hout.release();
         if (c->done) cudaEventDestroy(c->done);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
         cudaGetLastError();
@@ -379,19 +453,11 @@ int vpm_probe_ffma(vpm_ctx* c, double* tflops)
 }
 
 // ------------------------------------------------------------- UJ_direct drop-in
-int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, int precision, int flags)
+// The drop-in call through the whole particle matrix: the matrix goes to the
+// device, the kernels update its rows in place, the touched rows come back.
+// Used when the old J of every particle feeds Estr (SFS without RESET).
+static int uj_full_matrix(vpm_ctx* c, double* particles, int64_t np, int kernel, int precision, int flags)
 {
-    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj: ctx is NULL");
-    std::lock_guard<std::mutex> lk(c->mu);
-    RC(enter(c));
-    if (!particles && np > 0) return fail(c, VPM_ERR_ARG, "vpm_uj: particles is NULL");
-    if (ld != VPM_NFIELDS) return fail(c, VPM_ERR_ARG, "vpm_uj: ld must be %d (got %lld)", VPM_NFIELDS, (long long)ld);
-    if (np < 0 || np > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj: np=%lld out of range", (long long)np);
-    if (flags & ~(VPM_RESET | VPM_RESET_SFS | VPM_SFS | VPM_TRANSPOSED | VPM_CHECK_FINITE))
-        return fail(c, VPM_ERR_ARG, "vpm_uj: unknown flag bits 0x%x", flags);
-    RC(check_kernel(c, kernel, precision));
-    if (np == 0) return VPM_OK;
-    DeviceGuard dg(c->device);
     cudaStream_t st = c->stream;
     const size_t mat_bytes = (size_t)VPM_NFIELDS * np * sizeof(double);
     RC(grow(c, c->mat, mat_bytes, "particle matrix"));
@@ -451,6 +517,117 @@ int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, in
     CK(cudaStreamSynchronize(st), "D2H");
     if (hflag) return fail(c, VPM_ERR_NONFINITE, "vpm_uj: NaN or Inf in the computed U/J/SFS");
     return VPM_OK;
+}
+
+// The drop-in call with compact staging: only X, Gamma, sigma and the static
+// flag go to the device (64 B a particle instead of the 368 B column), the
+// kernels compute the U, J (and SFS) sums from zero, and the host applies them
+// to the matrix with UJ_direct's rules: with RESET the non-static particles'
+// rows 10:27 restart from zero, static ones accumulate; likewise RESET_SFS for
+// rows 40:42.  Valid whenever Estr does not need the old J (RESET or no SFS):
+// Estr reads J only of non-static particles, whose J is then the new sum.
+static int uj_staged(vpm_ctx* c, double* particles, int64_t np, int kernel, int precision, int flags)
+{
+    cudaStream_t st = c->stream;
+    const bool sfs = (flags & VPM_SFS) != 0;
+    const int nout = sfs ? 15 : 12;
+    RC(grow(c, c->x, 3 * np * sizeof(double), "positions"));
+    RC(grow(c, c->g, 3 * np * sizeof(double), "strengths"));
+    RC(grow(c, c->s, np * sizeof(double), "core sizes"));
+    RC(grow(c, c->st, np, "static flags"));
+    RC(grow(c, c->din, (size_t)8 * np * sizeof(double), "staged inputs"));
+    RC(grow(c, c->dout, (size_t)15 * np * sizeof(double), "staged outputs"));
+    if (c->hin.grow((size_t)8 * np * sizeof(double)) != cudaSuccess ||
+        c->hout.grow((size_t)15 * np * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, VPM_ERR_CAPACITY, "could not allocate %lld B of pinned host staging", (long long)(23 * 8 * np));
+    }
+    Workspace w;
+    RC(ensure_work(c, np, np, precision, sfs, &w));
+    double* hin = (double*)c->hin.p;
+    double* hout = (double*)c->hout.p;
+    host_parallel(np, [&](int64_t a, int64_t b) {
+        for (int64_t i = a; i < b; i++) {
+            const double* p = particles + (int64_t)VPM_NFIELDS * i;
+            double* q = hin + 8 * i;
+            for (int k = 0; k < 7; k++) q[k] = p[k];
+            q[7] = p[R_STATIC];
+        }
+    });
+    double* din = (double*)c->din.p;
+    double* dU = (double*)c->dout.p;
+    double* dJ = dU + 3 * np;
+    double* dS = dJ + 9 * np;
+    double* x = (double*)c->x.p;
+    double* g = (double*)c->g.p;
+    double* s = (double*)c->s.p;
+    uint8_t* stf = (uint8_t*)c->st.p;
+    CK(cudaMemcpyAsync(din, hin, (size_t)8 * np * sizeof(double), cudaMemcpyHostToDevice, st), "H2D staged inputs");
+    unpack_compact<<<nblk(np), EB, 0, st>>>(np, din, x, g, s, stf);
+    c->launches++;
+    CK(cudaMemsetAsync(dU, 0, (size_t)nout * np * sizeof(double), st), "memset staged outputs");
+    UJArgs a;
+    a.nt = np; a.ns = np; a.xt = x; a.xs = x; a.gs = g; a.sgs = s;
+    a.U = dU; a.ldU = 3; a.J = dJ; a.ldJ = 9;
+    a.kernel = kernel; a.precision = precision; a.self = true;
+    CK(launch_uj(a, w, c->num_sms, st, &c->launches), "UJ kernels");
+    if (sfs) {
+        EstrArgs e;
+        e.nt = np; e.ns = np;
+        e.xt = x; e.Jt = dJ; e.ldJt = 9; e.static_t = stf;
+        e.xs = x; e.gs = g; e.sgs = s; e.Js = dJ; e.ldJs = 9; e.static_s = stf;
+        e.SFS = dS; e.ldS = 3;
+        e.kernel = kernel; e.precision = precision;
+        e.transposed = (flags & VPM_TRANSPOSED) != 0; e.self = true;
+        CK(launch_estr(e, w, c->num_sms, st, &c->launches), "Estr kernels");
+    }
+    CK(cudaMemcpyAsync(hout, dU, (size_t)nout * np * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H staged outputs");
+    RC(bounded_wait(c));
+    const bool reset = (flags & VPM_RESET) != 0, reset_sfs = (flags & VPM_RESET_SFS) != 0;
+    const double* hU = hout;
+    const double* hJ = hU + 3 * np;
+    const double* hS = hJ + 9 * np;
+    std::atomic<int> bad{0};
+    host_parallel(np, [&](int64_t a0, int64_t b0) {
+        int nonfinite = 0;
+        for (int64_t i = a0; i < b0; i++) {
+            double* p = particles + (int64_t)VPM_NFIELDS * i;
+            const bool is_static = p[R_STATIC] != 0.0;
+            if (reset && !is_static)
+                for (int k = R_U; k < R_PSE + 3; k++) p[k] = 0.0;
+            for (int k = 0; k < 3; k++) p[R_U + k] += hU[3 * i + k];
+            for (int k = 0; k < 9; k++) p[R_J + k] += hJ[9 * i + k];
+            if (reset_sfs && !is_static)
+                for (int k = 0; k < 3; k++) p[R_SFS + k] = 0.0;
+            if (sfs)
+                for (int k = 0; k < 3; k++) p[R_SFS + k] += hS[3 * i + k];
+            if (flags & VPM_CHECK_FINITE) {
+                for (int k = R_U; k < R_PSE + 3; k++) nonfinite |= !std::isfinite(p[k]);
+                if (sfs)
+                    for (int k = 0; k < 3; k++) nonfinite |= !std::isfinite(p[R_SFS + k]);
+            }
+        }
+        if (nonfinite) bad = 1;
+    });
+    if (bad) return fail(c, VPM_ERR_NONFINITE, "vpm_uj: NaN or Inf in the computed U/J/SFS");
+    return VPM_OK;
+}
+
+int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, int precision, int flags)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj: ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (!particles && np > 0) return fail(c, VPM_ERR_ARG, "vpm_uj: particles is NULL");
+    if (ld != VPM_NFIELDS) return fail(c, VPM_ERR_ARG, "vpm_uj: ld must be %d (got %lld)", VPM_NFIELDS, (long long)ld);
+    if (np < 0 || np > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj: np=%lld out of range", (long long)np);
+    if (flags & ~(VPM_RESET | VPM_RESET_SFS | VPM_SFS | VPM_TRANSPOSED | VPM_CHECK_FINITE))
+        return fail(c, VPM_ERR_ARG, "vpm_uj: unknown flag bits 0x%x", flags);
+    RC(check_kernel(c, kernel, precision));
+    if (np == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if ((flags & VPM_SFS) && !(flags & VPM_RESET)) return uj_full_matrix(c, particles, np, kernel, precision, flags);
+    return uj_staged(c, particles, np, kernel, precision, flags);
 }
 
 int vpm_uj_cross(vpm_ctx* c, const double* src, int64_t ld_src, int64_t ns, double* tgt, int64_t ld_tgt,
@@ -617,6 +794,69 @@ int vpm_zeta(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, 
     const size_t pitch = VPM_NFIELDS * sizeof(double);
     CK(cudaMemcpy2DAsync(particles + R_J, pitch, mat + R_J, pitch, 3 * sizeof(double), (size_t)np,
                          cudaMemcpyDeviceToHost, st), "D2H rows 16:18");
+    return bounded_wait(c);
+}
+
+// ------------------------------------------------- dynamic SFS test-filter differences
+int vpm_dynamic_diff_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
+                         const double* J, double alpha, double* dJ, double* dSFS, int kernel, int precision,
+                         int flags)
+{
+    const char* fn = "vpm_dynamic_diff_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (!(alpha > 0.0 && alpha < 1.0)) return fail(c, VPM_ERR_ARG, "%s: alpha must be in (0, 1)", fn);
+    if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
+    RC(check_kernel(c, kernel, precision));
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(J) || !is_device_ptr(dJ) ||
+        !is_device_ptr(dSFS))
+        return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
+    cudaStream_t st = c->stream;
+    Workspace w;
+    RC(ensure_work(c, n, n, precision, true, &w));
+    RC(grow(c, c->s, n * sizeof(double), "test-filter core sizes"));
+    double* sig_a = (double*)c->s.p;
+    scale_copy<<<nblk(n), EB, 0, st>>>(n, sig, alpha, sig_a);
+    c->launches++;
+    const bool tr = (flags & VPM_TRANSPOSED) != 0;
+    EstrArgs e;
+    e.nt = n; e.ns = n; e.xt = x; e.ldJt = 9; e.static_t = nullptr;
+    e.xs = x; e.gs = gam; e.ldJs = 9; e.static_s = nullptr;
+    e.ldS = 3; e.kernel = kernel; e.precision = precision; e.transposed = tr; e.self = true;
+    if (precision == VPM_FP32COMP) {
+        CK(cudaMemsetAsync(dJ, 0, 9 * n * sizeof(double), st), "memset dJ");
+        CK(cudaMemsetAsync(dSFS, 0, 3 * n * sizeof(double), st), "memset dSFS");
+        CK(launch_uj_filter_diff(n, x, gam, sig, alpha, dJ, kernel, w, st, &c->launches), "filter-difference UJ");
+        // the weight difference at J, then an ordinary Estr of dJ at alpha sigma
+        e.Jt = J; e.Js = J; e.sgs = sig; e.SFS = dSFS; e.dz_alpha = alpha;
+        CK(launch_estr(e, w, c->num_sms, st, &c->launches), "weight-difference Estr");
+        e.Jt = dJ; e.Js = dJ; e.sgs = sig_a; e.dz_alpha = 0.0;
+        CK(launch_estr(e, w, c->num_sms, st, &c->launches), "test-filter Estr");
+    } else {
+        // FP64: the reference's two evaluations, then their differences
+        RC(grow(c, c->mat2, (size_t)18 * n * sizeof(double), "test-filter scratch"));
+        double* Ua = (double*)c->mat2.p;
+        double* Ja = Ua + 3 * n;
+        double* Sa = Ja + 9 * n;
+        double* S0 = Sa + 3 * n;
+        CK(cudaMemsetAsync(Ua, 0, (size_t)18 * n * sizeof(double), st), "memset scratch");
+        UJArgs a;
+        a.nt = n; a.ns = n; a.xt = x; a.xs = x; a.gs = gam; a.sgs = sig_a;
+        a.U = Ua; a.ldU = 3; a.J = Ja; a.ldJ = 9; a.kernel = kernel; a.precision = precision; a.self = true;
+        CK(launch_uj(a, w, c->num_sms, st, &c->launches), "test-filter UJ");
+        e.Jt = Ja; e.Js = Ja; e.sgs = sig_a; e.SFS = Sa;
+        CK(launch_estr(e, w, c->num_sms, st, &c->launches), "test-filter Estr");
+        e.Jt = J; e.Js = J; e.sgs = sig; e.SFS = S0;
+        CK(launch_estr(e, w, c->num_sms, st, &c->launches), "Estr");
+        sub_arrays<<<nblk(9 * n), EB, 0, st>>>(9 * n, Ja, J, dJ);
+        sub_arrays<<<nblk(3 * n), EB, 0, st>>>(3 * n, Sa, S0, dSFS);
+        c->launches += 2;
+        CK(cudaGetLastError(), "differences");
+    }
     return bounded_wait(c);
 }
 

@@ -29,6 +29,23 @@ static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * 
 // rounding is what limits the mixed Estr; sums of 8 added with compensation
 // bring it from ~1e-5 to ~2e-6 of max |SFS| on a smooth field.
 constexpr int ESTR_SUB = 8;
+
+// zeta~(r, alpha sigma) / zeta~(r, sigma) - 1 at s = (r/sigma)^2, zeta~(r, sigma) =
+// zeta(r/sigma)/sigma^3 (src/FLOWVPM_kernel.jl:45-84); fd = (alpha^-3 - 1, alpha^-3, alpha^-2 - 1)
+template <int K>
+__device__ __forceinline__ float zeta_ratio_m1(float s, float3 fd)
+{
+    if constexpr (K == K_GAUSERF) {          // zeta ~ e^{-rho^2/2}
+        return fmaf(fd.y, expm1f(-0.5f * s * fd.z), fd.x);
+    } else if constexpr (K == K_GAUS) {      // zeta ~ e^{-rho^3}
+        return fmaf(fd.y, expm1f(-s * sqrtf(s) * fd.x), fd.x);
+    } else if constexpr (K == K_WNKLMNS) {   // zeta ~ (rho^2 + 1)^-3.5
+        const float eps = s * fd.z / fmaf(s, 1.0f + fd.z, 1.0f);
+        return fmaf(fd.y, expm1f(3.5f * log1pf(-eps)), fd.x);
+    } else {
+        return 0.0f;
+    }
+}
 static_assert(UJ_BLOCK % ESTR_SUB == 0, "whole sub-blocks");
 
 size_t estr_src_pack_bytes(int64_t ns, int precision)
@@ -196,12 +213,16 @@ estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __rest
     write_estr(t, idx, o, SFS, ldS, partial, nt_pad);
 }
 
-template <int K, bool ZETA>
+// With DZ (the weight difference of the dynamic procedure's test filter,
+// dynamic.cu) each weight zeta~(r, sigma_s) is replaced by
+// zeta~(r, alpha sigma_s) - zeta~(r, sigma_s) = zeta~(r, sigma_s) (ratio - 1),
+// ratio - 1 from zeta_ratio_m1 with the factors fd = (alpha^-3 - 1, alpha^-3, alpha^-2 - 1).
+template <int K, bool ZETA, bool DZ = false>
 __global__ void __launch_bounds__(UJ_THREADS)
 estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
                   const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrMixed* __restrict__ src,
                   int64_t per_split, bool self, bool transposed, double* SFS, int64_t ldS, double* partial,
-                  int64_t nt_pad)
+                  int64_t nt_pad, float3 fd = make_float3(0.f, 0.f, 0.f))
 {
     __shared__ SrcEstrMixed tile[UJ_TILE];
     __shared__ float4 off[UJ_WARPS][UJ_TILE];
@@ -239,21 +260,26 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
             float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
 #pragma unroll 1
             for (int sub = 0; sub < UJ_BLOCK; sub += ESTR_SUB) {
+                // s of the sub-block's sources; the sub-block is skipped when every pair of the warp
+                // is past zeta_skip_s (zeta/zeta(0) < 1e-13 there)
+                float sv8[ESTR_SUB], r28[ESTR_SUB];
+                bool far = true;
+#pragma unroll
+                for (int jj = 0; jj < ESTR_SUB; jj++) {
+                    const float4 a = off[warp][sb + sub + jj];
+                    const float dx = to.x - a.x, dy = to.y - a.y, dz = to.z - a.z;
+                    r28[jj] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    sv8[jj] = r28[jj] * a.w;
+                    far = far && sv8[jj] > zeta_skip_s<K>();
+                }
+                if (zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, far)) continue;
                 float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
-                bool any = false;   // warp-uniform: some source of the sub-block was not skipped
 #pragma unroll
                 for (int jj = 0; jj < ESTR_SUB; jj++) {
                     const int j = sb + sub + jj;
-                    const float4 a = off[warp][j];
-                    const float dx = to.x - a.x, dy = to.y - a.y, dz = to.z - a.z;
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float s = r2 * a.w;
-                    if constexpr (zeta_skip_s<K>() > 0.0f) {
-                        if (__all_sync(0xffffffffu, s > zeta_skip_s<K>())) continue;
-                    }
-                    any = true;
-                    float z = zhat_f32<K>(s);
-                    if constexpr (!ZETA) z = (r2 == 0.0f) ? 0.0f : z;
+                    float z = zhat_f32<K>(sv8[jj]);
+                    if constexpr (DZ) z *= zeta_ratio_m1<K>(sv8[jj], fd);
+                    if constexpr (!ZETA) z = (r28[jj] == 0.0f) ? 0.0f : z;
                     const float4 g = tile[j].g;
                     fg[0] = fmaf(z, g.x, fg[0]);
                     fg[1] = fmaf(z, g.y, fg[1]);
@@ -265,12 +291,10 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
                         fv[2] = fmaf(z, v.z, fv[2]);
                     }
                 }
-                if (any) {
 #pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        comp_add(sg[k], cg[k], fg[k]);
-                        if constexpr (!ZETA) comp_add(sv[k], cv[k], fv[k]);
-                    }
+                for (int k = 0; k < 3; k++) {
+                    comp_add(sg[k], cg[k], fg[k]);
+                    if constexpr (!ZETA) comp_add(sv[k], cv[k], fv[k]);
                 }
             }
 #pragma unroll
@@ -306,6 +330,7 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
     if (e != cudaSuccess) return e;
     const uint8_t* static_s = a.zeta ? nullptr : a.static_s;
     const uint8_t* static_t = a.zeta ? nullptr : a.static_t;
+    if (a.dz_alpha > 0.0 && a.precision == 0) return cudaErrorInvalidValue;   // FP32-comp only
     if (a.precision == 0) {
         SrcEstrF64* src = (SrcEstrF64*)w.src_pack;
         pack_estr_f64<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.zeta ? nullptr : a.Js, a.ldJs,
@@ -326,7 +351,14 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
             estr_mixed_kernel<K, true><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
                                                                     per_split, a.self, a.transposed, a.SFS, a.ldS,
                                                                     partial, nt_pad);
-        else
+        else if (a.dz_alpha > 0.0) {
+            const double al = a.dz_alpha;
+            const float3 fd = make_float3((float)(1.0 / (al * al * al) - 1.0), (float)(1.0 / (al * al * al)),
+                                          (float)(1.0 / (al * al) - 1.0));
+            estr_mixed_kernel<K, false, true><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad,
+                                                                           src, per_split, a.self, a.transposed,
+                                                                           a.SFS, a.ldS, partial, nt_pad, fd);
+        } else
             estr_mixed_kernel<K, false><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
                                                                      per_split, a.self, a.transposed, a.SFS, a.ldS,
                                                                      partial, nt_pad);

@@ -58,6 +58,7 @@ struct EstrArgs {
     int kernel, precision;
     bool transposed, self;
     bool zeta = false;    // zeta_direct instead: SFS receives W = sum zeta Gamma (J unused, statics included)
+    double dz_alpha = 0.0;   // > 0: the weight difference zeta~(r, alpha sigma) - zeta~(r, sigma) (mixed only)
 };
 
 // Reverse mode of the self-induced UJ of one particle set.
@@ -106,6 +107,10 @@ cudaError_t launch_estr(const EstrArgs& a, const Workspace& w, int num_sms, cuda
                         int64_t* launches);
 cudaError_t launch_uj_adjoint(const AdjArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
                               int64_t* launches);
+// dJ[n,9] += J(alpha sigma) - J(sigma) of one particle set, all pairs, FP32-comp (dynamic.cu)
+size_t dyn_src_pack_bytes(int64_t ns);
+cudaError_t launch_uj_filter_diff(int64_t n, const double* x, const double* gam, const double* sig, double alpha,
+                                  double* dJ, int kernel, const Workspace& w, cudaStream_t st, int64_t* launches);
 
 // ------------------------------------------------------------------ near field
 // A device allocation that grows on demand and never shrinks.

@@ -50,6 +50,7 @@ SIGNATURES = {
     "vpm_uj_dev_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp]),
     "vpm_uj_adjoint_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int]),
     "vpm_zeta": (_int, [_vp, _vp, _i64, _i64, _int, _int]),
+    "vpm_dynamic_diff_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _int, _int]),
     "vpm_zeta_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _int, _int]),
     "vpm_p2p_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int,
                                     _vp]),
@@ -188,6 +189,16 @@ class Context:
         self._torch_stream()
         self._check(self._L.vpm_zeta_dev(self._h, xt.shape[0], _ptr(xt), xs.shape[0], _ptr(xs), _ptr(gs),
                                          _ptr(sgs), _ptr(W), int(kernel), int(precision)))
+
+    def dynamic_diff_dev(self, x, gam, sig, J, alpha: float, dJ, dSFS, kernel: int, precision: int,
+                         transposed: bool = True):
+        """dJ = J(alpha sigma) - J(sigma), dSFS = SFS(alpha sigma; J + dJ) - SFS(sigma; J) (set, not added)."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(J, 9); _check_dev(dJ, 9)
+        _check_dev(dSFS, 3)
+        self._torch_stream()
+        self._check(self._L.vpm_dynamic_diff_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(J),
+                                                 float(alpha), _ptr(dJ), _ptr(dSFS), int(kernel), int(precision),
+                                                 TRANSPOSED if transposed else 0))
 
     def uj_cross(self, src: np.ndarray, ns: int, tgt: np.ndarray, nt: int, kernel: int, precision: int):
         for m in (src, tgt):

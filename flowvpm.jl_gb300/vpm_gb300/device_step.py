@@ -85,13 +85,19 @@ def uj(fld: DeviceField, ctx: _lib.Context, *, sfs: bool = False, reset: bool = 
 
 @dataclass
 class DynamicSFSParams:
-    """DynamicSFS settings; defaults = SFS_Cd_twolevel_nobackscatter (src/FLOWVPM.jl:223)."""
+    """DynamicSFS settings; defaults = SFS_Cd_twolevel_nobackscatter (src/FLOWVPM.jl:223).
+
+    fused: with FP32-comp pair sums, take the test-filter differences from
+    vpm_dynamic_diff_dev (evaluated as differences, FP32 relative accuracy)
+    instead of subtracting two separate evaluations (the reference's way,
+    whose FP32 rounding the 1e-3 differences amplify to 1e-4 .. 1e-2)."""
     alpha: float = 0.999
     rlxf: float = 0.005
     minC: float = 0.0
     maxC: float = 1.0
     force_positive: bool = True
     clip_backscatter: bool = True
+    fused: bool = True
 
 
 @dataclass
@@ -161,11 +167,24 @@ def _dynamic_before(fld, ctx, p: DynamicSFSParams):
     fld.sig /= p.alpha
 
 
-def _dynamic_after(fld, p: DynamicSFSParams, zeta0: float):
+def _dynamic_fused(fld, ctx, p: DynamicSFSParams):
+    """M[0:3] = S(J_alpha) - S(J) and M[3:6] = SFS_alpha - SFS from the directly
+    evaluated differences (after the stage's own UJ + Estr at sigma)."""
+    dJ = torch.zeros_like(fld.J)
+    dS = torch.zeros_like(fld.SFS)
+    ctx.dynamic_diff_dev(fld.x, fld.gam, fld.sig, fld.J, p.alpha, dJ, dS, fld.kernel, fld.precision,
+                         fld.transposed)
+    fld.M.zero_()
+    fld.M[:, 0:3] = _stretch(dJ, fld.gam, fld.transposed)
+    fld.M[:, 3:6] = dS
+
+
+def _dynamic_after(fld, p: DynamicSFSParams, zeta0: float, subtract: bool = True):
     G = fld.gam
     M = fld.M
-    M[:, 0:3] -= _stretch(fld.J, G, fld.transposed)
-    M[:, 3:6] -= fld.SFS
+    if subtract:
+        M[:, 0:3] -= _stretch(fld.J, G, fld.transposed)
+        M[:, 3:6] -= fld.SFS
     s = fld.sig
     nume = (M[:, 0] * G[:, 0] + M[:, 1] * G[:, 1] + M[:, 2] * G[:, 2]) * (3 * p.alpha - 2)
     deno = (M[:, 3] * G[:, 0] + M[:, 4] * G[:, 1] + M[:, 5] * G[:, 2]) / (zeta0 / (s * s * s))
@@ -202,13 +221,16 @@ def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSP
     f, g = fld.f, fld.g
     Uinf = torch.tensor(Uinf, dtype=torch.float64, device=fld.x.device)
     fld.M.zero_()
+    fused = sfs is not None and sfs.fused and fld.precision == _lib.FP32COMP and fld.leaflist is None
     for a, b in STAGES:
         first = (a == 1 or a == 0)
-        if sfs is not None and first:
+        if sfs is not None and first and not fused:
             _dynamic_before(fld, ctx, sfs)
         uj(fld, ctx, sfs=sfs is not None, reset=True, reset_sfs=sfs is not None)
         if sfs is not None and first:
-            _dynamic_after(fld, sfs, zeta0)
+            if fused:
+                _dynamic_fused(fld, ctx, sfs)
+            _dynamic_after(fld, sfs, zeta0, subtract=not fused)
         # update_particle_states (src/FLOWVPM_timeintegration.jl:463-532)
         M, G, s = fld.M, fld.gam, fld.sig
         C = fld.C[:, 0]

@@ -165,6 +165,23 @@ int vpm_uj_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* g
                        const double* Ubar, const double* Jbar, double* xbar, double* gbar,
                        double* sbar, int kernel, int precision);
 
+/* The test-filter differences of the pseudo-three-level dynamic SFS procedure
+ * (src/FLOWVPM_subfilterscale.jl:447-673) on device arrays, for one particle
+ * set acting on itself (no static particles):
+ *   dJ[n,9]   = J(alpha sigma) - J(sigma)
+ *   dSFS[n,3] = SFS(alpha sigma; J + dJ) - SFS(sigma; J)
+ * where J[n,9] is the caller's J at sigma and SFS(sigma'; J') is Estr with core
+ * sizes sigma' and gradients J'.  The procedure forms M = S(J_alpha) - S(J)
+ * and SFS_alpha - SFS from these (S the stretching, linear in J).  VPM_FP64
+ * evaluates both filter widths and subtracts, as the reference does;
+ * VPM_FP32COMP evaluates the differences directly from the kernels' g' and g''
+ * (no difference of two FP32 sums), so they keep FP32 relative accuracy.
+ * flags: VPM_TRANSPOSED.  0 < alpha < 1.  No counterpart in the reference (it
+ * calls UJ twice). */
+int vpm_dynamic_diff_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                         const double* J, double alpha, double* dJ, double* dSFS, int kernel, int precision,
+                         int flags);
+
 /* zeta_direct(pfield) (src/FLOWVPM_viscous.jl:467-488), the RBF basis field of
  * core spreading: rows 16:18 (J[1:3]) of every particle, statics included, are
  * set to sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s over every source, the self

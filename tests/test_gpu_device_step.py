@@ -55,10 +55,14 @@ def _compare(pf, fld, tol, tolC, step):
         assert e <= tolC, (step, "C", e)
 
 
-@pytest.mark.parametrize("prec,tol,tolC", [(0, 1e-11, 1e-8), (1, 2e-5, 2e-2)])
+@pytest.mark.parametrize("prec,tol,tolC", [(0, 1e-11, 1e-8), (1, 2e-5, 2e-3)])
 def test_dynamic_sfs_core_spreading_matches_host_mirror(ctx, prec, tol, tolC):
+    """Both precisions of the device step against the FP64 host mirror.  The
+    FP32-comp step takes the test-filter differences from vpm_dynamic_diff_dev,
+    so its coefficients C follow the FP64 ones (subtracting two FP32-comp
+    evaluations instead leaves C with ~1e-2 of noise)."""
     nu, sgm0 = 1e-4, 0.05
-    UJ = vpm.UJ_gb300 if prec == 0 else vpm.UJ_gb300_mixed
+    UJ = vpm.UJ_gb300
     pf, fld = _fields(2000, vpm.gaussianerf, UJ, vpm.SFS_Cd_twolevel_nobackscatter,
                       lambda: vpm.CoreSpreading(nu, sgm0), prec)
     sfs = ds.DynamicSFSParams()
@@ -154,3 +158,26 @@ def test_core_size_reset_matches_host_mirror(ctx, prec, tol):
         for name, rows, t in (("X", slice(0, 3), fld.x), ("Gamma", slice(3, 6), fld.gam)):
             assert normwise(t.cpu().numpy(), P[rows, :n].T)[0] <= tol, (step, name)
         assert bool((fld.sig == sgm0).all()) and np.all(P[6, :n] == sgm0)
+
+
+@pytest.mark.parametrize("kernel,alpha", [(2, 0.999), (3, 0.999), (1, 0.999), (2, 0.667)])
+def test_dynamic_diff_matches_two_fp64_evaluations(ctx, kernel, alpha):
+    """vpm_dynamic_diff_dev against the oracle's two evaluations:
+    dJ = J(alpha sigma) - J(sigma), dSFS = SFS(alpha sigma; J_alpha) - SFS(sigma; J)."""
+    import torch
+    import oracle
+    X, G, s = workloads.leapfrog_rings(3000, nper=10)
+    n = X.shape[0]
+    _, J0 = oracle.uj_pairs(X, X, G, s, kernel)
+    _, Ja = oracle.uj_pairs(X, X, G, s * alpha, kernel)
+    dJ_ref = Ja - J0
+    dS_ref = (oracle.estr_pairs(X, Ja, X, G, s * alpha, Ja, kernel, True) -
+              oracle.estr_pairs(X, J0, X, G, s, J0, kernel, True))
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    for prec, tolJ, tolS in ((0, 1e-10, 1e-9), (1, 2e-6, 2e-5)):
+        dJ = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+        dS = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+        ctx.dynamic_diff_dev(d(X), d(G), d(s), d(J0), alpha, dJ, dS, kernel, prec)
+        eJ = normwise(dJ.cpu().numpy(), dJ_ref)[0]
+        eS = normwise(dS.cpu().numpy(), dS_ref)[0]
+        assert eJ <= tolJ and eS <= tolS, (prec, eJ, eS)

@@ -264,3 +264,18 @@ def test_zeta_matrix_writes_rows_16_18_of_every_particle(ctx, prec):
     other = [r for r in range(46) if r not in (15, 16, 17)]
     assert np.array_equal(P[other, :], Q[other, :])
     assert np.array_equal(P[:, n:], Q[:, n:])
+
+
+@pytest.mark.parametrize("flags", [oracle.RESET | oracle.RESET_SFS | oracle.SFS | oracle.TRANSPOSED, 0])
+def test_uj_matrix_staged_many_threads(ctx, flags):
+    """vpm_uj stages X, Gamma, sigma and the static flag through compact pinned
+    buffers and applies the sums on the host with UJ_direct's reset rules (over
+    several host threads at this size); statics and pre-set rows included."""
+    n = 40000
+    X, G, s = random_cloud(n, seed=123, box=1.0)
+    static = (np.arange(n) % 97) == 5
+    P = matrix_of(X, G, s, static, extra=2, seed=5)
+    Q = P.copy(order="F")
+    oracle.uj_direct(Q, n, 2, flags)
+    ctx.uj(P, n, 2, FP32COMP, flags)
+    _compare_matrix(P, Q, n, FP32COMP, f"staged flags={flags}")
