@@ -240,10 +240,6 @@ constexpr int MID_BLOCKS = 4;               // FP32 blocks per FP32 mid-level su
 #define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
 #endif
 constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
-#ifndef VPM_UJ_UNROLL
-#define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
-#endif
-constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
 
 // Each warp streams the sources on its own: 32 per tile, double-buffered with
 // cp.async, so warps never wait for each other (no block-wide barrier).
