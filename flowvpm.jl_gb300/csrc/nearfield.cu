@@ -58,8 +58,9 @@ enum : int {
 
 typedef unsigned long long ull;
 
-// node centre and radius
-struct __align__(32) NodeCR { double x, y, z, w; };
+// what the traversal reads of a node, in one 64-B record: centre, radius,
+// first child, number of children (0: a leaf) and the leaf's index
+struct __align__(64) TravNode { double x, y, z, w; int first, nkid, leaf, pad[5]; };
 
 __device__ __forceinline__ uint64_t spread3(uint64_t v)
 {
@@ -298,7 +299,8 @@ __global__ void nt_box_inner(int d, const int4* __restrict__ nodes, const ull* _
 }
 
 // centre and radius, in tree.cpp's operation order: c = 0.5 (lo + hi), R = 0.5 sqrt(sum (hi - lo)^2)
-__global__ void nt_cr(const ull* __restrict__ ctr, const double* __restrict__ box, NodeCR* __restrict__ cr)
+__global__ void nt_cr(const ull* __restrict__ ctr, const double* __restrict__ box, const int4* __restrict__ nodes,
+                      const int32_t* __restrict__ node_leaf, TravNode* __restrict__ cr)
 {
     const int64_t nn = (int64_t)ctr[C_NODES];
     for (int64_t id = gtid(); id < nn; id += gstride()) {
@@ -309,14 +311,18 @@ __global__ void nt_cr(const ull* __restrict__ ctr, const double* __restrict__ bo
             const double w = __dsub_rn(b[3 + k], b[k]);
             d2 = __dadd_rn(d2, __dmul_rn(w, w));
         }
-        cr[id] = NodeCR{c[0], c[1], c[2], __dmul_rn(0.5, __dsqrt_rn(d2))};
+        const int4 nd = nodes[id];
+        TravNode t;
+        t.x = c[0]; t.y = c[1]; t.z = c[2]; t.w = __dmul_rn(0.5, __dsqrt_rn(d2));
+        t.first = nd.z; t.nkid = nd.w; t.leaf = node_leaf[id];
+        for (int k = 0; k < 5; k++) t.pad[k] = 0;
+        cr[id] = t;
     }
 }
 
 // -------------------------------------------------------------- traversal
-__global__ void nt_trav(int step, double theta, const int4* __restrict__ nodes, const NodeCR* __restrict__ cr,
-                        const int32_t* __restrict__ node_leaf, const int2* __restrict__ fin, int2* __restrict__ fout,
-                        uint64_t* __restrict__ near, ull* __restrict__ ctr, ull capF, ull capN)
+__global__ void nt_trav(int step, double theta, const TravNode* __restrict__ cr, const int2* __restrict__ fin,
+                        int2* __restrict__ fout, uint64_t* __restrict__ near, ull* __restrict__ ctr, ull capF, ull capN)
 {
     const ull raw = ctr[C_F + step];
     const int64_t cnt = (int64_t)(raw < capF ? raw : capF);
@@ -325,31 +331,32 @@ __global__ void nt_trav(int step, double theta, const int4* __restrict__ nodes, 
     for (int64_t base = (gtid() >> 5) << 5; base < cnt; base += warps << 5) {
         const int64_t i = base + lane;
         unsigned knear = 0, ksplit = 0;
-        int A = 0, B = 0, first = 0;
+        int A = 0, B = 0, first = 0, la_leaf = 0, lb_leaf = 0;
         bool split_a = false;
         if (i < cnt) {
             const int2 ab = fin[i];
             A = ab.x;
             B = ab.y;
-            const NodeCR a = cr[A], c = cr[B];
+            const TravNode a = cr[A], c = cr[B];
             const double dx = __dsub_rn(a.x, c.x), dy = __dsub_rn(a.y, c.y), dz = __dsub_rn(a.z, c.z);
             const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
             const bool far = (A != B) && (__dmul_rn(theta, r) >= __dadd_rn(a.w, c.w));
             if (!far) {
-                const int4 na = nodes[A], nb = nodes[B];
-                const bool la = na.w == 0, lb = nb.w == 0;
+                const bool la = a.nkid == 0, lb = c.nkid == 0;
                 if (la && lb) {
                     knear = 1;
+                    la_leaf = a.leaf;
+                    lb_leaf = c.leaf;
                 } else {
                     split_a = !la && (lb || a.w >= c.w);
-                    first = split_a ? na.z : nb.z;
-                    ksplit = (unsigned)(split_a ? na.w : nb.w);
+                    first = split_a ? a.first : c.first;
+                    ksplit = (unsigned)(split_a ? a.nkid : c.nkid);
                 }
             }
         }
         const ull sn = warp_append(&ctr[C_NEAR], knear);
         if (knear) {
-            if (sn < capN) near[sn] = ((uint64_t)(uint32_t)node_leaf[A] << 32) | (uint32_t)node_leaf[B];
+            if (sn < capN) near[sn] = ((uint64_t)(uint32_t)la_leaf << 32) | (uint32_t)lb_leaf;
             else ctr[C_OVF] = 1;
         }
         const ull sf = warp_append(&ctr[C_F + step + 1], ksplit);
@@ -537,7 +544,7 @@ cudaError_t near_build(NearScratch& s, int64_t n, const double* x, int leaf_size
     NT_TRY(s.nodes.grow(ncap * sizeof(int4)));
     NT_TRY(s.node_lvl.grow(ncap * sizeof(int32_t)));
     NT_TRY(s.node_box.grow(6 * ncap * sizeof(double)));
-    NT_TRY(s.node_cr.grow(ncap * sizeof(NodeCR)));
+    NT_TRY(s.node_cr.grow(ncap * sizeof(TravNode)));
     NT_TRY(s.node_leaf.grow(ncap * sizeof(int32_t)));
     NT_TRY(s.flag.grow(n * sizeof(int32_t)));
     NT_TRY(s.lb.grow(n * sizeof(int32_t)));
@@ -581,13 +588,15 @@ cudaError_t near_build(NearScratch& s, int64_t n, const double* x, int leaf_size
     double* nbox = s.node_box.as<double>();
     nt_box_leaf<<<gs_blocks(2 * n), GS_THREADS, 0, st>>>(nodes, ctr, s.xs.as<double>(), nbox);
     for (int d = MAX_DEPTH; d >= 0; d--) nt_box_inner<<<gs_blocks(n / 2 + 1), GS_THREADS, 0, st>>>(d, nodes, ctr, nbox);
-    nt_cr<<<gs_blocks(2 * n), GS_THREADS, 0, st>>>(ctr, nbox, s.node_cr.as<NodeCR>());
+    nt_cr<<<gs_blocks(2 * n), GS_THREADS, 0, st>>>(ctr, nbox, nodes, s.node_leaf.as<int32_t>(),
+                                                   s.node_cr.as<TravNode>());
     *launches += 2 * MAX_DEPTH + 1 + 4 + (MAX_DEPTH + 1) + 2;
     NT_TRY(cudaGetLastError());
 
     // 4. traversal; on overflow of a frontier or of the near list, grow and repeat
-    if (s.capF == 0) s.capF = (size_t)(n < 4096 ? 4096 : n) * 16;
-    if (s.capN == 0) s.capN = (size_t)(n < 4096 ? 4096 : n) * 16;
+    // a uniform cloud at leaf size 64 and theta 0.4 needs ~32 n frontier pairs and ~16 n near pairs
+    if (s.capF == 0) s.capF = (size_t)(n < 4096 ? 4096 : n) * 40;
+    if (s.capN == 0) s.capN = (size_t)(n < 4096 ? 4096 : n) * 24;
     for (int attempt = 0;; attempt++) {
         NT_TRY(s.fr0.grow(s.capF * sizeof(int2)));
         NT_TRY(s.fr1.grow(s.capF * sizeof(int2)));
@@ -597,8 +606,8 @@ cudaError_t near_build(NearScratch& s, int64_t n, const double* x, int leaf_size
         for (int k = 0; k < TRAV_STEPS; k++) {
             const int2* fin = (k & 1) ? s.fr1.as<int2>() : s.fr0.as<int2>();
             int2* fout = (k & 1) ? s.fr0.as<int2>() : s.fr1.as<int2>();
-            nt_trav<<<GS_BLOCKS, GS_THREADS, 0, st>>>(k, theta, nodes, s.node_cr.as<NodeCR>(), s.node_leaf.as<int32_t>(),
-                                                       fin, fout, s.near0.as<uint64_t>(), ctr, (ull)s.capF, (ull)s.capN);
+            nt_trav<<<GS_BLOCKS, GS_THREADS, 0, st>>>(k, theta, s.node_cr.as<TravNode>(), fin, fout,
+                                                       s.near0.as<uint64_t>(), ctr, (ull)s.capF, (ull)s.capN);
         }
         *launches += TRAV_STEPS + 1;
         NT_TRY(cudaGetLastError());
