@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -107,6 +108,22 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- helpers
+def max_over_ranks(ms: float, dist, device: str) -> float:
+    """The slowest rank's time (every rank gets it); `dist` None = one process."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, units_per_step: float, steps: int, elapsed_ms: float) -> float:
+    """Whole-job rate of `world` independent replicas, each doing `units_per_step`
+    per step, timed by the slowest rank."""
+    return world * units_per_step * steps / (elapsed_ms / 1e3)
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -221,12 +238,9 @@ def run_gpu(args, rank, world):
     launches = ctx.launches - launches0
     elapsed_ms = total.elapsed_time(total_end)
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, "cuda")
     pairs_per_step = float(n) * n
-    value = world * pairs_per_step * args.steps / (elapsed_ms / 1e3)
+    value = replica_rate(world, pairs_per_step, args.steps, elapsed_ms)
     # dominant kernel: the UJ launch (pack is O(N), microseconds); flops per launch / avg duration
     avg_kernel_s = statistics.mean(kernel_ms) / 1e3
     achieved_tflops = FLOP_PER_PAIR * pairs_per_step / avg_kernel_s / 1e12
@@ -347,6 +361,8 @@ def adjoint_ratio(ctx, vpm, torch, n=32000):
         return a.elapsed_time(b)
     fwd = timed(lambda: ctx.uj_dev(x, x, g, sg, U, J, KERNEL, vpm.FP64))
     adj = timed(lambda: ctx.uj_adjoint_dev(x, g, sg, Ub, Jb, xb, gb, sb, KERNEL, vpm.FP64))
+    fwd32 = timed(lambda: ctx.uj_dev(x, x, g, sg, U, J, KERNEL, vpm.FP32COMP))
+    adj32 = timed(lambda: ctx.uj_adjoint_dev(x, g, sg, Ub, Jb, xb, gb, sb, KERNEL, vpm.FP32COMP))
     steps = 5
     kw = dict(kernel=KERNEL, precision=vpm.FP64, vctx=ctx)
 
@@ -363,6 +379,8 @@ def adjoint_ratio(ctx, vpm, torch, n=32000):
     t_grad = timed(roll_grad(True))
     t_grad_rc = timed(roll_grad("recompute"))
     return {"n_particles": n, "uj_fwd_ms": fwd, "uj_adjoint_ms": adj, "uj_adjoint_over_fwd": adj / fwd,
+            "uj_fwd_ms_fp32comp": fwd32, "uj_adjoint_ms_fp32comp": adj32,
+            "uj_adjoint_over_fwd_fp32comp": adj32 / fwd32,
             "rollout_steps": steps, "rollout_fwd_ms": t_roll, "rollout_grad_ms": t_grad,
             "rollout_grad_over_fwd": t_grad / t_roll, "rollout_backward_over_fwd": (t_grad - t_roll) / t_roll,
             "rollout_grad_recompute_ms": t_grad_rc, "rollout_grad_recompute_over_fwd": t_grad_rc / t_roll,
@@ -525,9 +543,10 @@ def run_jet(args):
     octree (leaf size 64, theta = 0.4) and its leaf-pair lists are built on the
     GPU at every UJ call, and every near leaf pair is evaluated by P2P in
     FP32-comp (UJ, and Estr where the step asks for it).  The far field is not
-    computed.  Reported: the tree build alone, one UJ (+Estr) call, and whole
-    rVPM RK3 steps with dynamic SFS and relaxation (5 near-field UJ calls, 4
-    with Estr)."""
+    computed.  Reported: the tree build alone, one UJ (+Estr) call, one call of
+    the dynamic procedure's near-field differences, and whole rVPM RK3 steps
+    with dynamic SFS and relaxation (4 near-field UJ calls, 3 with Estr, and
+    the differences)."""
     import torch
     import vpm_gb300 as vpm
     from vpm_gb300 import device_step as ds, workloads
@@ -561,6 +580,8 @@ def run_jet(args):
     kw = dict(leaf_size=leaf, theta=theta, kernel=KERNEL, precision=vpm.FP32COMP)
     ms_uj, st = timed(lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, **kw), 5)
     ms_ujs, _ = timed(lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, S, sfs=True, **kw), 5)
+    dJ, dS = torch.zeros_like(J), torch.zeros_like(S)
+    ms_dyn, _ = timed(lambda: ctx.dynamic_diff_leaflist_dev(x, g, sg, J, 0.999, dJ, dS, **kw), 5)
     ms_uj64, _ = timed(lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, leaf_size=leaf, theta=theta, kernel=KERNEL,
                                                     precision=vpm.FP64), 1)
     # accuracy of the FP32-comp near field against the FP64 near field over the same lists
@@ -587,13 +608,77 @@ def run_jet(args):
            "tree_build_ms": ms_tree,
            "uj_call_ms": ms_uj, "uj_pairs_per_s": pairs / (ms_uj / 1e3),
            "uj_estr_call_ms": ms_ujs, "uj_estr_pairs_per_s": 2 * pairs / (ms_ujs / 1e3),
+           "dynamic_diff_call_ms": ms_dyn,
            "uj_call_ms_fp64": ms_uj64, "fp32comp_over_fp64": ms_uj64 / ms_uj,
            "err_fp32comp_vs_fp64": {"U_max_rel": rel(U32, U64), "J_max_rel": rel(J32, J64)},
            "step_ms": ms_step, "steps_timed": nst, "particle_steps_per_s": n / (ms_step / 1e3),
-           "step": "rVPM RK3 + dynamic SFS + Pedrizzetti relaxation, 5 near-field UJ calls (4 with Estr), "
-                   "tree rebuilt at each call",
+           "step": "rVPM RK3 + dynamic SFS + Pedrizzetti relaxation: 4 near-field UJ calls (3 with Estr) and "
+                   "the near-field test-filter differences, tree rebuilt at each call",
            "far_field": "not computed (FastMultipole.jl's multipole part is outside this library)"}
     print(json.dumps(out), flush=True)
+
+
+def run_rollout(args):
+    """Adjoint of a rollout: the isolated ring at 1000 sections x 32 particles
+    (32,000 particles, R=1, a=0.1R, sigma=a/2, Gaussian-erf), rVPM RK3 with
+    Pedrizzetti relaxation, --ro-steps steps of dt=0.01; loss = kinetic-energy
+    estimate + strength-weighted axial centroid at the final step.  FP64
+    forward and its gradient with per-step checkpointing (each step's UJ values
+    kept, the adjoint kernel in the backward pass), checked against central
+    differences (h=1e-6) along --ro-dirs seeded random unit directions in
+    (X, Gamma, sigma); the FP32-comp forward is timed beside it."""
+    import torch
+    import vpm_gb300 as vpm
+    import vpm_gb300.rings as rings
+    from vpm_gb300 import autodiff as ad
+    ctx = vpm.Context(0)
+    X, G, s, _ = rings.ring_sections(1.0, 1.0, 0.1, 1000, 32, 0.05)
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    x0, g0, s0 = d(X), d(G), d(s)
+    steps, dt = args.ro_steps, 0.01
+    kw = dict(kernel=KERNEL, precision=vpm.FP64, vctx=ctx)
+
+    def loss_at(x, g, sg, prec=vpm.FP64):
+        k2 = dict(kernel=KERNEL, precision=prec, vctx=ctx)
+        with torch.no_grad():
+            return float(ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=False, **k2), **k2))
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3, out
+    ms_fwd, L0 = timed(lambda: loss_at(x0, g0, s0))
+    ms_fwd32, L32 = timed(lambda: loss_at(x0, g0, s0, vpm.FP32COMP))
+
+    def grad():
+        x, g, sg = x0.clone().requires_grad_(), g0.clone().requires_grad_(), s0.clone().requires_grad_()
+        ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=True, **kw), **kw).backward()
+        return x.grad, g.grad, sg.grad
+    ms_grad, (gx, gg, gs) = timed(grad)
+    rng = np.random.default_rng(3)
+    h = 1e-6
+    worst = 0.0
+    checks = []
+    for _ in range(args.ro_dirs):
+        v = [d(rng.normal(size=t.shape)) for t in (x0, g0, s0)]
+        nrm = math.sqrt(sum(float((t * t).sum()) for t in v))
+        v = [t / nrm for t in v]
+        fd = (loss_at(x0 + h * v[0], g0 + h * v[1], s0 + h * v[2]) -
+              loss_at(x0 - h * v[0], g0 - h * v[1], s0 - h * v[2])) / (2 * h)
+        an = float((gx * v[0]).sum() + (gg * v[1]).sum() + (gs * v[2]).sum())
+        rel = abs(fd - an) / max(abs(an), 1e-300)
+        worst = max(worst, rel)
+        checks.append({"fd": fd, "adjoint": an, "rel": rel})
+    print(json.dumps({"mode": "rollout", "n_particles": X.shape[0], "steps": steps, "dt": dt,
+                      "loss_fp64": L0, "loss_fp32comp": L32, "forward_ms_fp64": ms_fwd,
+                      "forward_ms_fp32comp": ms_fwd32, "gradient_ms_fp64": ms_grad,
+                      "gradient_over_forward": ms_grad / ms_fwd,
+                      "backward_over_forward": (ms_grad - ms_fwd) / ms_fwd,
+                      "fd_directions": args.ro_dirs, "fd_h": h, "fd_max_rel_err": worst, "fd_checks": checks,
+                      "note": "gradient = forward + backward with per-step checkpointing that keeps each step's "
+                              "UJ values; central differences of the FP64 forward"}), flush=True)
 
 
 def run_kernel_only_jet(args):
@@ -638,13 +723,15 @@ def main():
     ap.add_argument("--kernel", default="gaussianerf", choices=["singular", "gaussian", "gaussianerf", "winckelmans"])
     ap.add_argument("--estr", action="store_true")
     # the other workloads (one JSON line each, not the bench line)
-    ap.add_argument("--workload", default="cloud", choices=["cloud", "leapfrog", "jet"])
+    ap.add_argument("--workload", default="cloud", choices=["cloud", "leapfrog", "jet", "rollout"])
     ap.add_argument("--lf-n", type=int, default=200_000)
     ap.add_argument("--lf-steps", type=int, default=200)
     ap.add_argument("--lf-f64-steps", type=int, default=2)
     ap.add_argument("--lf-small", type=int, default=20_000)
     ap.add_argument("--jet-n", type=int, default=1 << 20)
     ap.add_argument("--jet-steps", type=int, default=3)
+    ap.add_argument("--ro-steps", type=int, default=50)
+    ap.add_argument("--ro-dirs", type=int, default=4)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
@@ -654,6 +741,8 @@ def main():
         run_leapfrog(args)
     elif args.workload == "jet":
         run_jet(args)
+    elif args.workload == "rollout":
+        run_rollout(args)
     elif args.kernel_only:
         run_kernel_only(args)
     elif args.impl == "reference":

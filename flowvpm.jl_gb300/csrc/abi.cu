@@ -918,6 +918,112 @@ int vpm_p2p_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
     return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags, stats);
 }
 
+int vpm_zeta_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig, double* W,
+                          int leaf_size, double theta, int kernel, int precision, int64_t* stats)
+{
+    const char* fn = "vpm_zeta_leaflist_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (stats) stats[0] = stats[1] = stats[2] = 0;
+    if (leaf_size < 1 || leaf_size > LEAF_SIZE_MAX)
+        return fail(c, VPM_ERR_ARG, "%s: leaf_size must be in 1..%d", fn, LEAF_SIZE_MAX);
+    if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "%s: bad theta", fn);
+    if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    RC(check_kernel(c, kernel, precision));
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(W))
+        return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
+    NearLists L;
+    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, &L, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
+    e = near_groups(c->near, &L, c->stream, near_sync, c, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
+    RC(grow(c, c->leaf, leaf_work_bytes(n), "near-field packs"));
+    LeafArgs a;
+    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = nullptr; a.J = nullptr; a.SFS = nullptr;
+    a.static_flags = nullptr; a.kernel = kernel; a.precision = precision; a.sfs = false; a.transposed = true;
+    CK(launch_leaf_zeta(a, L, W, c->leaf.p, c->stream, &c->launches), "near-field zeta");
+    RC(bounded_wait(c));
+    if (stats) {
+        stats[0] = L.nleaves;
+        stats[1] = L.nlpairs;
+        stats[2] = L.pairs;
+    }
+    return VPM_OK;
+}
+
+int vpm_dynamic_diff_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
+                                  const uint8_t* static_flags, const double* J, double alpha, double* dJ,
+                                  double* dSFS, int leaf_size, double theta, int kernel, int precision, int flags,
+                                  int64_t* stats)
+{
+    const char* fn = "vpm_dynamic_diff_leaflist_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (stats) stats[0] = stats[1] = stats[2] = 0;
+    if (leaf_size < 1 || leaf_size > LEAF_SIZE_MAX)
+        return fail(c, VPM_ERR_ARG, "%s: leaf_size must be in 1..%d", fn, LEAF_SIZE_MAX);
+    if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "%s: bad theta", fn);
+    if (!(alpha > 0.0 && alpha < 1.0)) return fail(c, VPM_ERR_ARG, "%s: alpha must be in (0, 1)", fn);
+    if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
+    if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    RC(check_kernel(c, kernel, precision));
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(J) || !is_device_ptr(dJ) ||
+        !is_device_ptr(dSFS) || (static_flags && !is_device_ptr(static_flags)))
+        return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
+    cudaStream_t st = c->stream;
+    NearLists L;
+    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, st, near_sync, c, &L, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
+    e = near_groups(c->near, &L, st, near_sync, c, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
+    RC(grow(c, c->leaf, leaf_work_bytes(n), "near-field packs"));
+    RC(grow(c, c->s, n * sizeof(double), "test-filter core sizes"));
+    double* sig_a = (double*)c->s.p;
+    scale_copy<<<nblk(n), EB, 0, st>>>(n, sig, alpha, sig_a);
+    c->launches++;
+    CK(cudaMemsetAsync(dJ, 0, 9 * n * sizeof(double), st), "memset dJ");
+    CK(cudaMemsetAsync(dSFS, 0, 3 * n * sizeof(double), st), "memset dSFS");
+    LeafArgs a;
+    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = nullptr; a.J = const_cast<double*>(J); a.SFS = dSFS;
+    a.static_flags = static_flags; a.kernel = kernel; a.precision = precision; a.sfs = true;
+    a.transposed = (flags & VPM_TRANSPOSED) != 0;
+    if (precision == VPM_FP32COMP) {
+        CK(launch_leaf_dynamic(a, L, alpha, sig_a, dJ, dSFS, c->leaf.p, st, &c->launches),
+           "near-field test-filter differences");
+    } else {
+        // FP64: the near-field leg at alpha sigma, the Estr pass at sigma with J, then the differences
+        RC(grow(c, c->mat2, (size_t)18 * n * sizeof(double), "test-filter scratch"));
+        double* Ua = (double*)c->mat2.p;
+        double* Ja = Ua + 3 * n;
+        double* Sa = Ja + 9 * n;
+        double* S0 = Sa + 3 * n;
+        CK(cudaMemsetAsync(Ua, 0, (size_t)18 * n * sizeof(double), st), "memset scratch");
+        LeafArgs b = a;
+        b.sig = sig_a; b.U = Ua; b.J = Ja; b.SFS = Sa;
+        CK(launch_leaflist(b, L, c->leaf.p, st, &c->launches), "test-filter near field");
+        LeafArgs z = a;
+        z.uj = false; z.SFS = S0;
+        CK(launch_leaflist(z, L, c->leaf.p, st, &c->launches), "near-field Estr");
+        sub_arrays<<<nblk(9 * n), EB, 0, st>>>(9 * n, Ja, J, dJ);
+        sub_arrays<<<nblk(3 * n), EB, 0, st>>>(3 * n, Sa, S0, dSFS);
+        c->launches += 2;
+        CK(cudaGetLastError(), "differences");
+    }
+    RC(bounded_wait(c));
+    if (stats) {
+        stats[0] = L.nleaves;
+        stats[1] = L.nlpairs;
+        stats[2] = L.pairs;
+    }
+    return VPM_OK;
+}
+
 int vpm_p2p_lists_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
                       const uint8_t* static_flags, double* U, double* J, double* SFS, const int32_t* perm,
                       int64_t nl, const int64_t* leaf_begin, const int64_t* leaf_end, const int64_t* row,
@@ -1030,7 +1136,9 @@ int vpm_uj_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam
     RC(enter(c));
     if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: n out of range");
     RC(check_kernel(c, kernel, precision));
-    if (precision != VPM_FP64) return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: only VPM_FP64 is implemented");
+    if (precision == VPM_FP32COMP && kernel == VPM_KERNEL_GAUSSIAN)
+        return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: the FP32-comp adjoint covers the singular, Gaussian-erf "
+                                    "and Winckelmans kernels (the Gaussian kernel needs VPM_FP64)");
     if (n == 0) return VPM_OK;
     DeviceGuard dg(c->device);
     if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(Ubar) ||

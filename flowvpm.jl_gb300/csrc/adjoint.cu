@@ -21,6 +21,7 @@
 // atomic per source and block (so the summation order of those sums is not
 // fixed).  Arithmetic is FP64 throughout.
 #include "internal.h"
+#include "uj_pair.cuh"
 #include "vpm_math.cuh"
 
 namespace vpm {
@@ -200,6 +201,292 @@ __global__ void pack_src_adj(int64_t ns, int64_t ns_pad, const double* __restric
     out[i] = p;
 }
 
+// ------------------------------------------------------------- FP32-comp adjoint
+// The same pair derivatives in FP32 with the forward mixed kernel's layout:
+// targets and sources in Morton order, FP32 offsets from the warp's first
+// target, four-source votes between the singular form (every lane's pairs
+// beyond s_far and twice the warp radius) and the full form on the
+// double-float displacement.  With s = r^2/sigma^2 and e = e^{-s/2}, the
+// coefficients of the pair term are written so that nothing cancels at small s:
+//   A   = -C4 sigma^-3 G(s),   G = g/rho^3
+//   B   = -C4 sigma^-5 H(s),   H = (g'/rho^2 - 3 g/rho^3)/s
+//   B'/r= -C4 sigma^-7 K(s),   K = (g'' rho^2 - 7 g' rho + 15 g)/(rho^3 s^2)
+//   dA/dsigma = C4 sigma^-4 a(s),  a = g'/rho^2
+//   dB/dsigma = -C4 sigma^-6 b(s), b = (2 g' - rho g'')/rho^4
+// (Gaussian-erf: G, H and K from one series of positive terms below s = 6, G
+// from the erfcx fit above; a = b = sqrt(2/pi) e.  Winckelmans: rational, q = s + 1:
+// G = (s+2.5) q^-2.5, H = -3 (s+3.5) q^-3.5, K = (15 s + 67.5) q^-4.5,
+// a = 7.5 q^-3.5, b = 52.5 q^-4.5.  Singular form: G = s^-1.5, H = -3 s^-2.5,
+// K = 15 s^-3.5, a = b = 0.)  Source-side sums are reduced across the warp in
+// FP32, across the block's warps, then added with one FP64 atomic per source
+// and block; target-side sums in FP32 blocks of 64 sources, then FP64.
+
+// S3(s) = sum_m s^m/(2m+7)!! (16 terms: 1e-9 relative at s = 6).  Kummer's series
+// of erf gives Gaussian-erf's G = c2 e (1/3 + s S2), H = -3 c2 e S2, K = 15 c2 e S3
+// with S2 = 1/15 + s S3 and e = e^{-s/2}: positive terms, where the closed forms
+// H = (a - 3G)/s and K = (15 G - a (5 + s))/s^2 lose up to 20x (s = 2) to cancellation.
+__device__ __forceinline__ float gerf_S3_series(float s)
+{
+    float p = 3.1266513920057787e-24f;
+    p = fmaf(p, s, 1.2193940428822536e-22f);
+    p = fmaf(p, s, 4.5117579586643385e-21f);
+    p = fmaf(p, s, 1.5791152855325184e-19f);
+    p = fmaf(p, s, 5.211080442257311e-18f);
+    p = fmaf(p, s, 1.6154349370997664e-16f);
+    p = fmaf(p, s, 4.684761317589322e-15f);
+    p = fmaf(p, s, 1.264885555749117e-13f);
+    p = fmaf(p, s, 3.1622138893727926e-12f);
+    p = fmaf(p, s, 7.273091945557423e-11f);
+    p = fmaf(p, s, 1.5273493085670588e-09f);
+    p = fmaf(p, s, 2.901963686277412e-08f);
+    p = fmaf(p, s, 4.9333382666716e-07f);
+    p = fmaf(p, s, 7.4000074000074e-06f);
+    p = fmaf(p, s, 9.62000962000962e-05f);
+    p = fmaf(p, s, 0.0010582010582010583f);
+    p = fmaf(p, s, 0.009523809523809525f);
+    return p;
+}
+constexpr float S_SERIES_ADJ = 6.0f;   // Gaussian-erf adjoint: series below this s (closed forms lose < 3x above)
+
+// (G, H, K, a, b) of kernel K at s (any s > 0) in FP32
+template <int K>
+__device__ __forceinline__ void adj_coeffs_f32(float s, float& G, float& H, float& Kc, float& a, float& b)
+{
+    if constexpr (K == K_GAUSERF) {
+        if (s > S_FAR_GERF) {
+            const float rs = rsqrtf(s), rs2 = rs * rs;
+            G = rs * rs2; H = -3.0f * G * rs2; Kc = -5.0f * H * rs2; a = 0.0f; b = 0.0f;
+        } else {
+            const float e = exp2f(s * -0.72134752044448170f);
+            a = F_C2 * e;
+            b = a;
+            if (s < S_SERIES_ADJ) {
+                const float p3 = gerf_S3_series(s);
+                const float p2 = fmaf(s, p3, 0.066666666666666667f);
+                G = a * fmaf(s, p2, 0.33333333333333333f);
+                H = -3.0f * a * p2;
+                Kc = 15.0f * a * p3;
+            } else {
+                const float rs = rsqrtf(s), rs2 = rs * rs;
+                G = gerf_G_erfcx(s, e, rs);
+                H = (a - 3.0f * G) * rs2;
+                Kc = fmaf(15.0f, G, -a * (5.0f + s)) * rs2 * rs2;
+            }
+        }
+    } else if constexpr (K == K_WNKLMNS) {
+        const float q = s + 1.0f;
+        const float iq = __frcp_rn(q);
+        const float iq25 = iq * iq * rsqrtf(q);
+        const float iq35 = iq25 * iq, iq45 = iq35 * iq;
+        G = (s + 2.5f) * iq25;
+        H = -3.0f * (s + 3.5f) * iq35;
+        Kc = fmaf(15.0f, s, 67.5f) * iq45;
+        a = 7.5f * iq35;
+        b = 52.5f * iq45;
+    } else {   // singular
+        const float rs = rsqrtf(s), rs2 = rs * rs;
+        G = rs * rs2; H = -3.0f * G * rs2; Kc = -5.0f * H * rs2; a = 0.0f; b = 0.0f;
+    }
+}
+
+// The seven derivatives of phi for one pair in FP32 (o[0..2] d/d(dx), o[3..5]
+// d/dGamma, o[6] d/dsigma), from the coefficients of the pair.
+__device__ __forceinline__ void adj_pair_f32(float dx, float dy, float dz, float Gx, float Gy, float Gz, float A,
+                                             float B, float Bpr, float dA, float dB, const float (&Ub)[3],
+                                             const float (&Jb)[9], const float (&wb)[3], float (&o)[7])
+{
+    const float cx = fmaf(dy, Gz, -dz * Gy), cy = fmaf(dz, Gx, -dx * Gz), cz = fmaf(dx, Gy, -dy * Gx);
+    const float JDx = fmaf(Jb[0], dx, fmaf(Jb[3], dy, Jb[6] * dz));
+    const float JDy = fmaf(Jb[1], dx, fmaf(Jb[4], dy, Jb[7] * dz));
+    const float JDz = fmaf(Jb[2], dx, fmaf(Jb[5], dy, Jb[8] * dz));
+    const float JTcx = fmaf(Jb[0], cx, fmaf(Jb[1], cy, Jb[2] * cz));
+    const float JTcy = fmaf(Jb[3], cx, fmaf(Jb[4], cy, Jb[5] * cz));
+    const float JTcz = fmaf(Jb[6], cx, fmaf(Jb[7], cy, Jb[8] * cz));
+    const float P = fmaf(Ub[0], cx, fmaf(Ub[1], cy, fmaf(Ub[2], cz, fmaf(wb[0], Gx, fmaf(wb[1], Gy, wb[2] * Gz)))));
+    const float Q = fmaf(cx, JDx, fmaf(cy, JDy, cz * JDz));
+    const float sc = fmaf(B, P, Bpr * Q);
+    o[0] = fmaf(sc, dx, fmaf(A, fmaf(Gy, Ub[2], -Gz * Ub[1]), B * (fmaf(Gy, JDz, -Gz * JDy) + JTcx)));
+    o[1] = fmaf(sc, dy, fmaf(A, fmaf(Gz, Ub[0], -Gx * Ub[2]), B * (fmaf(Gz, JDx, -Gx * JDz) + JTcy)));
+    o[2] = fmaf(sc, dz, fmaf(A, fmaf(Gx, Ub[1], -Gy * Ub[0]), B * (fmaf(Gx, JDy, -Gy * JDx) + JTcz)));
+    o[3] = fmaf(A, fmaf(Ub[1], dz, fmaf(-Ub[2], dy, wb[0])), B * fmaf(JDy, dz, -JDz * dy));
+    o[4] = fmaf(A, fmaf(Ub[2], dx, fmaf(-Ub[0], dz, wb[1])), B * fmaf(JDz, dx, -JDx * dz));
+    o[5] = fmaf(A, fmaf(Ub[0], dy, fmaf(-Ub[1], dx, wb[2])), B * fmaf(JDx, dy, -JDy * dx));
+    o[6] = fmaf(dA, P, dB * Q);
+}
+
+// Packed source of the FP32-comp adjoint, 48 B: position as a double-float,
+// 1/sigma, Gamma, and the particle's index.
+struct __align__(16) SrcAdjMixed { float4 a; float4 b; float4 g; };
+
+template <int K>
+__global__ void pack_src_adj_mixed(int64_t n, int64_t ns_pad, const double* __restrict__ xs,
+                                   const double* __restrict__ gs, const double* __restrict__ sgs,
+                                   const TgtPos* __restrict__ order, SrcAdjMixed* __restrict__ out)
+{
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= ns_pad) return;
+    SrcAdjMixed p;
+    if (o < n) {
+        const int64_t i = order[o].idx;
+        const double x = xs[3 * i], y = xs[3 * i + 1], z = xs[3 * i + 2];
+        const float xh = (float)x, yh = (float)y, zh = (float)z;
+        const double sig = (K == K_SING) ? 1.0 : sgs[i];
+        p.a = make_float4(xh, yh, zh, (float)(1.0 / sig));
+        p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
+        p.g = make_float4((float)gs[3 * i], (float)gs[3 * i + 1], (float)gs[3 * i + 2], __int_as_float((int)i));
+    } else {   // padding: far away, no strength
+        p.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+        p.b = make_float4(0.f, 0.f, 0.f, 0.f);
+        p.g = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    }
+    out[o] = p;
+}
+
+template <int K>
+__global__ void __launch_bounds__(UJ_THREADS)
+uj_adjoint_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Ubar,
+                        const double* __restrict__ Jbar, int64_t ns_pad, const SrcAdjMixed* __restrict__ src,
+                        int64_t per_split, double* xbar, double* gbar, double* sbar)
+{
+    __shared__ SrcAdjMixed tile[UJ_TILE];
+    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    __shared__ float red[UJ_WARPS][UJ_TILE][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
+    const bool valid = t < nt;
+    double tx = 3.0e4, ty = 3.0e4, tz = 3.0e4;
+    int64_t idx = 0;
+    float Ub[3] = {0.f, 0.f, 0.f}, Jb[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Jb[k] = 0.f;
+    if (valid) {
+        const TgtPos p = tgt[t];
+        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
+#pragma unroll
+        for (int k = 0; k < 3; k++) Ub[k] = (float)Ubar[3 * idx + k];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Jb[k] = (float)Jbar[9 * idx + k];
+    }
+    const float wb[3] = {Jb[1 + 3 * 2] - Jb[2 + 3 * 1], Jb[2 + 3 * 0] - Jb[0 + 3 * 2], Jb[0 + 3 * 1] - Jb[1 + 3 * 0]};
+    const float3 th = make_float3((float)tx, (float)ty, (float)tz);
+    const float3 tl = make_float3((float)(tx - (double)th.x), (float)(ty - (double)th.y), (float)(tz - (double)th.z));
+    const double ox = __shfl_sync(0xffffffffu, tx, 0);
+    const double oy = __shfl_sync(0xffffffffu, ty, 0);
+    const double oz = __shfl_sync(0xffffffffu, tz, 0);
+    const float3 oh = make_float3((float)ox, (float)oy, (float)oz);
+    const float3 ol = make_float3((float)(ox - (double)oh.x), (float)(oy - (double)oh.y), (float)(oz - (double)oh.z));
+    const float3 to = valid ? make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz))
+                            : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
+    float b2 = valid ? fmaf(to.x, to.x, fmaf(to.y, to.y, to.z * to.z)) : 0.0f;
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
+    const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
+    const float sfar = singular_tail<K>() ? s_far<K>() : 3.0e38f;
+
+    double accd[3] = {0.0, 0.0, 0.0};
+    float acc[3] = {0.f, 0.f, 0.f};
+    const int64_t s0 = (int64_t)blockIdx.y * per_split;
+    const int64_t s1 = min(s0 + per_split, ns_pad);
+    for (int64_t base = s0; base < s1; base += UJ_TILE) {
+        __syncthreads();
+        tile[threadIdx.x] = src[base + threadIdx.x];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < UJ_TILE / 32; q++) {
+            const int j = lane + 32 * q;
+            const float4 a = tile[j].a, b = tile[j].b;
+            const float sg2 = 1.0f / (a.w * a.w);
+            off[warp][j] = make_float4((a.x - oh.x) + (b.x - ol.x), (a.y - oh.y) + (b.y - ol.y),
+                                       (a.z - oh.z) + (b.z - ol.z), fmaxf(sfar * sg2, r2n));
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int j0 = 0; j0 < UJ_TILE; j0 += 4) {
+            float dx[4], dy[4], dz[4], r2[4];
+            bool far = true;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float4 h = off[warp][j0 + q];
+                dx[q] = to.x - h.x; dy[q] = to.y - h.y; dz[q] = to.z - h.z;
+                r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
+                far = far && r2[q] > h.w;
+            }
+            const bool allfar = __all_sync(0xffffffffu, far);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const SrcAdjMixed& sp = tile[j0 + q];
+                const float isig = sp.a.w;
+                float ex = dx[q], ey = dy[q], ez = dz[q], e2 = r2[q];
+                if (!allfar) {   // double-float displacement
+                    ex = (th.x - sp.a.x) + (tl.x - sp.b.x);
+                    ey = (th.y - sp.a.y) + (tl.y - sp.b.y);
+                    ez = (th.z - sp.a.z) + (tl.z - sp.b.z);
+                    e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                }
+                float o[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if (e2 > 0.0f) {
+                    const float i2 = isig * isig;
+                    const float s = e2 * i2;
+                    float G, H, Kc, a, b;
+                    if (allfar) {   // singular form (no sigma derivative)
+                        const float rs = rsqrtf(s), rs2 = rs * rs;
+                        G = rs * rs2; H = -3.0f * G * rs2; Kc = -5.0f * H * rs2; a = 0.0f; b = 0.0f;
+                    } else {
+                        adj_coeffs_f32<K>(s, G, H, Kc, a, b);
+                    }
+                    const float i3 = i2 * isig;
+                    const float A = -F_C4 * i3 * G;
+                    const float B = -F_C4 * i3 * i2 * H;
+                    const float Bpr = -F_C4 * i3 * i2 * i2 * Kc;
+                    const float dA = F_C4 * i2 * i2 * a;
+                    const float dB = -F_C4 * i3 * i3 * b;
+                    adj_pair_f32(ex, ey, ez, sp.g.x, sp.g.y, sp.g.z, A, B, Bpr, dA, dB, Ub, Jb, wb, o);
+                }
+                if (!valid) {
+#pragma unroll
+                    for (int k = 0; k < 7; k++) o[k] = 0.f;
+                }
+                acc[0] += o[0]; acc[1] += o[1]; acc[2] += o[2];
+                o[0] = -o[0]; o[1] = -o[1]; o[2] = -o[2];
+#pragma unroll
+                for (int k = 0; k < 7; k++) {
+                    float v = o[k];
+#pragma unroll
+                    for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+                    o[k] = v;
+                }
+                if (lane == 0) {
+#pragma unroll
+                    for (int k = 0; k < 7; k++) red[warp][j0 + q][k] = o[k];
+                }
+            }
+            if ((j0 & 63) == 60) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) { accd[k] += (double)acc[k]; acc[k] = 0.f; }
+            }
+        }
+        __syncthreads();
+        const int si = (int)__float_as_int(tile[threadIdx.x].g.w);
+        if (si >= 0) {
+            double v[7];
+#pragma unroll
+            for (int k = 0; k < 7; k++)
+                v[k] = (double)red[0][threadIdx.x][k] + (double)red[1][threadIdx.x][k] +
+                       (double)red[2][threadIdx.x][k] + (double)red[3][threadIdx.x][k];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                atomicAdd(&xbar[3 * (int64_t)si + k], v[k]);
+                atomicAdd(&gbar[3 * (int64_t)si + k], v[3 + k]);
+            }
+            if (K != K_SING) atomicAdd(&sbar[si], v[6]);
+        }
+    }
+    if (valid) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) atomicAdd(&xbar[3 * idx + k], accd[k] + (double)acc[k]);
+    }
+}
+
 template <int K>
 static cudaError_t launch_adj_k(const AdjArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
                                 int64_t* launches)
@@ -212,11 +499,19 @@ static cudaError_t launch_adj_k(const AdjArgs& a, const Workspace& w, int num_sm
     const TgtPos* tgt = nullptr;
     cudaError_t e = order_targets(a.n, a.x, w.order, w.order_bytes, st, launches, &tgt);
     if (e != cudaSuccess) return e;
-    SrcF64* src = (SrcF64*)w.src_pack;
-    pack_src_adj<K><<<(unsigned)((ns_pad + 255) / 256), 256, 0, st>>>(a.n, ns_pad, a.x, a.gam, a.sig, src);
     const dim3 grid((unsigned)(nt_pad / UJ_THREADS), (unsigned)nsplit);
-    uj_adjoint_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.n, tgt, a.Ubar, a.Jbar, a.n, ns_pad, src, per_split,
-                                                          a.xbar, a.gbar, a.sbar);
+    if (a.precision) {
+        SrcAdjMixed* src = (SrcAdjMixed*)w.src_pack;
+        pack_src_adj_mixed<K><<<(unsigned)((ns_pad + 255) / 256), 256, 0, st>>>(a.n, ns_pad, a.x, a.gam, a.sig, tgt,
+                                                                                src);
+        uj_adjoint_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.n, tgt, a.Ubar, a.Jbar, ns_pad, src, per_split,
+                                                                a.xbar, a.gbar, a.sbar);
+    } else {
+        SrcF64* src = (SrcF64*)w.src_pack;
+        pack_src_adj<K><<<(unsigned)((ns_pad + 255) / 256), 256, 0, st>>>(a.n, ns_pad, a.x, a.gam, a.sig, src);
+        uj_adjoint_f64_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.n, tgt, a.Ubar, a.Jbar, a.n, ns_pad, src, per_split,
+                                                              a.xbar, a.gbar, a.sbar);
+    }
     *launches += 2;
     return cudaGetLastError();
 }

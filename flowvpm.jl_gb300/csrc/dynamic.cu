@@ -26,6 +26,7 @@
 //     + Estr(alpha sigma; dJ)                                                     (an ordinary Estr)
 // with zeta~(r, sigma) = zeta(r/sigma)/sigma^3; the first is the Estr kernel in
 // its weight-difference mode (estr.cu), the second the Estr kernel itself.
+#include "dyn_math.cuh"
 #include "internal.h"
 #include "uj_pair.cuh"
 #include "vpm_math.cuh"
@@ -33,64 +34,6 @@
 #include <cmath>
 
 namespace vpm {
-
-// g'(t) and g''(t) of kernel K in FP32 (src/FLOWVPM_kernel.jl:45-84, differentiated)
-template <int K>
-__device__ __forceinline__ void g_d1_d2_f32(float t, float& d1, float& d2)
-{
-    if constexpr (K == K_GAUSERF) {
-        const float e = F_C2 * exp2f(t * t * -0.72134752044448170f);   // sqrt(2/pi) e^{-t^2/2}
-        d1 = t * t * e;
-        d2 = t * (2.0f - t * t) * e;
-    } else if constexpr (K == K_GAUS) {
-        const float t3 = t * t * t;
-        const float e = exp2f(t3 * -1.4426950408889634f);              // e^{-t^3}
-        d1 = 3.0f * t * t * e;
-        d2 = t * (6.0f - 9.0f * t3) * e;
-    } else if constexpr (K == K_WNKLMNS) {
-        const float q = fmaf(t, t, 1.0f);
-        const float iq = __frcp_rn(q);
-        const float iq35 = iq * iq * iq * rsqrtf(q);                   // q^-3.5
-        d1 = 7.5f * t * t * iq35;
-        d2 = 7.5f * t * (2.0f - 5.0f * t * t) * iq35 * iq;
-    } else {
-        d1 = 0.0f;
-        d2 = 0.0f;
-    }
-}
-
-// s = rho^2 beyond which a pair's filter differences are below 1e-12 of the
-// near pairs' (warp-wide skip); +inf: never skipped
-template <int K>
-__host__ __device__ constexpr float dyn_skip_s()
-{
-    return K == K_GAUSERF ? 60.0f : K == K_GAUS ? 9.0f : 3.0e38f;
-}
-
-// (dg, dg1) of one pair at rho for the filter factor alpha (ha = 1/alpha - 1):
-// m two-point Gauss-Legendre panels on [rho, rho/alpha] (m from ha, warp-uniform;
-// one panel for alpha = 0.999, eight for alpha = 0.667)
-template <int K>
-__device__ __forceinline__ void filter_diff(float rho, float ha, int m, float& dg, float& dg1)
-{
-    const float h = rho * ha / (float)m;
-    const float o = 0.28867513459481287f * h;    // h / (2 sqrt 3)
-    float s1 = 0.0f, s2 = 0.0f;
-    for (int k = 0; k < m; k++) {
-        const float c = fmaf((float)k + 0.5f, h, rho);
-        float a1, a2, b1, b2;
-        g_d1_d2_f32<K>(c - o, a1, a2);
-        g_d1_d2_f32<K>(c + o, b1, b2);
-        s1 += a1 + b1;
-        s2 += fmaf(c - o, a2, a1) + fmaf(c + o, b2, b1);
-    }
-    dg = 0.5f * h * s1;
-    dg1 = 0.5f * h * s2 / rho;
-}
-
-// Gauss-Legendre panels for the filter factor: the two-point rule's error per
-// panel ~ (h/m)^5, so m grows with ha = 1/alpha - 1
-inline int filter_panels(double ha) { return ha <= 0.0625 ? 1 : (int)std::ceil(ha * 16.0); }
 
 constexpr int DYN_THREADS = 128;
 constexpr int DYN_TILE = 128;
@@ -122,9 +65,9 @@ uj_filter_diff_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad
     const float3 to = make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz));
     const float skip = dyn_skip_s<K>();
 
-    double acc[12];
+    double acc[9];
 #pragma unroll
-    for (int k = 0; k < 12; k++) acc[k] = 0.0;
+    for (int k = 0; k < 9; k++) acc[k] = 0.0;
     for (int64_t base = 0; base < ns_pad; base += DYN_TILE) {
         __syncthreads();
         tile[threadIdx.x] = src[base + threadIdx.x];
@@ -140,9 +83,9 @@ uj_filter_diff_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad
         __syncwarp();
 #pragma unroll 1
         for (int sb = 0; sb < DYN_TILE; sb += 64) {
-            float f[12];
+            float f[9];
 #pragma unroll
-            for (int k = 0; k < 12; k++) f[k] = 0.0f;
+            for (int k = 0; k < 9; k++) f[k] = 0.0f;
 #pragma unroll 1
             for (int j0 = sb; j0 < sb + 64; j0 += 4) {
                 bool far = true;
@@ -161,43 +104,16 @@ uj_filter_diff_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad
                     const float ez = (th.z - s.a.z) + (tl.z - s.b.z);
                     const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
                     if (!(r2 > 0.0f)) continue;
-                    const float isig = s.b.w;
-                    const float rinv = rsqrtf(r2);
-                    const float rho = r2 * rinv * isig;
-                    float dg, dg1;
-                    filter_diff<K>(rho, ha, panels, dg, dg1);
-                    // Gamma * (-1/(4 pi)) from the pack (Winckelmans packs it over sigma^3)
-                    float gx = s.gam.x, gy = s.gam.y, gz = s.gam.z;
-                    if constexpr (!singular_tail<K>()) {
-                        const float sig3 = 1.0f / (isig * isig * isig);
-                        gx *= sig3; gy *= sig3; gz *= sig3;
-                    }
-                    const float ri2 = rinv * rinv, ri3 = ri2 * rinv;
-                    // c = -(dx x Gamma)/(4 pi r^3); dU = dg c; a = daux c with
-                    // daux = dg1 / (sigma r) - 3 dg / r^2; daux2 = -dg / (4 pi r^3)
-                    const float cx = ri3 * (ey * gz - ez * gy), cy = ri3 * (ez * gx - ex * gz), cz = ri3 * (ex * gy - ey * gx);
-                    const float daux = fmaf(dg1 * isig, rinv, -3.0f * dg * ri2);
-                    const float dax2 = dg * ri3;   // times -Gamma/(4 pi): the packed gam
-                    const float a1 = daux * cx, a2 = daux * cy, a3 = daux * cz;
-                    f[0] = fmaf(dg, cx, f[0]); f[1] = fmaf(dg, cy, f[1]); f[2] = fmaf(dg, cz, f[2]);
-                    f[3] = fmaf(a1, ex, f[3]);
-                    f[4] = fmaf(a2, ex, fmaf(-dax2, gz, f[4]));
-                    f[5] = fmaf(a3, ex, fmaf(dax2, gy, f[5]));
-                    f[6] = fmaf(a1, ey, fmaf(dax2, gz, f[6]));
-                    f[7] = fmaf(a2, ey, f[7]);
-                    f[8] = fmaf(a3, ey, fmaf(-dax2, gx, f[8]));
-                    f[9] = fmaf(a1, ez, fmaf(-dax2, gy, f[9]));
-                    f[10] = fmaf(a2, ez, fmaf(dax2, gx, f[10]));
-                    f[11] = fmaf(a3, ez, f[11]);
+                    filter_diff_pair<K>(ex, ey, ez, r2, s.b.w, s.gam, ha, panels, f);
                 }
             }
 #pragma unroll
-            for (int k = 0; k < 12; k++) acc[k] += (double)f[k];
+            for (int k = 0; k < 9; k++) acc[k] += (double)f[k];
         }
     }
     if (!valid) return;
 #pragma unroll
-    for (int k = 0; k < 9; k++) dJ[9 * (int64_t)idx + k] += acc[3 + k];
+    for (int k = 0; k < 9; k++) dJ[9 * (int64_t)idx + k] += acc[k];
 }
 
 template <int K>

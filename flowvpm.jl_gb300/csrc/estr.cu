@@ -16,6 +16,7 @@
 // r = 0 (the self pair, and coincident particles, whose J are equal so that
 // their reference term is zero; in the factored form their two terms would
 // only cancel to FP32 rounding, at the largest weight zeta(0)).
+#include "dyn_math.cuh"
 #include "internal.h"
 #include "vpm_math.cuh"
 
@@ -30,22 +31,6 @@ static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * 
 // bring it from ~1e-5 to ~2e-6 of max |SFS| on a smooth field.
 constexpr int ESTR_SUB = 8;
 
-// zeta~(r, alpha sigma) / zeta~(r, sigma) - 1 at s = (r/sigma)^2, zeta~(r, sigma) =
-// zeta(r/sigma)/sigma^3 (src/FLOWVPM_kernel.jl:45-84); fd = (alpha^-3 - 1, alpha^-3, alpha^-2 - 1)
-template <int K>
-__device__ __forceinline__ float zeta_ratio_m1(float s, float3 fd)
-{
-    if constexpr (K == K_GAUSERF) {          // zeta ~ e^{-rho^2/2}
-        return fmaf(fd.y, expm1f(-0.5f * s * fd.z), fd.x);
-    } else if constexpr (K == K_GAUS) {      // zeta ~ e^{-rho^3}
-        return fmaf(fd.y, expm1f(-s * sqrtf(s) * fd.x), fd.x);
-    } else if constexpr (K == K_WNKLMNS) {   // zeta ~ (rho^2 + 1)^-3.5
-        const float eps = s * fd.z / fmaf(s, 1.0f + fd.z, 1.0f);
-        return fmaf(fd.y, expm1f(3.5f * log1pf(-eps)), fd.x);
-    } else {
-        return 0.0f;
-    }
-}
 static_assert(UJ_BLOCK % ESTR_SUB == 0, "whole sub-blocks");
 
 size_t estr_src_pack_bytes(int64_t ns, int precision)

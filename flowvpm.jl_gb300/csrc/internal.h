@@ -78,6 +78,7 @@ struct LeafArgs {
     const uint8_t* static_flags;                              // [n] or null
     int kernel, precision;
     bool sfs, transposed;
+    bool uj = true;                                           // false: the Estr pass alone (J is input)
 };
 
 // Scratch and packing buffers supplied by the caller (the context).
@@ -185,5 +186,12 @@ cudaError_t near_groups(NearScratch& s, NearLists* L, cudaStream_t st, SyncFn sy
 constexpr int LEAF_SIZE_MAX = 4096;
 size_t leaf_work_bytes(int64_t n);
 cudaError_t launch_leaflist(const LeafArgs& a, const NearLists& L, void* work, cudaStream_t st, int64_t* launches);
+// zeta_fmm's near-field sum: W[n,3] += sum over the near lists of zeta(r/sigma_s)/sigma_s^3 Gamma_s.
+cudaError_t launch_leaf_zeta(const LeafArgs& a, const NearLists& L, double* W, void* work, cudaStream_t st,
+                             int64_t* launches);
+// The dynamic procedure's test-filter differences over the near lists (FP32-comp):
+// dJ, dSFS (+=, original order) from a.x, a.gam, a.sig, a.J and sig_a = alpha sig.
+cudaError_t launch_leaf_dynamic(const LeafArgs& a, const NearLists& L, double alpha, const double* sig_a, double* dJ,
+                                double* dSFS, void* work, cudaStream_t st, int64_t* launches);
 
 }  // namespace vpm

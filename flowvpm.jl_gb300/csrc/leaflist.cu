@@ -15,6 +15,7 @@
 // that of the all-pairs kernels (uj_pair.cuh for FP32-comp, the reference
 // formula for FP64); Estr uses the factored form of estr.cu with the self
 // pair excluded by position.
+#include "dyn_math.cuh"
 #include "internal.h"
 #include "uj_pair.cuh"
 #include "vpm_math.cuh"
@@ -25,6 +26,9 @@ constexpr int NF_WARPS = 4;                  // warp groups per block
 constexpr int NF_THREADS = 32 * NF_WARPS;
 constexpr int NF_BLK_TILES = 2;              // 32-source tiles summed in FP32 per block
 constexpr int NF_MID_BLKS = 4;               // blocks summed in FP32 before the FP64 add
+#ifndef VPM_NF_MIN_BLOCKS
+#define VPM_NF_MIN_BLOCKS 4                  // resident blocks per SM the UJ kernel is compiled for
+#endif
 
 __global__ void tgt_from_perm(int64_t n, const double* __restrict__ x, const int32_t* __restrict__ perm,
                               TgtPos* __restrict__ out)
@@ -74,7 +78,8 @@ __global__ void leaf_pack_f64(int64_t n, const double* __restrict__ x, const dou
     out[o] = p;
 }
 
-// Estr source payloads in Morton order (v = J^T Gamma or J Gamma, zero for static sources).
+// Estr source payloads in Morton order (v = J^T Gamma or J Gamma, zero for static sources;
+// Js = NULL: v = 0, the zeta sum's payload).
 template <int K>
 __global__ void leaf_pack_estr(int64_t n, const double* __restrict__ x, const double* __restrict__ gs,
                                const double* __restrict__ sgs, const double* __restrict__ Js,
@@ -86,12 +91,14 @@ __global__ void leaf_pack_estr(int64_t n, const double* __restrict__ x, const do
     const int64_t i = perm[o];
     const bool off = static_s && static_s[i];
     const double gx = gs[3 * i], gy = gs[3 * i + 1], gz = gs[3 * i + 2];
-    const double* J = Js + 9 * i;
-    double vx, vy, vz;
-    if (transposed) {
-        vx = J[0] * gx + J[1] * gy + J[2] * gz; vy = J[3] * gx + J[4] * gy + J[5] * gz; vz = J[6] * gx + J[7] * gy + J[8] * gz;
-    } else {
-        vx = J[0] * gx + J[3] * gy + J[6] * gz; vy = J[1] * gx + J[4] * gy + J[7] * gz; vz = J[2] * gx + J[5] * gy + J[8] * gz;
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    if (Js) {
+        const double* J = Js + 9 * i;
+        if (transposed) {
+            vx = J[0] * gx + J[1] * gy + J[2] * gz; vy = J[3] * gx + J[4] * gy + J[5] * gz; vz = J[6] * gx + J[7] * gy + J[8] * gz;
+        } else {
+            vx = J[0] * gx + J[3] * gy + J[6] * gz; vy = J[1] * gx + J[4] * gy + J[7] * gz; vz = J[2] * gx + J[5] * gy + J[8] * gz;
+        }
     }
     const double isig = 1.0 / sgs[i];
     if (precision) {
@@ -179,7 +186,7 @@ struct IntervalWalk {
 
 // ------------------------------------------------------------- UJ, FP32-comp
 template <int K>
-__global__ void __launch_bounds__(NF_THREADS)
+__global__ void __launch_bounds__(NF_THREADS, VPM_NF_MIN_BLOCKS)
 nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
             const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const SrcMixed* __restrict__ src,
             double* U, double* J)
@@ -234,7 +241,7 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
         __syncwarp();
         const int ng = (cnt + 3) >> 2;
         for (int q = 0; q < ng; q++)
-            pair4_mixed<K, true>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, me.bit);
+            pair4_mixed<K, true, false>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, me.bit);
         if (++tiles == NF_BLK_TILES) {
             tiles = 0;
 #pragma unroll
@@ -264,6 +271,91 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
     for (int k = 0; k < 3; k++) U[3 * (int64_t)me.idx + k] += dU[k];
 #pragma unroll
     for (int k = 0; k < 9; k++) J[9 * (int64_t)me.idx + k] += j9[k];
+}
+
+// ------------------------------------------- dynamic procedure, FP32-comp
+// dJ_t += the test-filter difference of every near pair's J term,
+// j(dx, Gamma_s, alpha sigma_s) - j(dx, Gamma_s, sigma_s), evaluated as a
+// difference (dynamic.cu) over the group's intervals; masked pairs and pairs
+// at r = 0 skipped, 4-source groups past the kernel's reach skipped warp-wide.
+template <int K>
+__global__ void __launch_bounds__(NF_THREADS)
+nf_filter_diff(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
+               const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const SrcMixed* __restrict__ src,
+               float ha, int panels, double* dJ)
+{
+    __shared__ SrcMixed tile[NF_WARPS][32];
+    __shared__ float4 off[NF_WARPS][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
+    if (grp >= ngroups) return;
+    const int64_t p0 = 32 * grp;
+    const GroupTarget me = group_target(n, p0, lane, tgt, leaf_of);
+    const TgtPos o = tgt[p0];
+    const float3 th = make_float3((float)me.tx, (float)me.ty, (float)me.tz);
+    const float3 tl = make_float3((float)(me.tx - (double)th.x), (float)(me.ty - (double)th.y),
+                                  (float)(me.tz - (double)th.z));
+    const float3 oh = make_float3((float)o.x, (float)o.y, (float)o.z);
+    const float3 ol = make_float3((float)(o.x - (double)oh.x), (float)(o.y - (double)oh.y), (float)(o.z - (double)oh.z));
+    const float3 to = make_float3((float)(me.tx - o.x), (float)(me.ty - o.y), (float)(me.tz - o.z));
+    const float skip = dyn_skip_s<K>();
+    double acc[9];
+    float f[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) { acc[k] = 0.0; f[k] = 0.f; }
+    int tiles = 0;
+    IntervalWalk walk;
+    walk.init(ivs, grp_row[grp], grp_row[grp + 1], lane);
+    for (;;) {
+        int sp;
+        unsigned smask;
+        const int cnt = walk.next(lane, sp, smask);
+        if (cnt == 0) break;
+        SrcMixed sj;
+        if (sp >= 0) {
+            sj = src[sp];
+        } else {   // padding: far away, no strength, no target
+            sj.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+            sj.b = make_float4(0.f, 0.f, 0.f, 1.f);
+            sj.gam = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        sj.gam.w = __uint_as_float(smask);
+        __syncwarp();
+        tile[warp][lane] = sj;
+        off[warp][lane] = make_float4((sj.a.x - oh.x) + (sj.b.x - ol.x), (sj.a.y - oh.y) + (sj.b.y - ol.y),
+                                      (sj.a.z - oh.z) + (sj.b.z - ol.z), sj.b.w * sj.b.w);
+        __syncwarp();
+        for (int j0 = 0; j0 < cnt; j0 += 4) {   // cnt <= 32: j0 + 3 stays in the tile
+            bool far = true;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float4 h = off[warp][j0 + q];
+                const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
+                const bool mine = (__float_as_uint(tile[warp][j0 + q].gam.w) & me.bit) != 0u;
+                far = far && (!mine || fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * h.w > skip);
+            }
+            if (__all_sync(0xffffffffu, far)) continue;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const SrcMixed& s = tile[warp][j0 + q];
+                if (!(__float_as_uint(s.gam.w) & me.bit)) continue;
+                const float ex = (th.x - s.a.x) + (tl.x - s.b.x);
+                const float ey = (th.y - s.a.y) + (tl.y - s.b.y);
+                const float ez = (th.z - s.a.z) + (tl.z - s.b.z);
+                const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                if (!(r2 > 0.0f)) continue;
+                filter_diff_pair<K>(ex, ey, ez, r2, s.b.w, s.gam, ha, panels, f);
+            }
+        }
+        if (++tiles == NF_BLK_TILES) {
+            tiles = 0;
+#pragma unroll
+            for (int k = 0; k < 9; k++) { acc[k] += (double)f[k]; f[k] = 0.f; }
+        }
+    }
+    if (!me.valid) return;
+#pragma unroll
+    for (int k = 0; k < 9; k++) dJ[9 * (int64_t)me.idx + k] += acc[k] + (double)f[k];
 }
 
 // --------------------------------------------------------------------- UJ, FP64
@@ -331,13 +423,20 @@ nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int3
 // SFS_t += J_t^T sum_s z_s g_s - sum_s z_s v_s  (z = zeta(r/sigma_s), g and v
 // pre-scaled by ZNORM / sigma_s^3 in the pack), over the group's intervals,
 // skipping the self pair (mixed: every pair at r = 0, as in estr.cu), for
-// non-static targets.
-template <int K, bool MIXED>
+// non-static targets.  With DZ (mixed only) each weight is the dynamic
+// procedure's weight difference zeta~(r, alpha sigma_s) - zeta~(r, sigma_s),
+// fd as in estr.cu.  With ZETA the kernel is zeta_fmm's near-field sum
+// (src/FLOWVPM_viscous.jl:523-556): SFS_t += sum_s z_s g_s over every target,
+// the self pair and static particles included (payload packed with Js = NULL).
+template <int K, bool MIXED, bool DZ = false, bool ZETA = false>
 __global__ void __launch_bounds__(NF_THREADS)
 nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
         const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const void* __restrict__ srcv,
-        const double* __restrict__ Jt, const uint8_t* __restrict__ static_t, bool transposed, double* SFS)
+        const double* __restrict__ Jt, const uint8_t* __restrict__ static_t, bool transposed, double* SFS,
+        float3 fd = make_float3(0.f, 0.f, 0.f))
 {
+    static_assert(MIXED || !DZ, "weight differences are FP32-comp only");
+    static_assert(!(DZ && ZETA), "one mode at a time");
     // mixed: per source (x_hi, 1/sigma^2), (x_lo), g, v;  FP64: the packed source
     __shared__ __align__(16) float4 mtile[MIXED ? NF_WARPS : 1][4][32];
     __shared__ SrcEstrF64 dtile[MIXED ? 1 : NF_WARPS][32];
@@ -348,7 +447,7 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
     if (grp >= ngroups) return;
     const int64_t p0 = 32 * grp;
     const GroupTarget me = group_target(n, p0, lane, tgt, leaf_of);
-    const bool live = me.valid && !(static_t && static_t[me.idx]);
+    const bool live = me.valid && (ZETA || !(static_t && static_t[me.idx]));
     const unsigned bit = live ? me.bit : 0u;
     const int tpos = (int)(p0 + lane);
     const float3 th = make_float3((float)me.tx, (float)me.ty, (float)me.tz);
@@ -393,11 +492,16 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
                     const float dz = (th.z - h.z) + (tl.z - l.z);
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     float z = zhat_f32<K>(r2 * h.w);
-                    const bool on = (tmask[warp][j] & bit) != 0u && r2 != 0.0f;   // pairs at r = 0 are skipped
+                    if constexpr (DZ) z *= zeta_ratio_m1<K>(r2 * h.w, fd);
+                    // pairs at r = 0 are skipped (ZETA: kept, the self pair included)
+                    const bool on = (tmask[warp][j] & bit) != 0u && (ZETA || r2 != 0.0f);
                     z = on ? z : 0.0f;
-                    const float4 g = mtile[warp][2][j], v = mtile[warp][3][j];
+                    const float4 g = mtile[warp][2][j];
                     fg[0] = fmaf(z, g.x, fg[0]); fg[1] = fmaf(z, g.y, fg[1]); fg[2] = fmaf(z, g.z, fg[2]);
-                    fv[0] = fmaf(z, v.x, fv[0]); fv[1] = fmaf(z, v.y, fv[1]); fv[2] = fmaf(z, v.z, fv[2]);
+                    if constexpr (!ZETA) {
+                        const float4 v = mtile[warp][3][j];
+                        fv[0] = fmaf(z, v.x, fv[0]); fv[1] = fmaf(z, v.y, fv[1]); fv[2] = fmaf(z, v.z, fv[2]);
+                    }
                 }
 #pragma unroll
                 for (int k = 0; k < 3; k++) { comp_add(sg[k], cg[k], fg[k]); comp_add(sv[k], cv[k], fv[k]); }
@@ -413,7 +517,7 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
             }
         } else {
             for (int j = 0; j < cnt; j++) {
-                if (!(tmask[warp][j] & bit) || spos[warp][j] == tpos) continue;
+                if (!(tmask[warp][j] & bit) || (!ZETA && spos[warp][j] == tpos)) continue;
                 const SrcEstrF64& p = dtile[warp][j];
                 const double dx = p.xy.x - me.tx, dy = p.xy.y - me.ty, dz = p.z_isig.x - me.tz;
                 const double isig = p.z_isig.y;
@@ -428,8 +532,13 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
         for (int k = 0; k < 3; k++) { zg[k] += (double)sg[k] + (double)cg[k]; zv[k] += (double)sv[k] + (double)cv[k]; }
     }
     if (!live) return;
-    const double* Jp = Jt + 9 * (int64_t)me.idx;
     double o[3];
+    if constexpr (ZETA) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) SFS[3 * (int64_t)me.idx + k] += zg[k];
+        return;
+    }
+    const double* Jp = Jt + 9 * (int64_t)me.idx;
     if (transposed) {
         o[0] = Jp[0] * zg[0] + Jp[1] * zg[1] + Jp[2] * zg[2] - zv[0];
         o[1] = Jp[3] * zg[0] + Jp[4] * zg[1] + Jp[5] * zg[2] - zv[1];
@@ -463,16 +572,18 @@ static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* wo
     const unsigned g = (unsigned)((n + 255) / 256);
     const unsigned gb = (unsigned)((L.ngroups + NF_WARPS - 1) / NF_WARPS);
     tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
-    if (a.precision) {
+    *launches += 1;
+    if (a.uj && a.precision) {
         leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
         nf_uj_mixed<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
                                                   (const SrcMixed*)src, a.U, a.J);
-    } else {
+        *launches += 2;
+    } else if (a.uj) {
         leaf_pack_f64<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcF64*)src);
         nf_uj_f64<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
                                                 (const SrcF64*)src, a.U, a.J);
+        *launches += 2;
     }
-    *launches += 3;
     if (a.sfs) {
         leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm,
                                               a.precision, src);
@@ -485,6 +596,93 @@ static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* wo
         *launches += 2;
     }
     return cudaGetLastError();
+}
+
+// The dynamic procedure's differences over the near lists, FP32-comp:
+// dJ = the filter difference of J; dSFS = the weight-difference Estr at J plus
+// the Estr of dJ at alpha sigma (sig_a); a.J is J, a.sfs and a.U unused.
+template <int K>
+static cudaError_t launch_leaf_dyn_k(const LeafArgs& a, const NearLists& L, double alpha, const double* sig_a,
+                                     double* dJ, double* dSFS, void* work, cudaStream_t st, int64_t* launches)
+{
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const int64_t n = a.n;
+    char* p = (char*)work;
+    TgtPos* tgt = (TgtPos*)p;            p += al(n * sizeof(TgtPos));
+    void* src = p;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    const unsigned gb = (unsigned)((L.ngroups + NF_WARPS - 1) / NF_WARPS);
+    const double ha = 1.0 / alpha - 1.0;
+    tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
+    *launches += 1;
+    if constexpr (K != K_SING) {   // g = 1 has no sigma dependence: dJ = 0
+        leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
+        nf_filter_diff<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                     (const SrcMixed*)src, (float)ha, filter_panels(ha), dJ);
+        *launches += 2;
+    }
+    const float3 fd = make_float3((float)(1.0 / (alpha * alpha * alpha) - 1.0), (float)(1.0 / (alpha * alpha * alpha)),
+                                  (float)(1.0 / (alpha * alpha) - 1.0));
+    leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm, 1, src);
+    nf_estr<K, true, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
+                                                      a.static_flags, a.transposed, dSFS, fd);
+    leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, sig_a, dJ, a.static_flags, a.transposed, L.perm, 1, src);
+    nf_estr<K, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, dJ,
+                                                a.static_flags, a.transposed, dSFS);
+    *launches += 4;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_dynamic(const LeafArgs& a, const NearLists& L, double alpha, const double* sig_a, double* dJ,
+                                double* dSFS, void* work, cudaStream_t st, int64_t* launches)
+{
+    if (a.n <= 0) return cudaSuccess;
+    if (!a.precision) return cudaErrorInvalidValue;   // FP32-comp only
+    switch (a.kernel) {
+    case K_SING: return launch_leaf_dyn_k<K_SING>(a, L, alpha, sig_a, dJ, dSFS, work, st, launches);
+    case K_GAUS: return launch_leaf_dyn_k<K_GAUS>(a, L, alpha, sig_a, dJ, dSFS, work, st, launches);
+    case K_GAUSERF: return launch_leaf_dyn_k<K_GAUSERF>(a, L, alpha, sig_a, dJ, dSFS, work, st, launches);
+    case K_WNKLMNS: return launch_leaf_dyn_k<K_WNKLMNS>(a, L, alpha, sig_a, dJ, dSFS, work, st, launches);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// zeta_fmm's near-field sum: W += sum over the near lists of zeta(r/sigma_s)/sigma_s^3 Gamma_s
+// (a.x, a.gam, a.sig; every particle a target, the self pair included).
+template <int K>
+static cudaError_t launch_leaf_zeta_k(const LeafArgs& a, const NearLists& L, double* W, void* work, cudaStream_t st,
+                                      int64_t* launches)
+{
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const int64_t n = a.n;
+    char* p = (char*)work;
+    TgtPos* tgt = (TgtPos*)p;            p += al(n * sizeof(TgtPos));
+    void* src = p;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    const unsigned gb = (unsigned)((L.ngroups + NF_WARPS - 1) / NF_WARPS);
+    tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
+    leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, nullptr, nullptr, true, L.perm, a.precision, src);
+    if (a.precision)
+        nf_estr<K, true, false, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src,
+                                                                 nullptr, nullptr, true, W);
+    else
+        nf_estr<K, false, false, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src,
+                                                                  nullptr, nullptr, true, W);
+    *launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_zeta(const LeafArgs& a, const NearLists& L, double* W, void* work, cudaStream_t st,
+                             int64_t* launches)
+{
+    if (a.n <= 0) return cudaSuccess;
+    switch (a.kernel) {
+    case K_SING: return launch_leaf_zeta_k<K_SING>(a, L, W, work, st, launches);
+    case K_GAUS: return launch_leaf_zeta_k<K_GAUS>(a, L, W, work, st, launches);
+    case K_GAUSERF: return launch_leaf_zeta_k<K_GAUSERF>(a, L, W, work, st, launches);
+    case K_WNKLMNS: return launch_leaf_zeta_k<K_WNKLMNS>(a, L, W, work, st, launches);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_leaflist(const LeafArgs& a, const NearLists& L, void* work, cudaStream_t st, int64_t* launches)

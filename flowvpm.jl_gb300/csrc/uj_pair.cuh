@@ -44,25 +44,34 @@ __device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float G
 //   mybit   : with MASK, this lane's bit in each source's target mask (the bits
 //             of gam.w): a source whose mask lacks it contributes nothing (every
 //             lane still votes and computes)
-template <int K, bool MASK = false>
+//   VOTE    : false skips the far vote and takes the near form for every group
+//             (the near-field lists, whose pairs are almost all within reach),
+//             four pairs at a time with the form chosen warp-wide (near_GQ4)
+//             and no singular branch; off[].w (1/sigma^2 for Winckelmans) is
+//             still read
+template <int K, bool MASK = false, bool VOTE = true>
 __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, const float3& tl, float r2n,
                                             const float4* __restrict__ off, const SrcMixed* __restrict__ tile,
                                             int j0, float (&u)[3], float (&jq)[8], float (&w)[3],
                                             unsigned mybit = 0u)
 {
     float dx[4], dy[4], dz[4], r2[4], hw[4];
-    bool far = true;
+    bool far = VOTE;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        const float4 h = off[j0 + q];
-        dx[q] = to.x - h.x;
-        dy[q] = to.y - h.y;
-        dz[q] = to.z - h.z;
-        r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
-        hw[q] = h.w;
-        far = far && (r2[q] > (singular_tail<K>() ? h.w : r2n));
+        if constexpr (VOTE || !singular_tail<K>()) {
+            const float4 h = off[j0 + q];
+            hw[q] = h.w;
+            if constexpr (VOTE) {
+                dx[q] = to.x - h.x;
+                dy[q] = to.y - h.y;
+                dz[q] = to.z - h.z;
+                r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
+                far = far && (r2[q] > (singular_tail<K>() ? h.w : r2n));
+            }
+        }
     }
-    if (__all_sync(0xffffffffu, far)) {
+    if (VOTE && __all_sync(0xffffffffu, far)) {
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             float G, Q;
@@ -82,7 +91,9 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             }
             accum_pair(dx[q], dy[q], dz[q], G, Q, gq, u, jq, w);
         }
-    } else {
+    } else if constexpr (VOTE) {
+        // near groups of the all-pairs kernels: per pair (their register budget
+        // does not hold four pairs' near-form intermediates)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const float4 a = tile[j0 + q].a, b = tile[j0 + q].b;
@@ -110,6 +121,35 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
                 Q = on ? Q : 0.0f;
             }
             accum_pair(ex, ey, ez, G, Q, gq, u, jq, w);
+        }
+    } else {
+        // every group (the near-field lists): the four pairs' forms chosen warp-wide
+        float ex[4], ey[4], ez[4], e2[4], s4[4], i2[4], G[4], Q[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float4 a = tile[j0 + q].a, b = tile[j0 + q].b;
+            ex[q] = (th.x - a.x) + (tl.x - b.x);
+            ey[q] = (th.y - a.y) + (tl.y - b.y);
+            ez[q] = (th.z - a.z) + (tl.z - b.z);
+            e2[q] = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+            i2[q] = singular_tail<K>() ? b.w * b.w : hw[q];
+            s4[q] = e2[q] * i2[q];
+        }
+        near_GQ4<K, false>(s4, i2, G, Q);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float g = G[q], qq = Q[q];
+            if constexpr (singular_tail<K>()) {
+                const float isig3 = i2[q] * tile[j0 + q].b.w;
+                g *= isig3;
+                qq *= isig3;
+            }
+            const float4 gq = tile[j0 + q].gam;
+            bool on = e2[q] > 0.0f;
+            if constexpr (MASK) on = on && (__float_as_uint(gq.w) & mybit) != 0u;
+            g = on ? g : 0.0f;
+            qq = on ? qq : 0.0f;
+            accum_pair(ex[q], ey[q], ez[q], g, qq, gq, u, jq, w);
         }
     }
 }

@@ -80,42 +80,10 @@ __device__ __forceinline__ double zeta_f64(double rho)
 
 // ------------------------------------------------------------------ FP32
 constexpr float F_C2 = 0.7978845608028654f;
-constexpr float S_SERIES = 2.0f;      // Taylor series below this s (Gaussian-erf)
+constexpr float F_C4 = 0.07957747154594767f;   // 1/(4 pi)
+constexpr float S_SERIES = 2.0f;      // positive series below this s (Gaussian-erf, gerf_GQ)
 constexpr float S_FAR_GERF = 50.0f;   // singular form above this s (rho > 7.07)
 constexpr float S_FAR_GAUS = 8.0f;    // singular form above this s (rho^3 > 22.6)
-
-// Taylor coefficients of G(s) = sqrt(2/pi) sum (-1/2)^k s^k / (k! (2k+3))
-// and H(s) = -sqrt(2/pi) sum (-1/2)^k s^k / (k! (2k+5)).
-__device__ __forceinline__ float gerf_G_series(float s)
-{
-    float p = 9.335750486555003e-12f;
-    p = fmaf(p, s, -2.0449739161025244e-10f);
-    p = fmaf(p, s, 4.0684217909829174e-09f);
-    p = fmaf(p, s, -7.275295437992981e-08f);
-    p = fmaf(p, s, 1.1543468761615528e-06f);
-    p = fmaf(p, s, -1.5983264439159964e-05f);
-    p = fmaf(p, s, 0.00018889312519007232f);
-    p = fmaf(p, s, -0.0018469550018584847f);
-    p = fmaf(p, s, 0.014247938585765453f);
-    p = fmaf(p, s, -0.07978845608028655f);
-    p = fmaf(p, s, 0.26596152026762176f);
-    return p;
-}
-__device__ __forceinline__ float gerf_H_series(float s)
-{
-    float p = -8.588890447630603e-12f;
-    p = fmaf(p, s, 1.8671500973110005e-10f);
-    p = fmaf(p, s, -3.680953048984544e-09f);
-    p = fmaf(p, s, 6.509474865572668e-08f);
-    p = fmaf(p, s, -1.0185413613190173e-06f);
-    p = fmaf(p, s, 1.3852162513938635e-05f);
-    p = fmaf(p, s, -0.00015983264439159965f);
-    p = fmaf(p, s, 0.0015111450015205786f);
-    p = fmaf(p, s, -0.011081730011150908f);
-    p = fmaf(p, s, 0.056991754343061814f);
-    p = fmaf(p, s, -0.1595769121605731f);
-    return p;
-}
 
 // Gaussian kernel, t = rho^3: G = (1 - e^-t)/t = sum (-t)^k/(k+1)!,
 // H = 3 rho sum_{k>=2} (-1)^(k+1) (k-1)/k! t^(k-2).
@@ -175,8 +143,116 @@ __device__ __forceinline__ void far_GQ(float s, float isig2, float& G, float& Q)
     Q = G * (rs2 * isig2);
 }
 
-// Full form of kernel K for one lane (any s > 0).
-template <int K>
+// G = g/rho^3 of Gaussian-erf for s >= 2 from the erfcx fit, given e = e^{-s/2}, rs = s^-1/2
+__device__ __forceinline__ float gerf_G_erfcx(float s, float e, float rs)
+{
+    const float rho = s * rs;
+    const float t = __fdividef(1.0f, fmaf(0.5f, fminf(rho, 10.0f), 1.0f));
+    const float w = fmaf(4.77190564267067f, t, -1.795317607111778f);
+    float p = -5.1560079373370265e-06f;
+    p = fmaf(p, w, 5.998428003101994e-06f);
+    p = fmaf(p, w, 0.00010125038777505872f);
+    p = fmaf(p, w, -0.00030713426402493693f);
+    p = fmaf(p, w, -0.0023330098304451836f);
+    p = fmaf(p, w, 0.009623567049071946f);
+    p = fmaf(p, w, 0.13016216050000662f);
+    p = fmaf(p, w, 0.5926831417002281f);
+    const float h = fmaf(F_C2, rho, p * t);
+    return fmaf(-e, h, 1.0f) * rs * (rs * rs);
+}
+
+// Gaussian-erf G and Q = -H/(3 sigma^2) of one lane at any s >= 0, with
+// e = e^{-s/2} (coefficients from fit_gerf.py):
+//   s < 2:  G = c2 e (1/3 + s S2(s)), -H/3 = c2 e S2(s), S2(s) = sum_m s^m/(2m+5)!!
+//           (Kummer's series of erf: positive terms, no cancellation);
+//   s >= 2: g = 1 - e (erfcx(rho/sqrt2) + c2 rho) with erfcx(rho/sqrt2) = P(w) t,
+//           t = 1/(1 + rho/2), w = A t + B, P of degree 7 (rho capped at 10, beyond
+//           which e < 2e-22 and G is its singular form s^-1.5); G = g/rho^3,
+//           -H/3 = (G - c2 e/3)/s.
+// No erf call.  FAR adds a third branch, the singular form beyond s = 50, for
+// callers whose near groups hold many lanes past the kernel's reach (the
+// all-pairs kernels); without it those lanes take the s >= 2 form, which is
+// valid there.
+template <bool FAR>
+__device__ __forceinline__ void gerf_GQ(float s, float isig2, float& G, float& Q)
+{
+    if (FAR && s > S_FAR_GERF) {
+        far_GQ(s, isig2, G, Q);
+        return;
+    }
+    const float e = exp2f(s * -0.72134752044448170f);
+    if (s < S_SERIES) {
+        float p = 3.1622138893727926e-12f;
+        p = fmaf(p, s, 7.273091945557423e-11f);
+        p = fmaf(p, s, 1.5273493085670588e-09f);
+        p = fmaf(p, s, 2.901963686277412e-08f);
+        p = fmaf(p, s, 4.9333382666716e-07f);
+        p = fmaf(p, s, 7.4000074000074e-06f);
+        p = fmaf(p, s, 9.62000962000962e-05f);
+        p = fmaf(p, s, 0.0010582010582010583f);
+        p = fmaf(p, s, 0.009523809523809525f);
+        p = fmaf(p, s, 0.06666666666666667f);
+        const float ce = F_C2 * e;
+        G = ce * fmaf(s, p, 0.33333333333333333f);
+        Q = ce * p * isig2;
+    } else {
+        const float rs = rsqrtf(s);
+        const float rs2 = rs * rs;
+        G = gerf_G_erfcx(s, e, rs);
+        Q = fmaf(F_C2 * -0.33333333333333333f, e, G) * rs2 * isig2;
+    }
+}
+
+// gerf_GQ for four pairs of one lane, with the choice of forms made for the
+// whole warp so that the four pairs' chains interleave: every lane past s = 50
+// (FAR only): the singular form; otherwise the s >= 2 form for all four (valid
+// at any s > 0), replaced by the series, per pair, where s < 2 when any lane
+// of the warp has such a pair.  All 32 lanes must call it.
+template <bool FAR>
+__device__ __forceinline__ void gerf_GQ4(const float (&s)[4], const float (&isig2)[4], float (&G)[4], float (&Q)[4])
+{
+    bool allfar = FAR, anyser = false;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        allfar = allfar && s[q] > S_FAR_GERF;
+        anyser = anyser || s[q] < S_SERIES;
+    }
+    if (FAR && __all_sync(0xffffffffu, allfar)) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) far_GQ(s[q], isig2[q], G[q], Q[q]);
+        return;
+    }
+    float e[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        e[q] = exp2f(s[q] * -0.72134752044448170f);
+        const float rs = rsqrtf(s[q]);
+        G[q] = gerf_G_erfcx(s[q], e[q], rs);
+        Q[q] = fmaf(F_C2 * -0.33333333333333333f, e[q], G[q]) * (rs * rs) * isig2[q];
+    }
+    if (__any_sync(0xffffffffu, anyser)) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float p = 3.1622138893727926e-12f;
+            p = fmaf(p, s[q], 7.273091945557423e-11f);
+            p = fmaf(p, s[q], 1.5273493085670588e-09f);
+            p = fmaf(p, s[q], 2.901963686277412e-08f);
+            p = fmaf(p, s[q], 4.9333382666716e-07f);
+            p = fmaf(p, s[q], 7.4000074000074e-06f);
+            p = fmaf(p, s[q], 9.62000962000962e-05f);
+            p = fmaf(p, s[q], 0.0010582010582010583f);
+            p = fmaf(p, s[q], 0.009523809523809525f);
+            p = fmaf(p, s[q], 0.06666666666666667f);
+            const float ce = F_C2 * e[q];
+            const bool ser = s[q] < S_SERIES;
+            G[q] = ser ? ce * fmaf(s[q], p, 0.33333333333333333f) : G[q];
+            Q[q] = ser ? ce * p * isig2[q] : Q[q];
+        }
+    }
+}
+
+// Full form of kernel K for one lane (any s > 0); FAR as in gerf_GQ.
+template <int K, bool FAR = true>
 __device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q)
 {
     if constexpr (K == K_WNKLMNS) {
@@ -189,20 +265,7 @@ __device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q
     } else if constexpr (K == K_SING) {
         far_GQ(s, isig2, G, Q);
     } else if constexpr (K == K_GAUSERF) {
-        if (s > S_FAR_GERF) {
-            far_GQ(s, isig2, G, Q);
-        } else if (s < S_SERIES) {
-            G = gerf_G_series(s);
-            Q = gerf_H_series(s) * (isig2 * -0.33333333333333333f);
-        } else {
-            const float rs = rsqrtf(s);
-            const float rs2 = rs * rs;
-            const float rho = s * rs;
-            const float e = expf(-0.5f * s);
-            const float g = erff(rho * 0.70710678118654752f) - F_C2 * rho * e;
-            G = g * rs * rs2;
-            Q = fmaf(F_C2 * -0.33333333333333333f, e, G) * rs2 * isig2;   // -H/3 = (G - c2 e / 3)/s
-        }
+        gerf_GQ<FAR>(s, isig2, G, Q);
     } else {  // Gaussian
         if (s > S_FAR_GAUS) {
             far_GQ(s, isig2, G, Q);
@@ -220,6 +283,18 @@ __device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q
                 Q = fmaf(-t, e, 1.0f - e) * rs2 * rs2 * rs * isig2;   // -H/3 = (1 - e - t e)/rho^5
             }
         }
+    }
+}
+
+// near_GQ for four pairs of one lane; all 32 lanes must call it.
+template <int K, bool FAR = true>
+__device__ __forceinline__ void near_GQ4(const float (&s)[4], const float (&isig2)[4], float (&G)[4], float (&Q)[4])
+{
+    if constexpr (K == K_GAUSERF) {
+        gerf_GQ4<FAR>(s, isig2, G, Q);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) near_GQ<K, FAR>(s[q], isig2[q], G[q], Q[q]);
     }
 }
 

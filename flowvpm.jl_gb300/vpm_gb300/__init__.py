@@ -16,7 +16,7 @@ from .timeintegration import (AfterUJ, BeforeUJ, ConstantSFS, CoreSpreading, Dyn
                               clipping_backscatter, correctedpedrizzetti, isSFSenabled, noSFS,
                               norelaxation, pedrizzetti, rbf_conjugategradient, rungekutta3, run_vpm,
                               update_particle_states)
-from .uj import UJ_gb300, UJ_gb300_cross, UJ_gb300_mixed, zeta_gb300, zeta_gb300_mixed
+from .uj import UJ_gb300, UJ_gb300_cross, UJ_gb300_mixed, zeta_fmm_gb300, zeta_gb300, zeta_gb300_mixed
 from . import rings
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -52,6 +52,9 @@ SIGNATURES = {
     "vpm_zeta": (_int, [_vp, _vp, _i64, _i64, _int, _int]),
     "vpm_dynamic_diff_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _int, _int]),
     "vpm_zeta_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _int, _int]),
+    "vpm_zeta_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _vp]),
+    "vpm_dynamic_diff_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _dbl, _int,
+                                             _int, _int, _vp]),
     "vpm_p2p_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int,
                                     _vp]),
     "vpm_p2p_lists_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp,
@@ -199,6 +202,33 @@ class Context:
         self._check(self._L.vpm_dynamic_diff_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(J),
                                                  float(alpha), _ptr(dJ), _ptr(dSFS), int(kernel), int(precision),
                                                  TRANSPOSED if transposed else 0))
+
+    def zeta_leaflist_dev(self, x, gam, sig, W, *, leaf_size: int = 64, theta: float = 0.4,
+                          kernel: int = KERNEL_GAUSSIANERF, precision: int = FP64):
+        """zeta_fmm's near-field sum, W[n,3] += (CUDA float64 tensors); returns
+        (leaves, leaf pairs, particle pairs)."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(W, 3)
+        self._torch_stream()
+        stats = np.zeros(3, dtype=np.int64)
+        self._check(self._L.vpm_zeta_leaflist_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(W),
+                                                  int(leaf_size), float(theta), int(kernel), int(precision),
+                                                  stats.ctypes.data))
+        return tuple(int(v) for v in stats)
+
+    def dynamic_diff_leaflist_dev(self, x, gam, sig, J, alpha: float, dJ, dSFS, *, leaf_size: int = 64,
+                                  theta: float = 0.4, kernel: int = KERNEL_GAUSSIANERF, precision: int = FP32COMP,
+                                  transposed: bool = True, static=None):
+        """dynamic_diff_dev over the near field of p2p_leaflist_dev (same leaf_size, theta; J the
+        near-field J at sigma); dJ, dSFS set.  Returns (leaves, leaf pairs, particle pairs)."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(J, 9); _check_dev(dJ, 9)
+        _check_dev(dSFS, 3)
+        self._torch_stream()
+        stats = np.zeros(3, dtype=np.int64)
+        self._check(self._L.vpm_dynamic_diff_leaflist_dev(
+            self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(static), _ptr(J), float(alpha), _ptr(dJ),
+            _ptr(dSFS), int(leaf_size), float(theta), int(kernel), int(precision),
+            TRANSPOSED if transposed else 0, stats.ctypes.data))
+        return tuple(int(v) for v in stats)
 
     def uj_cross(self, src: np.ndarray, ns: int, tgt: np.ndarray, nt: int, kernel: int, precision: int):
         for m in (src, tgt):

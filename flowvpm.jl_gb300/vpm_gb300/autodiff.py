@@ -2,7 +2,7 @@
 
 `UJFunction` is the torch.autograd.Function over the two C entry points
 `vpm_uj_dev` (forward) and `vpm_uj_adjoint_dev` (backward, the hand-written
-FP64 adjoint kernel).  It plays the role of the ChainRulesCore `rrule` that
+adjoint kernel, in the forward's precision).  It plays the role of the ChainRulesCore `rrule` that
 src/FLOWVPM_rrules.jl:179-330 sketches but never wires in; a Julia binding
 would wrap the same two calls in an rrule.
 
@@ -41,6 +41,7 @@ class UJFunction(torch.autograd.Function):
         vctx.uj_dev(x, x, gam, sig, U, J, kernel, precision)
         ctx.save_for_backward(x, gam, sig)
         ctx.kernel = kernel
+        ctx.precision = precision
         ctx.vctx = vctx
         return U, J
 
@@ -53,7 +54,9 @@ class UJFunction(torch.autograd.Function):
         xb = torch.zeros_like(x)
         gb = torch.zeros_like(gam)
         sb = torch.zeros_like(sig)
-        ctx.vctx.uj_adjoint_dev(x, gam, sig, Ubar, Jbar, xb, gb, sb, ctx.kernel, _lib.FP64)
+        # the adjoint in the forward's precision (the FP32-comp adjoint covers all kernels but the Gaussian)
+        prec = _lib.FP64 if ctx.kernel == _lib.KERNEL_GAUSSIAN else getattr(ctx, "precision", _lib.FP64)
+        ctx.vctx.uj_adjoint_dev(x, gam, sig, Ubar, Jbar, xb, gb, sb, ctx.kernel, prec)
         return xb, gb, sb, None, None, None
 
 
@@ -74,16 +77,17 @@ class _KeptUJ(torch.autograd.Function):
     inputs; its backward is the adjoint kernel, as for UJFunction."""
 
     @staticmethod
-    def forward(ctx, x, gam, sig, U, J, kernel: int, vctx: _lib.Context):
+    def forward(ctx, x, gam, sig, U, J, kernel: int, precision: int, vctx: _lib.Context):
         ctx.save_for_backward(x, gam, sig)
         ctx.kernel = kernel
+        ctx.precision = precision
         ctx.vctx = vctx
         return U.clone(), J.clone()
 
     @staticmethod
     def backward(ctx, Ubar, Jbar):
         xb, gb, sb, *_ = UJFunction.backward(ctx, Ubar, Jbar)
-        return xb, gb, sb, None, None, None, None
+        return xb, gb, sb, None, None, None, None, None
 
 
 def _uj_default(x, gam, sig, kernel, precision, vctx):
@@ -148,7 +152,7 @@ class _StepKeepUJ(torch.autograd.Function):
 
         def replay(x_, g_, s_, kernel, precision, vctx):
             U, J = next(kept)
-            return _KeptUJ.apply(x_, g_, s_, U, J, kernel, vctx)
+            return _KeptUJ.apply(x_, g_, s_, U, J, kernel, precision, vctx)
         with torch.enable_grad():
             out = rk3_step(x, gam, sig, ctx.dt, uj_fn=replay, **ctx.kw)
         grads = [gx, gg, gs]

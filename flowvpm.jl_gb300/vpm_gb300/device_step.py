@@ -88,7 +88,8 @@ class DynamicSFSParams:
     """DynamicSFS settings; defaults = SFS_Cd_twolevel_nobackscatter (src/FLOWVPM.jl:223).
 
     fused: with FP32-comp pair sums, take the test-filter differences from
-    vpm_dynamic_diff_dev (evaluated as differences, FP32 relative accuracy)
+    vpm_dynamic_diff_dev, or vpm_dynamic_diff_leaflist_dev for a near-field
+    state (evaluated as differences, FP32 relative accuracy)
     instead of subtracting two separate evaluations (the reference's way,
     whose FP32 rounding the 1e-3 differences amplify to 1e-4 .. 1e-2)."""
     alpha: float = 0.999
@@ -113,9 +114,17 @@ class CoreSpreadingParams:
 
 
 def zeta(fld: DeviceField, ctx: _lib.Context) -> torch.Tensor:
-    """zeta_direct: W[n,3] = sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s (self pair included)."""
+    """zeta_direct: W[n,3] = sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s (self pair included);
+    for a near-field state, zeta_fmm's sum over the near leaf pairs, into a zeroed W
+    (the reference's zeta_fmm adds to J[1:3] without zeroing them; the conjugate
+    gradient here takes each evaluation on its own, as with zeta_direct)."""
     W = torch.zeros_like(fld.gam)
-    ctx.zeta_dev(fld.x, fld.x, fld.gam, fld.sig, W, fld.kernel, fld.precision)
+    if fld.leaflist is None:
+        ctx.zeta_dev(fld.x, fld.x, fld.gam, fld.sig, W, fld.kernel, fld.precision)
+    else:
+        leaf_size, theta = fld.leaflist
+        ctx.zeta_leaflist_dev(fld.x, fld.gam, fld.sig, W, leaf_size=leaf_size, theta=theta, kernel=fld.kernel,
+                              precision=fld.precision)
     return W
 
 
@@ -172,8 +181,14 @@ def _dynamic_fused(fld, ctx, p: DynamicSFSParams):
     evaluated differences (after the stage's own UJ + Estr at sigma)."""
     dJ = torch.zeros_like(fld.J)
     dS = torch.zeros_like(fld.SFS)
-    ctx.dynamic_diff_dev(fld.x, fld.gam, fld.sig, fld.J, p.alpha, dJ, dS, fld.kernel, fld.precision,
-                         fld.transposed)
+    if fld.leaflist is None:
+        ctx.dynamic_diff_dev(fld.x, fld.gam, fld.sig, fld.J, p.alpha, dJ, dS, fld.kernel, fld.precision,
+                             fld.transposed)
+    else:
+        leaf_size, theta = fld.leaflist
+        ctx.dynamic_diff_leaflist_dev(fld.x, fld.gam, fld.sig, fld.J, p.alpha, dJ, dS, leaf_size=leaf_size,
+                                      theta=theta, kernel=fld.kernel, precision=fld.precision,
+                                      transposed=fld.transposed)
     fld.M.zero_()
     fld.M[:, 0:3] = _stretch(dJ, fld.gam, fld.transposed)
     fld.M[:, 3:6] = dS
@@ -221,7 +236,7 @@ def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSP
     f, g = fld.f, fld.g
     Uinf = torch.tensor(Uinf, dtype=torch.float64, device=fld.x.device)
     fld.M.zero_()
-    fused = sfs is not None and sfs.fused and fld.precision == _lib.FP32COMP and fld.leaflist is None
+    fused = sfs is not None and sfs.fused and fld.precision == _lib.FP32COMP
     for a, b in STAGES:
         first = (a == 1 or a == 0)
         if sfs is not None and first and not fused:

@@ -71,3 +71,25 @@ def zeta_gb300_mixed(pfield: ParticleField, *, ctx: _lib.Context | None = None) 
     """zeta_direct on the GB300 with FP32 pair math and FP64 block reduction."""
     c = ctx if ctx is not None else _lib.default_context()
     c.zeta(pfield.particles, pfield.np, _kernel_id(pfield), _lib.FP32COMP)
+
+
+def zeta_fmm_gb300(pfield: ParticleField, *, leaf_size: int = 64, theta: float = 0.4,
+                   precision: int = _lib.FP64, ctx: _lib.Context | None = None) -> None:
+    """zeta_fmm(pfield) (src/FLOWVPM_viscous.jl:523-556) on the GB300: rows 16:18
+    (J[1:3]) of every particle, statics included, += the basis field summed over
+    the near leaf pairs of the octree (leaf_size and theta play the parts of
+    pfield.fmm.ncrit and .theta; the far field is neglected, as in the
+    reference).  Like the reference it adds without zeroing the rows first;
+    zeta_direct (zeta_gb300) sets them."""
+    import numpy as np
+    import torch
+    c = ctx if ctx is not None else _lib.default_context()
+    n = pfield.np
+    if n == 0:
+        return
+    P = pfield.particles
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    W = d(P[15:18, :n].T)
+    c.zeta_leaflist_dev(d(P[0:3, :n].T), d(P[3:6, :n].T), d(P[6, :n]), W, leaf_size=leaf_size, theta=theta,
+                        kernel=_kernel_id(pfield), precision=precision)
+    P[15:18, :n] = W.cpu().numpy().T

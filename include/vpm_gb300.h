@@ -207,6 +207,30 @@ int vpm_p2p_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double*
                          int leaf_size, double theta, int kernel, int precision, int flags,
                          int64_t* stats);
 
+/* zeta_fmm(pfield) (src/FLOWVPM_viscous.jl:523-556): the RBF basis field over
+ * the near field only (the reference's zeta_fmm evaluates FastMultipole's
+ * direct_list and neglects the far field): W[n,3] += sum over the near leaf
+ * pairs of vpm_p2p_leaflist_dev (same leaf_size, theta) of
+ * zeta(r/sigma_s)/sigma_s^3 Gamma_s, every particle a target and the self pair
+ * included.  Like the reference's loop it adds to W (the reference adds into
+ * J[1:3] without zeroing them, unlike zeta_direct).  Device pointers; stats as
+ * vpm_p2p_leaflist_dev. */
+int vpm_zeta_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                          double* W, int leaf_size, double theta, int kernel, int precision, int64_t* stats);
+
+/* vpm_dynamic_diff_dev over the near field only: the differences of the two
+ * evaluations of the near-field leg (vpm_p2p_leaflist_dev with VPM_SFS, same
+ * leaf_size and theta) at core sizes alpha sigma and sigma, as the dynamic
+ * procedure (src/FLOWVPM_subfilterscale.jl:447-673) takes them when UJ is
+ * UJ_fmm.  J is the near-field J at sigma; dJ[n,9] and dSFS[n,3] are set.
+ * Static particles (static_flags, may be NULL) get no SFS, as in
+ * vpm_p2p_leaflist_dev.  stats as there.  FP64 evaluates and subtracts;
+ * FP32COMP evaluates the differences directly. */
+int vpm_dynamic_diff_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                                  const uint8_t* static_flags, const double* J, double alpha, double* dJ,
+                                  double* dSFS, int leaf_size, double theta, int kernel, int precision, int flags,
+                                  int64_t* stats);
+
 /* The same near-field P2P over leaf-pair lists the caller supplies in host
  * memory (for instance FastMultipole's direct_list of the reference's own
  * tree): particle perm[p] is at tree position p (perm a permutation of

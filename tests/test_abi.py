@@ -94,13 +94,106 @@ def _gerf_exact(s):
     return G, H
 
 
-def test_gaussianerf_series_coefficients():
-    s = np.linspace(0.05, 2.0, 40)
+def _kummer(s, first, terms=300):
+    """sum_m s^m / (2m + first)!! in double (positive terms)."""
+    out = np.zeros_like(s)
+    t = np.full_like(s, 1.0 / math.prod(range(first, 0, -2)))
+    for m in range(terms):
+        out += t
+        t = t * s / (2 * m + first + 2)
+    return out
+
+
+def _body(path, head, stop):
+    src = open(path).read()
+    i = src.index(head)
+    return src[i:src.index(stop, i)]
+
+
+def _poly(body, var):
+    c0 = re.search(r"float p = ([-+\d.e]+)f;", body).group(1)
+    rest = re.findall(r"p = fmaf\(p, " + var + r", ([-+\d.e]+)f\);", body)
+    return [float(c0)] + [float(x) for x in rest]   # highest degree first
+
+
+def _erfcx_fit():
+    body = _body(MATH, "float gerf_G_erfcx(", "return fmaf")
+    A, B = (float(v) for v in re.search(r"w = fmaf\(([-+\d.e]+)f, t, ([-+\d.e]+)f\)", body).groups())
+    return A, B, _poly(body, "w")
+
+
+def test_gaussianerf_positive_series():
+    """gerf_GQ below s = 2: G = c2 e (1/3 + s S2), -H/3 = c2 e S2 with
+    S2 = sum s^m/(2m+5)!! (Kummer's series of erf), against the erf closed form."""
+    pytest.importorskip("scipy")
+    s = np.linspace(0.05, 2.0, 60)
     G, H = _gerf_exact(s)
-    Gs = _horner(_coeffs("gerf_G_series"), s)
-    Hs = _horner(_coeffs("gerf_H_series"), s)
-    assert np.abs(Gs / G - 1).max() < 2e-8
-    assert np.abs(Hs / H - 1).max() < 2e-8
+    S2 = _horner(_poly(_body(MATH, "if (s < S_SERIES) {", "const float ce"), "s"), s)
+    ce = math.sqrt(2 / math.pi) * np.exp(-s / 2)
+    assert np.abs(ce * (1 / 3 + s * S2) / G - 1).max() < 2e-9
+    assert np.abs(-3 * ce * S2 / H - 1).max() < 2e-9
+
+
+def test_gaussianerf_erfcx_fit():
+    """gerf_G_erfcx for s >= 2: g = 1 - e (erfcx(rho/sqrt2) + c2 rho), erfcx from
+    the degree-7 fit in w = A t + B, t = 1/(1 + rho/2), rho capped at 10."""
+    pytest.importorskip("scipy")
+    A, B, c = _erfcx_fit()
+    s = np.concatenate([np.linspace(2.0, 50.0, 2000), np.linspace(50.0, 400.0, 200)])
+    rho = np.sqrt(s)
+    t = 1 / (1 + 0.5 * np.minimum(rho, 10.0))
+    h = _horner(c, A * t + B) * t + math.sqrt(2 / math.pi) * rho
+    G = (1 - np.exp(-s / 2) * h) / rho ** 3
+    Gx, _ = _gerf_exact(s)
+    assert np.abs(G / Gx - 1).max() < 2e-8
+
+
+def test_gaussianerf_fp32_design_error():
+    """The whole gerf_GQ evaluated with FP32 rounding after every operation
+    (correctly rounded exp, rsqrt and reciprocal): worst relative error of G and
+    Q over 0 < s <= 120 within 5e-7 and 1.2e-6 -- the bound of the closed
+    form with a correctly rounded erf, set by the FP32 rounding of s^-1.5."""
+    r = lambda x: np.asarray(x, np.float64).astype(np.float32).astype(np.float64)
+    fma = lambda a, b, c: r(np.asarray(a) * np.asarray(b) + np.asarray(c))
+    mul = lambda a, b: r(np.asarray(a) * np.asarray(b))
+    c2 = math.sqrt(2 / math.pi)
+    cs = _poly(_body(MATH, "if (s < S_SERIES) {", "const float ce"), "s")
+    A, B, cw = _erfcx_fit()
+    s = r(np.concatenate([np.linspace(1e-4, 2.0, 4001), np.linspace(2.0, 120.0, 40001)]))
+    e = r(np.exp(-s / 2))
+    p = np.full_like(s, r(cs[0]))
+    for a in cs[1:]:
+        p = fma(p, s, r(a))
+    Gs, Qs = mul(mul(c2, e), fma(s, p, 1 / 3)), mul(mul(c2, e), p)
+    rs = r(1 / np.sqrt(s))
+    rs2 = mul(rs, rs)
+    rho = mul(s, rs)
+    t = r(1 / fma(0.5, np.minimum(rho, 10.0), 1.0))
+    w = fma(A, t, B)
+    q = np.full_like(s, r(cw[0]))
+    for a in cw[1:]:
+        q = fma(q, w, r(a))
+    h = fma(c2, rho, mul(q, t))
+    Gm = mul(mul(fma(-e, h, 1.0), rs), rs2)
+    Qm = mul(fma(-c2 / 3, e, Gm), rs2)
+    G, Q = np.where(s < 2, Gs, Gm), np.where(s < 2, Qs, Qm)
+    Ge = c2 * np.exp(-s / 2) * _kummer(s, 3)
+    Qe = c2 * np.exp(-s / 2) * _kummer(s, 5)
+    assert np.abs(G / Ge - 1).max() < 5e-7
+    assert np.abs(Q / Qe - 1).max() < 1.2e-6
+
+
+def test_adjoint_S3_series():
+    """The adjoint's K(s) = 15 c2 e S3(s), S3 = sum s^m/(2m+7)!!, below s = 6,
+    against K = (15 G - c2 e (5 + s))/s^2 from the erf closed form."""
+    pytest.importorskip("scipy")
+    adj = os.path.join(ROOT, "flowvpm.jl_gb300", "csrc", "adjoint.cu")
+    c = _poly(_body(adj, "float gerf_S3_series(", "return p;"), "s")
+    s = np.linspace(0.5, 6.0, 40)
+    G, _ = _gerf_exact(s)
+    e = math.sqrt(2 / math.pi) * np.exp(-s / 2)
+    K = (15 * G - e * (5 + s)) / s ** 2
+    assert np.abs(15 * e * _horner(c, s) / K - 1).max() < 1e-8
 
 
 def test_gaussian_series_coefficients():

@@ -136,3 +136,70 @@ def test_rollout_matches_host_mirror_step(ctx):
     assert normwise(xa.cpu().numpy(), pf.X)[0] <= 1e-12
     assert normwise(ga.cpu().numpy(), pf.Gamma)[0] <= 1e-12
     assert normwise(sa.cpu().numpy(), pf.sigma)[0] <= 1e-12
+
+
+@pytest.mark.parametrize("k", [0, 2, 3])
+@pytest.mark.parametrize("cloud", ["dense", "spread"])
+def test_mixed_adjoint_kernel_matches_oracle(ctx, k, cloud):
+    """The FP32-comp adjoint against the oracle's FP64 adjoint: normwise <= 2e-6
+    (dense: every pair near; spread: mostly the singular form)."""
+    import torch
+    n = 3000
+    X, G, s = random_cloud(n, seed=90 + k, box=0.15 if cloud == "dense" else 2.0)
+    rng = np.random.default_rng(k + 5)
+    Ub = rng.normal(size=(n, 3))
+    Jb = rng.normal(size=(n, 9))
+    z = lambda *sh: torch.zeros(*sh, device="cuda", dtype=torch.float64)
+    xb, gb, sb = z(n, 3), z(n, 3), z(n)
+    ctx.uj_adjoint_dev(_dev(X), _dev(G), _dev(s), _dev(Ub), _dev(Jb), xb, gb, sb, k, 1)
+    rx, rg, rs = oracle.uj_adjoint(X, G, s, Ub, Jb, k)
+    assert normwise(xb.cpu().numpy(), rx)[0] <= 2e-6
+    assert normwise(gb.cpu().numpy(), rg)[0] <= 2e-6
+    if k != 0:
+        assert normwise(sb.cpu().numpy(), rs)[0] <= 2e-6
+
+
+def test_mixed_rollout_gradient_follows_fp64(ctx):
+    """A ring rollout differentiated in FP32-comp (forward and adjoint) against
+    the FP64 gradient of the same rollout: relative difference <= 1e-4."""
+    from vpm_gb300 import autodiff as ad
+    grads = []
+    for prec in (0, 1):
+        x0, g0, s0 = _ring_state(nphi=40)
+        x, g, s = x0.requires_grad_(), g0.requires_grad_(), s0.requires_grad_()
+        kw = dict(kernel=2, precision=prec, vctx=ctx)
+        ad.ring_loss(*ad.rollout(x, g, s, 0.01, 3, checkpoint=True, **kw), **kw).backward()
+        grads.append([t.grad.cpu().numpy() for t in (x, g, s)])
+    for a, b in zip(grads[1], grads[0]):
+        assert normwise(a, b)[0] <= 1e-4
+
+
+def test_fifty_step_rollout_gradient_on_64_directions(ctx):
+    """The rollout check at the length the adjoint workload names -- 50 RK3 steps
+    (dt = 0.01) with Pedrizzetti relaxation, per-step checkpointing -- on the
+    1400-particle ring (200 sections x 7), against central differences (h = 1e-6)
+    of the FP64 forward along 64 seeded random directions: relative error <= 1e-5."""
+    import torch
+    from vpm_gb300 import autodiff as ad
+    x0, g0, s0 = _ring_state(nphi=200, nper=7)
+    kw = dict(kernel=2, precision=0, vctx=ctx)   # rk3_step relaxes with rlxf = 0.3 by default
+    x, g, s = x0.clone().requires_grad_(), g0.clone().requires_grad_(), s0.clone().requires_grad_()
+    ad.ring_loss(*ad.rollout(x, g, s, 0.01, 50, checkpoint=True, **kw), **kw).backward()
+
+    def loss(dx, dg, ds):
+        with torch.no_grad():
+            return float(ad.ring_loss(*ad.rollout(x0 + dx, g0 + dg, s0 + ds, 0.01, 50, checkpoint=False, **kw),
+                                      **kw))
+    rng = np.random.default_rng(64)
+    h = 1e-6
+    rels = []
+    for _ in range(64):
+        d = rng.normal(size=x0.numel() + g0.numel() + s0.numel())
+        d /= np.linalg.norm(d)
+        dx = _dev(d[:x0.numel()].reshape(x0.shape))
+        dg = _dev(d[x0.numel():x0.numel() + g0.numel()].reshape(g0.shape))
+        ds = _dev(d[x0.numel() + g0.numel():])
+        fd = (loss(h * dx, h * dg, h * ds) - loss(-h * dx, -h * dg, -h * ds)) / (2 * h)
+        an = float((x.grad * dx).sum() + (g.grad * dg).sum() + (s.grad * ds).sum())
+        rels.append(abs(fd - an) / max(abs(an), 1e-300))
+    assert max(rels) <= 1e-5, max(rels)

@@ -7,7 +7,9 @@ precision:
   (src/FLOWVPM.jl:223), core spreading nu=1e-4 and Pedrizzetti relaxation;
   state, U, J, SFS and the C coefficients after every step;
 * the same without SFS/viscosity (the plain ring step);
-* the near-field form with theta=0 equals the all-pairs form (random cloud).
+* the near-field form with theta=0 equals the all-pairs form (random cloud);
+* the near-field step with the dynamic SFS model: FP32-comp with the fused
+  near-field differences against the FP64 near-field step.
 Tolerances are normwise (max|err| / max|ref|).  C is a ratio of two
 differences of nearly equal stretching terms (filter widths 1 and 0.999), so
 it carries ~1e3 times the state's rounding.
@@ -181,3 +183,49 @@ def test_dynamic_diff_matches_two_fp64_evaluations(ctx, kernel, alpha):
         eJ = normwise(dJ.cpu().numpy(), dJ_ref)[0]
         eS = normwise(dS.cpu().numpy(), dS_ref)[0]
         assert eJ <= tolJ and eS <= tolS, (prec, eJ, eS)
+
+
+def test_nearfield_dynamic_sfs_step_follows_fp64(ctx):
+    """Near-field state (leaf_size 32, theta 0.4) with the dynamic SFS model: the
+    FP32-comp step, whose test-filter differences come from
+    vpm_dynamic_diff_leaflist_dev, against the FP64 step that evaluates the
+    near field twice and subtracts (the reference's way)."""
+    import torch
+    X, G, s = workloads.leapfrog_rings(2000, nper=10)
+    dev = lambda v: torch.tensor(np.ascontiguousarray(v), device="cuda", dtype=torch.float64)
+    flds = []
+    for prec in (0, 1):
+        f = ds.DeviceField(dev(X), dev(G), dev(s), kernel=vpm._lib.KERNEL_GAUSSIANERF, precision=prec)
+        f.leaflist = (32, 0.4)
+        flds.append(f)
+    p64, p32 = ds.DynamicSFSParams(), ds.DynamicSFSParams()
+    for step in range(3):
+        ds.rk3_step(flds[0], 0.005, ctx, sfs=p64, relax_rlxf=0.3)
+        ds.rk3_step(flds[1], 0.005, ctx, sfs=p32, relax_rlxf=0.3)
+        for name, tol in (("x", 2e-5), ("gam", 2e-5), ("sig", 2e-5), ("J", 2e-5), ("SFS", 2e-5), ("C", 2e-3)):
+            a, b = getattr(flds[0], name), getattr(flds[1], name)
+            e = normwise(b.cpu().numpy(), a.cpu().numpy())[0]
+            assert e <= tol, (step, name, e)
+
+
+def test_nearfield_core_size_reset_theta_zero_equals_all_pairs(ctx):
+    """The core-size reset of a near-field state takes zeta_fmm's sum over the
+    near lists (vpm_zeta_leaflist_dev); with theta = 0 on a random cloud every
+    pair is near, so the reset step equals the all-pairs one to rounding."""
+    import torch
+    from helpers import random_cloud
+    X, G, s = random_cloud(2000, seed=21, box=0.4, sig_lo=0.04, sig_hi=0.05)
+    n = X.shape[0]
+    dev = lambda v: torch.tensor(np.ascontiguousarray(v), device="cuda", dtype=torch.float64)
+    vol = dev(np.full(n, 0.4 ** 3 / n))
+    a = ds.DeviceField(dev(X), dev(G), dev(s), kernel=vpm._lib.KERNEL_GAUSSIANERF, precision=0, vol=vol)
+    b = ds.DeviceField(dev(X), dev(G), dev(s), kernel=vpm._lib.KERNEL_GAUSSIANERF, precision=0, vol=vol.clone())
+    b.leaflist = (64, 0.0)
+    va = ds.CoreSpreadingParams(1e-3, 0.045, beta=1.0001, iterror=False)
+    vb = ds.CoreSpreadingParams(1e-3, 0.045, beta=1.0001, iterror=False)
+    ds.rk3_step(a, 0.01, ctx, viscous=va)
+    ds.rk3_step(b, 0.01, ctx, viscous=vb)
+    assert va.t_sgm == 0.0 and vb.t_sgm == 0.0     # the reset ran on both
+    for name in ("x", "gam", "sig"):
+        ta, tb = getattr(a, name), getattr(b, name)
+        assert normwise(tb.cpu().numpy(), ta.cpu().numpy())[0] <= 1e-11, name

@@ -188,3 +188,105 @@ def test_malformed_caller_lists_are_rejected(ctx):
         with pytest.raises(L.VPMError) as ei:
             ctx.p2p_lists_dev(*args, lists, kernel=2, precision=1)
         assert ei.value.code == L.ERR_ARG
+
+
+@pytest.mark.parametrize("k,alpha", [(2, 0.999), (3, 0.999), (1, 0.999), (2, 0.667)])
+def test_near_field_dynamic_differences(ctx, k, alpha):
+    """vpm_dynamic_diff_leaflist_dev.  FP64 is the reference's way -- the near-field
+    leg at alpha sigma and at sigma, subtracted -- and equals two vpm_p2p_leaflist_dev
+    calls bit for bit; FP32-comp evaluates the differences directly and agrees with
+    them to FP32 relative accuracy (subtracting two FP32 evaluations would leave
+    ~1e-7 / (1 - alpha) of noise)."""
+    from vpm_gb300 import workloads
+    X, G, s = workloads.leapfrog_rings(3000, nper=10)
+    n = X.shape[0]
+    x, g, sg = _dev(np.ascontiguousarray(X)), _dev(np.ascontiguousarray(G)), _dev(np.ascontiguousarray(s))
+    leaf, theta = 32, 0.4
+
+    def near(sig):
+        U, J, S = _zeros(n, 3), _zeros(n, 9), _zeros(n, 3)
+        st = ctx.p2p_leaflist_dev(x, g, sig, U, J, S, leaf_size=leaf, theta=theta, kernel=k, precision=0, sfs=True)
+        return J, S, st
+
+    J0, S0, st0 = near(sg)
+    Ja, Sa, _ = near(sg * alpha)
+    assert st0[2] < n * n   # a genuine near field
+    dJ_ref, dS_ref = (Ja - J0).cpu().numpy(), (Sa - S0).cpu().numpy()
+    for prec, tolJ, tolS in ((0, 0.0, 0.0), (1, 2e-6, 2e-5)):
+        dJ, dS = _zeros(n, 9), _zeros(n, 3)
+        st = ctx.dynamic_diff_leaflist_dev(x, g, sg, J0, alpha, dJ, dS, leaf_size=leaf, theta=theta, kernel=k,
+                                           precision=prec)
+        assert st == st0
+        if prec == 0:
+            assert np.array_equal(dJ.cpu().numpy(), dJ_ref) and np.array_equal(dS.cpu().numpy(), dS_ref)
+        else:
+            eJ = normwise(dJ.cpu().numpy(), dJ_ref)[0]
+            eS = normwise(dS.cpu().numpy(), dS_ref)[0]
+            assert eJ <= tolJ and eS <= tolS, (eJ, eS)
+
+
+def test_near_field_dynamic_differences_reject_bad_arguments(ctx):
+    import vpm_gb300._lib as L
+    n = 100
+    X, G, s = random_cloud(n, seed=3)
+    x, g, sg = _dev(X), _dev(G), _dev(s)
+    J, dJ, dS = _zeros(n, 9), _zeros(n, 9), _zeros(n, 3)
+    for kw in (dict(alpha=1.0), dict(alpha=0.0), dict(alpha=0.9, leaf_size=0), dict(alpha=0.9, theta=-1.0)):
+        alpha = kw.pop("alpha")
+        with pytest.raises(L.VPMError):
+            ctx.dynamic_diff_leaflist_dev(x, g, sg, J, alpha, dJ, dS, **kw)
+    # host memory where device pointers are required
+    rc = ctx._L.vpm_dynamic_diff_leaflist_dev(ctx._h, n, X.ctypes.data, G.ctypes.data, s.ctypes.data, None,
+                                              X.ctypes.data, 0.9, X.ctypes.data, X.ctypes.data, 32, 0.4, 2, 1, 0,
+                                              None)
+    assert rc == L.ERR_ARG
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_near_field_zeta_matches_oracle_over_the_same_leaf_pairs(ctx, k, prec):
+    """zeta_fmm (src/FLOWVPM_viscous.jl:523-556): the basis field summed over the
+    near leaf pairs only, every particle a target, the self pair and a
+    coincident pair included; W accumulates (+=) like the reference's loop."""
+    import vpm_gb300._lib as L
+    n = 5000
+    X, G, s = random_cloud(n, seed=30 + k, box=0.5)
+    X[9] = X[4]
+    lists = L.leaflist_host(X, 32, 0.4)
+    perm, lb, le, row, col = lists
+    ref = np.zeros((n, 3))
+    for l in range(len(lb)):
+        tg = perm[lb[l]:le[l]]
+        src = np.concatenate([perm[lb[c]:le[c]] for c in col[row[l]:row[l + 1]]])
+        ref[tg] = oracle.zeta_pairs(X[tg], X[src], G[src], s[src], k)
+    W = _zeros(n, 3)
+    st = ctx.zeta_leaflist_dev(_dev(X), _dev(G), _dev(s), W, leaf_size=32, theta=0.4, kernel=k, precision=prec)
+    assert st[2] < n * n and st[1] == len(col)
+    assert normwise(W.cpu().numpy(), ref)[0] <= TOL[prec]
+    ctx.zeta_leaflist_dev(_dev(X), _dev(G), _dev(s), W, leaf_size=32, theta=0.4, kernel=k, precision=prec)
+    assert normwise(W.cpu().numpy(), 2 * ref)[0] <= TOL[prec]
+
+
+def test_zeta_fmm_hook_adds_to_rows_16_18():
+    """vpm.zeta_fmm_gb300 on the host matrix: rows 16:18 of every particle
+    (statics included) += the near-field sum; nothing else changes."""
+    import vpm_gb300 as vpm
+    import vpm_gb300._lib as L
+    n = 1200
+    X, G, s = random_cloud(n, seed=77, box=0.4)
+    static = np.zeros(n, bool)
+    static[::13] = True
+    pf = vpm.ParticleField(n + 3, kernel=vpm.gaussianerf)
+    pf.add_particles(X, G, s, static=static)
+    pf.particles[15:18, :n] = 0.5
+    Q = pf.particles.copy(order="F")
+    vpm.zeta_fmm_gb300(pf, leaf_size=16, theta=0.4)
+    perm, lb, le, row, col = L.leaflist_host(X, 16, 0.4)
+    ref = np.zeros((n, 3))
+    for l in range(len(lb)):
+        tg = perm[lb[l]:le[l]]
+        src = np.concatenate([perm[lb[c]:le[c]] for c in col[row[l]:row[l + 1]]])
+        ref[tg] = oracle.zeta_pairs(X[tg], X[src], G[src], s[src], 2)
+    assert normwise(pf.particles[15:18, :n].T - 0.5, ref)[0] <= 1e-12
+    other = [r for r in range(46) if r not in (15, 16, 17)]
+    assert np.array_equal(pf.particles[other, :], Q[other, :])
