@@ -683,8 +683,10 @@ def run_rollout(args):
 
 def run_kernel_only_jet(args):
     """Profiling helper: `warmup` + `steps` near-field UJ (+Estr with --estr)
-    calls on the jet cloud of --n particles at the density of the 2^20 case
-    (the cylinder is shortened in proportion), nothing else."""
+    calls -- or, with --jet-call dynamic, calls of the dynamic procedure's
+    near-field differences (alpha = 0.999) -- on the jet cloud of --n particles
+    at the density of the 2^20 case (the cylinder is shortened in proportion),
+    nothing else."""
     import torch
     import vpm_gb300 as vpm
     from vpm_gb300 import workloads
@@ -698,15 +700,23 @@ def run_kernel_only_jet(args):
     S = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
     prec = vpm.FP64 if args.precision == "fp64" else vpm.FP32COMP
     times, st = [], None
+    if args.jet_call == "dynamic":
+        ctx.p2p_leaflist_dev(x, g, sg, U, J, leaf_size=64, theta=0.4, kernel=KERNEL, precision=prec)
+        dJ, dS = torch.zeros_like(J), torch.zeros_like(S)
     for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = ctx.p2p_leaflist_dev(x, g, sg, U, J, S, leaf_size=64, theta=0.4, kernel=KERNEL, precision=prec,
-                                  sfs=bool(args.estr))
+        if args.jet_call == "dynamic":
+            st = ctx.dynamic_diff_leaflist_dev(x, g, sg, J, 0.999, dJ, dS, leaf_size=64, theta=0.4, kernel=KERNEL,
+                                               precision=prec)
+        else:
+            st = ctx.p2p_leaflist_dev(x, g, sg, U, J, S, leaf_size=64, theta=0.4, kernel=KERNEL, precision=prec,
+                                      sfs=bool(args.estr))
         if k >= args.warmup:
             times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.mean(times) if times else float("nan")
-    print(json.dumps({"mode": "kernel-only-jet", "n": n, "precision": args.precision, "estr": bool(args.estr),
-                      "ms": ms, "leaves": st[0], "leaf_pairs": st[1], "pairs": st[2],
+    print(json.dumps({"mode": "kernel-only-jet", "call": args.jet_call, "n": n, "precision": args.precision,
+                      "estr": bool(args.estr), "ms": ms, "leaves": st[0], "leaf_pairs": st[1], "pairs": st[2],
                       "pairs_per_s": st[2] / (ms / 1e3), "launches": ctx.launches}))
 
 
@@ -722,6 +732,7 @@ def main():
     ap.add_argument("--precision", default="fp32comp", choices=["fp64", "fp32comp"])
     ap.add_argument("--kernel", default="gaussianerf", choices=["singular", "gaussian", "gaussianerf", "winckelmans"])
     ap.add_argument("--estr", action="store_true")
+    ap.add_argument("--jet-call", default="uj", choices=["uj", "dynamic"])
     # the other workloads (one JSON line each, not the bench line)
     ap.add_argument("--workload", default="cloud", choices=["cloud", "leapfrog", "jet", "rollout"])
     ap.add_argument("--lf-n", type=int, default=200_000)

@@ -44,25 +44,67 @@ __host__ __device__ constexpr float dyn_skip_s()
     return K == K_GAUSERF ? 60.0f : K == K_GAUS ? 9.0f : 3.0e38f;
 }
 
-// (dg, dg1) of one pair at rho for the filter factor alpha (ha = 1/alpha - 1):
-// m two-point Gauss-Legendre panels on [rho, rho/alpha] (m from ha, warp-uniform;
-// one panel for alpha = 0.999, eight for alpha = 0.667)
-template <int K>
-__device__ __forceinline__ void filter_diff(float rho, float ha, int m, float& dg, float& dg1)
+// (dg, dg1) of one pair at rho for the filter factor alpha: m two-point
+// Gauss-Legendre panels on [rho, rho/alpha], hm = (1/alpha - 1)/m (m warp-uniform;
+// one panel for alpha = 0.999, eight for alpha = 0.667).  M > 0 fixes m = M at
+// compile time.
+template <int K, int M = 0>
+__device__ __forceinline__ void filter_diff(float rho, float hm, int m, float& dg, float& dg1)
 {
-    const float h = rho * ha / (float)m;
+    const float h = rho * hm;
     const float o = 0.28867513459481287f * h;    // h / (2 sqrt 3)
     float s1 = 0.0f, s2 = 0.0f;
-    for (int k = 0; k < m; k++) {
+    auto panel = [&](int k) {
         const float c = fmaf((float)k + 0.5f, h, rho);
         float a1, a2, b1, b2;
         g_d1_d2_f32<K>(c - o, a1, a2);
         g_d1_d2_f32<K>(c + o, b1, b2);
         s1 += a1 + b1;
         s2 += fmaf(c - o, a2, a1) + fmaf(c + o, b2, b1);
+    };
+    if constexpr (M > 0) {
+#pragma unroll
+        for (int k = 0; k < M; k++) panel(k);
+    } else {
+        for (int k = 0; k < m; k++) panel(k);
     }
     dg = 0.5f * h * s1;
-    dg1 = 0.5f * h * s2 / rho;
+    dg1 = __fdividef(0.5f * h * s2, rho);
+}
+
+// e^x - 1 and log(1 + x): Taylor series for |x| <= 1/8 (truncation below 1e-9
+// relative: the dynamic procedure's alpha = 0.999 keeps every argument there),
+// the library functions beyond
+__device__ __forceinline__ float expm1_small(float x)
+{
+    if (fabsf(x) <= 0.125f) {
+        float p = 1.9841269841269841e-4f;     // 1/5040
+        p = fmaf(p, x, 1.3888888888888889e-3f);
+        p = fmaf(p, x, 8.3333333333333333e-3f);
+        p = fmaf(p, x, 4.1666666666666667e-2f);
+        p = fmaf(p, x, 0.16666666666666667f);
+        p = fmaf(p, x, 0.5f);
+        p = fmaf(p, x, 1.0f);
+        return p * x;
+    }
+    return expm1f(x);
+}
+__device__ __forceinline__ float log1p_small(float x)
+{
+    if (fabsf(x) <= 0.125f) {
+        float p = -0.1f;        // log(1 + x)/x = sum_k (-x)^k/(k + 1)
+        p = fmaf(p, x, 0.11111111111111111f);
+        p = fmaf(p, x, -0.125f);
+        p = fmaf(p, x, 0.14285714285714286f);
+        p = fmaf(p, x, -0.16666666666666667f);
+        p = fmaf(p, x, 0.2f);
+        p = fmaf(p, x, -0.25f);
+        p = fmaf(p, x, 0.33333333333333333f);
+        p = fmaf(p, x, -0.5f);
+        p = fmaf(p, x, 1.0f);
+        return p * x;
+    }
+    return log1pf(x);
 }
 
 // zeta~(r, alpha sigma) / zeta~(r, sigma) - 1 at s = (r/sigma)^2, zeta~(r, sigma) =
@@ -71,31 +113,36 @@ template <int K>
 __device__ __forceinline__ float zeta_ratio_m1(float s, float3 fd)
 {
     if constexpr (K == K_GAUSERF) {          // zeta ~ e^{-rho^2/2}
-        return fmaf(fd.y, expm1f(-0.5f * s * fd.z), fd.x);
+        return fmaf(fd.y, expm1_small(-0.5f * s * fd.z), fd.x);
     } else if constexpr (K == K_GAUS) {      // zeta ~ e^{-rho^3}
-        return fmaf(fd.y, expm1f(-s * sqrtf(s) * fd.x), fd.x);
+        return fmaf(fd.y, expm1_small(-s * sqrtf(s) * fd.x), fd.x);
     } else if constexpr (K == K_WNKLMNS) {   // zeta ~ (rho^2 + 1)^-3.5
         const float eps = s * fd.z / fmaf(s, 1.0f + fd.z, 1.0f);
-        return fmaf(fd.y, expm1f(3.5f * log1pf(-eps)), fd.x);
+        return fmaf(fd.y, expm1_small(3.5f * log1p_small(-eps)), fd.x);
     } else {
         return 0.0f;
     }
 }
+
 // One pair's dJ (the pair's J term of src/FLOWVPM_fmm.jl:112-160 differenced
 // in sigma, column-major 3x3), added to f: e = x_t - x_s (|e|^2 = r2 > 0),
 // isig = 1/sigma_s, gam = the packed Gamma_s * (-1/(4 pi)) (over sigma_s^3 unless
-// singular_tail<K>), m Gauss-Legendre panels for ha = 1/alpha - 1.
-template <int K>
+// singular_tail<K>), panels as in filter_diff.  on = false adds zero (r2 must
+// still be positive and finite), so that callers can run four pairs without
+// branches.
+template <int K, int M = 0>
 __device__ __forceinline__ void filter_diff_pair(float ex, float ey, float ez, float r2, float isig, float4 gam,
-                                                 float ha, int m, float (&f)[9])
+                                                 float hm, int m, bool on, float (&f)[9])
 {
     const float rinv = rsqrtf(r2);
     const float rho = r2 * rinv * isig;
     float dg, dg1;
-    filter_diff<K>(rho, ha, m, dg, dg1);
+    filter_diff<K, M>(rho, hm, m, dg, dg1);
+    dg = on ? dg : 0.0f;
+    dg1 = on ? dg1 : 0.0f;
     float gx = gam.x, gy = gam.y, gz = gam.z;
     if constexpr (!singular_tail<K>()) {
-        const float sig3 = 1.0f / (isig * isig * isig);
+        const float sig3 = __fdividef(1.0f, isig * isig * isig);
         gx *= sig3; gy *= sig3; gz *= sig3;
     }
     const float ri2 = rinv * rinv, ri3 = ri2 * rinv;

@@ -41,10 +41,10 @@ constexpr int DYN_TILE = 128;
 // dJ of every target (Morton order) from every source of the pack (same
 // order), accumulated into dJ[idx*9 + k].  Pair math as above; dx as a
 // double-float (x_hi, x_lo); FP32 sums over 64-source blocks, FP64 beyond.
-template <int K>
+template <int K, int M>
 __global__ void __launch_bounds__(DYN_THREADS)
 uj_filter_diff_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad, const SrcMixed* __restrict__ src,
-                      float ha, int panels, double* __restrict__ dJ)
+                      float hm, int panels, double* __restrict__ dJ)
 {
     __shared__ SrcMixed tile[DYN_TILE];
     __shared__ float4 off[DYN_THREADS / 32][DYN_TILE];
@@ -96,16 +96,22 @@ uj_filter_diff_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad
                     far = far && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * h.w > skip;
                 }
                 if (__all_sync(0xffffffffu, far || !valid)) continue;
+                float ex[4], ey[4], ez[4], r2[4];
+                bool on[4];
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const SrcMixed& s = tile[j0 + q];
-                    const float ex = (th.x - s.a.x) + (tl.x - s.b.x);
-                    const float ey = (th.y - s.a.y) + (tl.y - s.b.y);
-                    const float ez = (th.z - s.a.z) + (tl.z - s.b.z);
-                    const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                    if (!(r2 > 0.0f)) continue;
-                    filter_diff_pair<K>(ex, ey, ez, r2, s.b.w, s.gam, ha, panels, f);
+                    ex[q] = (th.x - s.a.x) + (tl.x - s.b.x);
+                    ey[q] = (th.y - s.a.y) + (tl.y - s.b.y);
+                    ez[q] = (th.z - s.a.z) + (tl.z - s.b.z);
+                    r2[q] = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+                    on[q] = r2[q] > 0.0f;
+                    r2[q] = on[q] ? r2[q] : 1.0f;
                 }
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    filter_diff_pair<K, M>(ex[q], ey[q], ez[q], r2[q], tile[j0 + q].b.w, tile[j0 + q].gam, hm,
+                                           panels, on[q], f);
             }
 #pragma unroll
             for (int k = 0; k < 9; k++) acc[k] += (double)f[k];
@@ -154,7 +160,11 @@ static cudaError_t launch_uj_filter_diff_k(int64_t n, const double* x, const dou
     pack_src_dyn<K><<<(unsigned)((ns_pad + 255) / 256), 256, 0, st>>>(n, ns_pad, x, gam, sig, src);
     const unsigned grid = (unsigned)((n + DYN_THREADS - 1) / DYN_THREADS);
     const double ha = 1.0 / alpha - 1.0;
-    uj_filter_diff_kernel<K><<<grid, DYN_THREADS, 0, st>>>(n, tgt, ns_pad, src, (float)ha, filter_panels(ha), dJ);
+    const int m = filter_panels(ha);
+    if (m == 1)
+        uj_filter_diff_kernel<K, 1><<<grid, DYN_THREADS, 0, st>>>(n, tgt, ns_pad, src, (float)ha, 1, dJ);
+    else
+        uj_filter_diff_kernel<K, 0><<<grid, DYN_THREADS, 0, st>>>(n, tgt, ns_pad, src, (float)(ha / m), m, dJ);
     *launches += 2;
     return cudaGetLastError();
 }

@@ -276,29 +276,24 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
 // ------------------------------------------- dynamic procedure, FP32-comp
 // dJ_t += the test-filter difference of every near pair's J term,
 // j(dx, Gamma_s, alpha sigma_s) - j(dx, Gamma_s, sigma_s), evaluated as a
-// difference (dynamic.cu) over the group's intervals; masked pairs and pairs
-// at r = 0 skipped, 4-source groups past the kernel's reach skipped warp-wide.
-template <int K>
+// difference (dynamic.cu) over the group's intervals, four pairs at a time
+// without branches (masked pairs and pairs at r = 0 add zero); M as in
+// filter_diff.  No far vote: near-list pairs are almost all within reach.
+template <int K, int M>
 __global__ void __launch_bounds__(NF_THREADS)
 nf_filter_diff(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
                const int32_t* __restrict__ grp_row, const int4* __restrict__ ivs, const SrcMixed* __restrict__ src,
-               float ha, int panels, double* dJ)
+               float hm, int panels, double* dJ)
 {
     __shared__ SrcMixed tile[NF_WARPS][32];
-    __shared__ float4 off[NF_WARPS][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
     if (grp >= ngroups) return;
     const int64_t p0 = 32 * grp;
     const GroupTarget me = group_target(n, p0, lane, tgt, leaf_of);
-    const TgtPos o = tgt[p0];
     const float3 th = make_float3((float)me.tx, (float)me.ty, (float)me.tz);
     const float3 tl = make_float3((float)(me.tx - (double)th.x), (float)(me.ty - (double)th.y),
                                   (float)(me.tz - (double)th.z));
-    const float3 oh = make_float3((float)o.x, (float)o.y, (float)o.z);
-    const float3 ol = make_float3((float)(o.x - (double)oh.x), (float)(o.y - (double)oh.y), (float)(o.z - (double)oh.z));
-    const float3 to = make_float3((float)(me.tx - o.x), (float)(me.ty - o.y), (float)(me.tz - o.z));
-    const float skip = dyn_skip_s<K>();
     double acc[9];
     float f[9];
 #pragma unroll
@@ -322,30 +317,24 @@ nf_filter_diff(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const
         sj.gam.w = __uint_as_float(smask);
         __syncwarp();
         tile[warp][lane] = sj;
-        off[warp][lane] = make_float4((sj.a.x - oh.x) + (sj.b.x - ol.x), (sj.a.y - oh.y) + (sj.b.y - ol.y),
-                                      (sj.a.z - oh.z) + (sj.b.z - ol.z), sj.b.w * sj.b.w);
         __syncwarp();
         for (int j0 = 0; j0 < cnt; j0 += 4) {   // cnt <= 32: j0 + 3 stays in the tile
-            bool far = true;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float4 h = off[warp][j0 + q];
-                const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
-                const bool mine = (__float_as_uint(tile[warp][j0 + q].gam.w) & me.bit) != 0u;
-                far = far && (!mine || fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * h.w > skip);
-            }
-            if (__all_sync(0xffffffffu, far)) continue;
+            float ex[4], ey[4], ez[4], r2[4];
+            bool on[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const SrcMixed& s = tile[warp][j0 + q];
-                if (!(__float_as_uint(s.gam.w) & me.bit)) continue;
-                const float ex = (th.x - s.a.x) + (tl.x - s.b.x);
-                const float ey = (th.y - s.a.y) + (tl.y - s.b.y);
-                const float ez = (th.z - s.a.z) + (tl.z - s.b.z);
-                const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                if (!(r2 > 0.0f)) continue;
-                filter_diff_pair<K>(ex, ey, ez, r2, s.b.w, s.gam, ha, panels, f);
+                ex[q] = (th.x - s.a.x) + (tl.x - s.b.x);
+                ey[q] = (th.y - s.a.y) + (tl.y - s.b.y);
+                ez[q] = (th.z - s.a.z) + (tl.z - s.b.z);
+                r2[q] = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+                on[q] = (__float_as_uint(s.gam.w) & me.bit) != 0u && r2[q] > 0.0f;
+                r2[q] = on[q] ? r2[q] : 1.0f;
             }
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                filter_diff_pair<K, M>(ex[q], ey[q], ez[q], r2[q], tile[warp][j0 + q].b.w, tile[warp][j0 + q].gam, hm,
+                                       panels, on[q], f);
         }
         if (++tiles == NF_BLK_TILES) {
             tiles = 0;
@@ -465,8 +454,8 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
         const int cnt = walk.next(lane, sp, smask);
         if (cnt == 0) break;
         __syncwarp();
-        if (sp >= 0) {
-            if constexpr (MIXED) {
+        if constexpr (MIXED) {
+            if (sp >= 0) {
                 const SrcEstrMixed p = ((const SrcEstrMixed*)srcv)[sp];
                 const float xh = (float)p.x, yh = (float)p.y, zh = (float)p.z;
                 mtile[warp][0][lane] = make_float4(xh, yh, zh, p.isig2);
@@ -474,18 +463,23 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
                                                    (float)(p.z - (double)zh), 0.f);
                 mtile[warp][2][lane] = p.g;
                 mtile[warp][3][lane] = p.v;
-            } else {
-                dtile[warp][lane] = ((const SrcEstrF64*)srcv)[sp];
+            } else {   // padding: far away, no payload (read by the unrolled sub-blocks with mask 0)
+                mtile[warp][0][lane] = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+                mtile[warp][1][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                mtile[warp][2][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                mtile[warp][3][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
+        } else {
+            if (sp >= 0) dtile[warp][lane] = ((const SrcEstrF64*)srcv)[sp];
         }
         spos[warp][lane] = sp;
         tmask[warp][lane] = smask;
         __syncwarp();
         if constexpr (MIXED) {
-            for (int j0 = 0; j0 < cnt; j0 += 8) {
+            for (int j0 = 0; j0 < cnt; j0 += 8) {   // cnt <= 32: j0 + 7 stays in the tile (padding has mask 0)
                 float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
-                const int j1 = min(j0 + 8, cnt);
-                for (int j = j0; j < j1; j++) {
+#pragma unroll
+                for (int j = j0; j < j0 + 8; j++) {
                     const float4 h = mtile[warp][0][j], l = mtile[warp][1][j];
                     const float dx = (th.x - h.x) + (tl.x - l.x);
                     const float dy = (th.y - h.y) + (tl.y - l.y);
@@ -617,8 +611,13 @@ static cudaError_t launch_leaf_dyn_k(const LeafArgs& a, const NearLists& L, doub
     *launches += 1;
     if constexpr (K != K_SING) {   // g = 1 has no sigma dependence: dJ = 0
         leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
-        nf_filter_diff<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
-                                                     (const SrcMixed*)src, (float)ha, filter_panels(ha), dJ);
+        const int m = filter_panels(ha);
+        if (m == 1)
+            nf_filter_diff<K, 1><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                            (const SrcMixed*)src, (float)ha, 1, dJ);
+        else
+            nf_filter_diff<K, 0><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                            (const SrcMixed*)src, (float)(ha / m), m, dJ);
         *launches += 2;
     }
     const float3 fd = make_float3((float)(1.0 / (alpha * alpha * alpha) - 1.0), (float)(1.0 / (alpha * alpha * alpha)),

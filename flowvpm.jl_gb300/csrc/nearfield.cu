@@ -60,7 +60,7 @@ typedef unsigned long long ull;
 
 // what the traversal reads of a node, in one 64-B record: centre, radius,
 // first child, number of children (0: a leaf) and the leaf's index
-struct __align__(64) TravNode { double x, y, z, w; int first, nkid, leaf, pad[5]; };
+struct __align__(64) TravNode { double x, y, z, w; int first, nkid, leaf; float w32; int pad[4]; };
 
 __device__ __forceinline__ uint64_t spread3(uint64_t v)
 {
@@ -76,22 +76,35 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v)
 __device__ __forceinline__ int64_t gtid() { return blockIdx.x * (int64_t)blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
 
-// Every lane of the warp calls this; returns the lane's slot in a shared
-// append counter (one atomic per warp).
-__device__ __forceinline__ ull warp_append(ull* ctr, unsigned k)
+// Every thread of the block calls this (no early exit: it holds barriers);
+// returns the thread's slot in a shared append counter, with one atomic per
+// block.  sw: GS_THREADS/32 words of shared memory, sb: one.
+__device__ __forceinline__ ull block_append(ull* ctr, unsigned k, unsigned* sw, ull* sb)
 {
-    const unsigned lane = threadIdx.x & 31;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     unsigned incl = k;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (unsigned)o) incl += v;
     }
-    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
-    ull base = 0;
-    if (lane == 31 && total) base = atomicAdd(ctr, (ull)total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    return base + incl - k;
+    if (lane == 31) sw[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const unsigned t = lane < nw ? sw[lane] : 0u;
+        unsigned w = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (unsigned)o) w += v;
+        }
+        if (lane < nw) sw[lane] = w - t;                  // exclusive offset of each warp
+        if (lane == nw - 1) *sb = w ? atomicAdd(ctr, (ull)w) : 0ull;
+    }
+    __syncthreads();
+    const ull slot = *sb + sw[warp] + incl - k;
+    __syncthreads();                                      // sw, sb are reused by the next call
+    return slot;
 }
 
 // ------------------------------------------------------------------ keys
@@ -315,21 +328,30 @@ __global__ void nt_cr(const ull* __restrict__ ctr, const double* __restrict__ bo
         TravNode t;
         t.x = c[0]; t.y = c[1]; t.z = c[2]; t.w = __dmul_rn(0.5, __dsqrt_rn(d2));
         t.first = nd.z; t.nkid = nd.w; t.leaf = node_leaf[id];
-        for (int k = 0; k < 5; k++) t.pad[k] = 0;
+        t.w32 = (float)t.w;
+        for (int k = 0; k < 4; k++) t.pad[k] = 0;
         cr[id] = t;
     }
 }
 
 // -------------------------------------------------------------- traversal
+// The acceptance test theta r >= R_A + R_B is decided in FP32 on the squares,
+// from the FP64 centre differences (each rounded once to FP32): the FP32 sides
+// carry < 2^-20 relative error, so a difference above 2^-17 of their sum gives
+// tree.cpp's FP64 decision; closer calls, and A = B, take the FP64 test itself
+// (GB300's FP64 pipe runs at 1/64 of the FP32 rate: the FP64 test was most of
+// this kernel's time).
 __global__ void nt_trav(int step, double theta, const TravNode* __restrict__ cr, const int2* __restrict__ fin,
                         int2* __restrict__ fout, uint64_t* __restrict__ near, ull* __restrict__ ctr, ull capF, ull capN)
 {
+    __shared__ unsigned sw[GS_THREADS / 32];
+    __shared__ ull sb;
+    const float th2 = (float)(theta * theta);
     const ull raw = ctr[C_F + step];
     const int64_t cnt = (int64_t)(raw < capF ? raw : capF);
-    const unsigned lane = threadIdx.x & 31;
-    const int64_t warps = gstride() >> 5;
-    for (int64_t base = (gtid() >> 5) << 5; base < cnt; base += warps << 5) {
-        const int64_t i = base + lane;
+    // block-strided so that every thread of a block runs the same iterations (block_append)
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < cnt; base += gstride()) {
+        const int64_t i = base + threadIdx.x;
         unsigned knear = 0, ksplit = 0;
         int A = 0, B = 0, first = 0, la_leaf = 0, lb_leaf = 0;
         bool split_a = false;
@@ -339,8 +361,18 @@ __global__ void nt_trav(int step, double theta, const TravNode* __restrict__ cr,
             B = ab.y;
             const TravNode a = cr[A], c = cr[B];
             const double dx = __dsub_rn(a.x, c.x), dy = __dsub_rn(a.y, c.y), dz = __dsub_rn(a.z, c.z);
-            const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-            const bool far = (A != B) && (__dmul_rn(theta, r) >= __dadd_rn(a.w, c.w));
+            const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+            const float lhs = th2 * fmaf(fx, fx, fmaf(fy, fy, fz * fz));
+            const float rs = a.w32 + c.w32;
+            const float rhs = rs * rs;
+            bool far;
+            if (A != B && fabsf(lhs - rhs) > 7.62939453125e-06f * (lhs + rhs)) {
+                far = lhs > rhs;
+            } else {   // tree.cpp's FP64 test, in its operation order
+                const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                      __dmul_rn(dz, dz)));
+                far = (A != B) && (__dmul_rn(theta, r) >= __dadd_rn(a.w, c.w));
+            }
             if (!far) {
                 const bool la = a.nkid == 0, lb = c.nkid == 0;
                 if (la && lb) {
@@ -354,12 +386,12 @@ __global__ void nt_trav(int step, double theta, const TravNode* __restrict__ cr,
                 }
             }
         }
-        const ull sn = warp_append(&ctr[C_NEAR], knear);
+        const ull sn = block_append(&ctr[C_NEAR], knear, sw, &sb);
         if (knear) {
             if (sn < capN) near[sn] = ((uint64_t)(uint32_t)la_leaf << 32) | (uint32_t)lb_leaf;
             else ctr[C_OVF] = 1;
         }
-        const ull sf = warp_append(&ctr[C_F + step + 1], ksplit);
+        const ull sf = block_append(&ctr[C_F + step + 1], ksplit, sw, &sb);
         if (ksplit) {
             if (sf + ksplit <= capF) {
                 for (unsigned k = 0; k < ksplit; k++) {

@@ -213,3 +213,16 @@ def test_far_field_cutoffs_are_below_fp32_resolution():
     t = 8.0 ** 1.5
     e = math.exp(-t)
     assert abs((1 - e) - 1) < 1e-9 and abs(3 * (t * e - 1 + e) / -3 - 1) < 1e-8
+
+
+def test_dynamic_ratio_series():
+    """dyn_math.cuh's e^x - 1 and log(1 + x) series (used for |x| <= 1/8 in the
+    dynamic procedure's weight ratio) against numpy: < 1e-10 relative."""
+    dyn = os.path.join(ROOT, "flowvpm.jl_gb300", "csrc", "dyn_math.cuh")
+    x = np.linspace(-0.125, 0.125, 4001)
+    x = x[x != 0]
+    for head, ref in (("float expm1_small(", np.expm1), ("float log1p_small(", np.log1p)):
+        body = _body(dyn, head, "return p * x")
+        c = [float(re.search(r"float p = ([-+\d.e]+)f;", body).group(1))]
+        c += [float(v) for v in re.findall(r"p = fmaf\(p, x, ([-+\d.e]+)f\);", body)]
+        assert np.abs(_horner(c, x) * x / ref(x) - 1).max() < 1e-10, head
