@@ -918,6 +918,86 @@ int vpm_p2p_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
     return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags, stats);
 }
 
+int vpm_rk3_stage_dev(vpm_ctx* c, int64_t n, double a, double b, double dt, const double* Uinf, double f, double g,
+                      double zeta0, double nu, int flags, double* x, double* gam, double* sig, const double* U,
+                      const double* J, const double* SFS, const double* C, double* M)
+{
+    const char* fn = "vpm_rk3_stage_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
+    if (!Uinf) return fail(c, VPM_ERR_ARG, "%s: Uinf is NULL", fn);
+    if (!(std::isfinite(a) && std::isfinite(b) && std::isfinite(dt) && std::isfinite(f) && std::isfinite(g) &&
+          std::isfinite(zeta0) && zeta0 != 0.0 && std::isfinite(nu) && 1.0 + 3.0 * f != 0.0))
+        return fail(c, VPM_ERR_ARG, "%s: bad scalar argument", fn);
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(U) || !is_device_ptr(J) ||
+        !is_device_ptr(M) || (SFS && (!is_device_ptr(SFS) || !C || !is_device_ptr(C))))
+        return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer (C with SFS)", fn);
+    StageArgs s;
+    s.n = n; s.a = a; s.b = b; s.dt = dt; s.f = f; s.g = g; s.zeta0 = zeta0; s.nu = nu;
+    for (int k = 0; k < 3; k++) s.uinf[k] = Uinf[k];
+    s.transposed = (flags & VPM_TRANSPOSED) != 0;
+    s.x = x; s.gam = gam; s.sig = sig; s.U = U; s.J = J; s.SFS = SFS; s.C = SFS ? C : nullptr; s.M = M;
+    CK(launch_rk3_stage(s, c->stream, &c->launches), "RK3 stage");
+    return bounded_wait(c);
+}
+
+int vpm_relax_dev(vpm_ctx* c, int64_t n, double rlxf, const double* J, double* gam)
+{
+    const char* fn = "vpm_relax_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (!std::isfinite(rlxf)) return fail(c, VPM_ERR_ARG, "%s: bad rlxf", fn);
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(J) || !is_device_ptr(gam)) return fail(c, VPM_ERR_ARG, "%s: device pointers required", fn);
+    CK(launch_relax(n, rlxf, J, gam, c->stream, &c->launches), "relaxation");
+    return bounded_wait(c);
+}
+
+int vpm_dynamic_after_dev(vpm_ctx* c, int64_t n, double alpha, double rlxf, double minC, double maxC, double zeta0,
+                          int flags, const double* gam, const double* sig, const double* J, const double* SFS,
+                          double* C, double* M)
+{
+    const char* fn = "vpm_dynamic_after_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (flags & ~(VPM_TRANSPOSED | VPM_DYN_FORCE_POSITIVE | VPM_DYN_CLIP_BACKSCATTER | VPM_DYN_SUBTRACT))
+        return fail(c, VPM_ERR_ARG, "%s: unknown flags", fn);
+    if (!(std::isfinite(alpha) && std::isfinite(rlxf) && !std::isnan(minC) && !std::isnan(maxC) &&
+          std::isfinite(zeta0) && zeta0 != 0.0))
+        return fail(c, VPM_ERR_ARG, "%s: bad scalar argument", fn);
+    // the reference's error cases (src/FLOWVPM_subfilterscale.jl:549-556)
+    if (minC < 0.0) return fail(c, VPM_ERR_ARG, "Invalid C bounds: Got a negative bound for minC (%g)", minC);
+    if (maxC < 0.0) return fail(c, VPM_ERR_ARG, "Invalid C bounds: Got a negative bound for maxC (%g)", maxC);
+    if (minC > maxC) return fail(c, VPM_ERR_ARG, "Invalid C bounds: minC > maxC (%g > %g)", minC, maxC);
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(SFS) || !is_device_ptr(C) ||
+        !is_device_ptr(M) || ((flags & VPM_DYN_SUBTRACT) && !is_device_ptr(J)))
+        return fail(c, VPM_ERR_ARG, "%s: device pointers required", fn);
+    RC(grow(c, c->flag, sizeof(int), "flag"));
+    int* dflag = (int*)c->flag.p;
+    CK(cudaMemsetAsync(dflag, 0, sizeof(int), c->stream), "memset flag");
+    DynAfterArgs d;
+    d.n = n; d.alpha = alpha; d.rlxf = rlxf; d.minC = minC; d.maxC = maxC; d.zeta0 = zeta0; d.flags = flags;
+    d.gam = gam; d.sig = sig; d.J = J; d.SFS = SFS; d.C = C; d.M = M;
+    CK(launch_dynamic_after(d, dflag, c->stream, &c->launches), "dynamic procedure");
+    RC(bounded_wait(c));   // the kernel has finished: the flag's copy cannot block on it
+    int hflag = 0;
+    CK(cudaMemcpy(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost), "D2H flag");
+    if (hflag) return fail(c, VPM_ERR_NONFINITE, "%s: NaN in dynamicprocedure_pseudo3level_afterUJ", fn);
+    return VPM_OK;
+}
+
 int vpm_zeta_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig, double* W,
                           int leaf_size, double theta, int kernel, int precision, int64_t* stats)
 {

@@ -186,6 +186,26 @@ cudaError_t near_groups(NearScratch& s, NearLists* L, cudaStream_t st, SyncFn sy
 constexpr int LEAF_SIZE_MAX = 4096;
 size_t leaf_work_bytes(int64_t n);
 cudaError_t launch_leaflist(const LeafArgs& a, const NearLists& L, void* work, cudaStream_t st, int64_t* launches);
+// The per-particle work of an RK3 step (step.cu).
+struct StageArgs {
+    int64_t n;
+    double a, b, dt, uinf[3], f, g, zeta0, nu;   // nu < 0: no core spreading
+    bool transposed;
+    double* x; double* gam; double* sig;
+    const double* U; const double* J; const double* SFS; const double* C;
+    double* M;
+};
+struct DynAfterArgs {
+    int64_t n;
+    double alpha, rlxf, minC, maxC, zeta0;
+    int flags;
+    const double* gam; const double* sig; const double* J; const double* SFS;
+    double* C; double* M;
+};
+cudaError_t launch_rk3_stage(const StageArgs& a, cudaStream_t st, int64_t* launches);
+cudaError_t launch_relax(int64_t n, double rlxf, const double* J, double* gam, cudaStream_t st, int64_t* launches);
+cudaError_t launch_dynamic_after(const DynAfterArgs& a, int* nan_flag, cudaStream_t st, int64_t* launches);
+
 // zeta_fmm's near-field sum: W[n,3] += sum over the near lists of zeta(r/sigma_s)/sigma_s^3 Gamma_s.
 cudaError_t launch_leaf_zeta(const LeafArgs& a, const NearLists& L, double* W, void* work, cudaStream_t st,
                              int64_t* launches);

@@ -20,6 +20,7 @@ OK, ERR_ARG, ERR_CAPACITY, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NODEVICE, E
 KERNEL_SINGULAR, KERNEL_GAUSSIAN, KERNEL_GAUSSIANERF, KERNEL_WINCKELMANS = 0, 1, 2, 3
 FP64, FP32COMP = 0, 1
 RESET, RESET_SFS, SFS, TRANSPOSED, CHECK_FINITE = 1, 2, 4, 8, 16
+DYN_FORCE_POSITIVE, DYN_CLIP_BACKSCATTER, DYN_SUBTRACT = 32, 64, 128
 NFIELDS = 46
 FLOP_PER_UJ_PAIR = 74
 FLOP_PER_ESTR_PAIR = 25
@@ -52,6 +53,10 @@ SIGNATURES = {
     "vpm_zeta": (_int, [_vp, _vp, _i64, _i64, _int, _int]),
     "vpm_dynamic_diff_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _int, _int]),
     "vpm_zeta_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _int, _int]),
+    "vpm_rk3_stage_dev": (_int, [_vp, _i64, _dbl, _dbl, _dbl, _vp, _dbl, _dbl, _dbl, _dbl, _int, _vp, _vp, _vp, _vp,
+                                 _vp, _vp, _vp, _vp]),
+    "vpm_relax_dev": (_int, [_vp, _i64, _dbl, _vp, _vp]),
+    "vpm_dynamic_after_dev": (_int, [_vp, _i64, _dbl, _dbl, _dbl, _dbl, _dbl, _int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "vpm_zeta_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _vp]),
     "vpm_dynamic_diff_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _dbl, _int,
                                              _int, _int, _vp]),
@@ -202,6 +207,44 @@ class Context:
         self._check(self._L.vpm_dynamic_diff_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(J),
                                                  float(alpha), _ptr(dJ), _ptr(dSFS), int(kernel), int(precision),
                                                  TRANSPOSED if transposed else 0))
+
+    # ------------------------------------------- per-particle work of a step
+    def rk3_stage_dev(self, a: float, b: float, dt: float, Uinf, f: float, g: float, zeta0: float, x, gam, sig,
+                      U, J, M, *, SFS=None, C=None, nu: float | None = None, transposed: bool = True):
+        """One stage of update_particle_states (+ core spreading with nu) on device tensors, in place."""
+        _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(U, 3); _check_dev(J, 9)
+        _check_dev(M, 9)
+        if SFS is not None:
+            _check_dev(SFS, 3); _check_dev(C, 3)
+        ui = (ctypes.c_double * 3)(*[float(v) for v in Uinf])
+        self._torch_stream()
+        self._check(self._L.vpm_rk3_stage_dev(self._h, x.shape[0], float(a), float(b), float(dt), ui, float(f),
+                                              float(g), float(zeta0), -1.0 if nu is None else float(nu),
+                                              TRANSPOSED if transposed else 0, _ptr(x), _ptr(gam), _ptr(sig),
+                                              _ptr(U), _ptr(J), _ptr(SFS), _ptr(C), _ptr(M)))
+
+    def relax_dev(self, rlxf: float, J, gam):
+        """relax_pedrizzetti on device tensors, gam in place."""
+        _check_dev(J, 9); _check_dev(gam, 3)
+        self._torch_stream()
+        self._check(self._L.vpm_relax_dev(self._h, gam.shape[0], float(rlxf), _ptr(J), _ptr(gam)))
+
+    def dynamic_after_dev(self, alpha: float, rlxf: float, minC: float, maxC: float, zeta0: float, gam, sig, J,
+                          SFS, C, M, *, force_positive: bool = True, clip_backscatter: bool = True,
+                          subtract: bool = False, transposed: bool = True):
+        """dynamicprocedure_pseudo3level_afterUJ (+ clipping_backscatter) on device tensors: C and M in place.
+        A NaN coefficient raises FloatingPointError, as the reference's error()."""
+        _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(J, 9); _check_dev(SFS, 3); _check_dev(C, 3)
+        _check_dev(M, 9)
+        flags = ((TRANSPOSED if transposed else 0) | (DYN_FORCE_POSITIVE if force_positive else 0) |
+                 (DYN_CLIP_BACKSCATTER if clip_backscatter else 0) | (DYN_SUBTRACT if subtract else 0))
+        self._torch_stream()
+        rc = self._L.vpm_dynamic_after_dev(self._h, gam.shape[0], float(alpha), float(rlxf), float(minC),
+                                           float(maxC), float(zeta0), flags, _ptr(gam), _ptr(sig), _ptr(J),
+                                           _ptr(SFS), _ptr(C), _ptr(M))
+        if rc == ERR_NONFINITE:
+            raise FloatingPointError("NaN in dynamicprocedure_pseudo3level_afterUJ")
+        self._check(rc)
 
     def zeta_leaflist_dev(self, x, gam, sig, W, *, leaf_size: int = 64, theta: float = 0.4,
                           kernel: int = KERNEL_GAUSSIANERF, precision: int = FP64):

@@ -194,38 +194,12 @@ def _dynamic_fused(fld, ctx, p: DynamicSFSParams):
     fld.M[:, 3:6] = dS
 
 
-def _dynamic_after(fld, p: DynamicSFSParams, zeta0: float, subtract: bool = True):
-    G = fld.gam
-    M = fld.M
-    if subtract:
-        M[:, 0:3] -= _stretch(fld.J, G, fld.transposed)
-        M[:, 3:6] -= fld.SFS
-    s = fld.sig
-    nume = (M[:, 0] * G[:, 0] + M[:, 1] * G[:, 1] + M[:, 2] * G[:, 2]) * (3 * p.alpha - 2)
-    deno = (M[:, 3] * G[:, 0] + M[:, 4] * G[:, 1] + M[:, 5] * G[:, 2]) / (zeta0 / (s * s * s))
-    Cp = fld.C
-    C3 = torch.where(Cp[:, 2] == 0, deno, Cp[:, 2])
-    C3 = torch.where(C3 == 0, torch.full_like(C3, EPS), C3)
-    nume = p.rlxf * nume + (1 - p.rlxf) * Cp[:, 1]
-    deno = p.rlxf * deno + (1 - p.rlxf) * C3
-    ratio = (nume / deno).abs()
-    big = ratio > p.maxC
-    deno = torch.where(big & (deno.abs() < C3.abs()), torch.sign(deno) * C3.abs(), deno)
-    nume = torch.where(big & ((nume / deno).abs() >= p.maxC), torch.sign(nume) * deno.abs() * p.maxC, nume)
-    small = (~big) & (ratio < p.minC)
-    nume = torch.where(small, torch.sign(nume) * deno.abs() * p.minC, nume)
-    C1 = nume / deno
-    if bool(torch.isnan(C1).any()):
-        raise FloatingPointError("NaN in dynamicprocedure_pseudo3level_afterUJ")
-    if p.force_positive:
-        C1 = C1 * torch.sign(C1)
-    Cp[:, 0] = C1
-    Cp[:, 1] = nume
-    Cp[:, 2] = deno
-    M.zero_()
-    if p.clip_backscatter:
-        clip = Cp[:, 0] * (G * fld.SFS).sum(1) < 0
-        Cp[:, 0] = torch.where(clip, Cp[:, 0] * 0, Cp[:, 0])
+def _dynamic_after(fld, ctx, p: DynamicSFSParams, zeta0: float, subtract: bool = True):
+    """dynamicprocedure_pseudo3level_afterUJ + clipping_backscatter (vpm_dynamic_after_dev):
+    with subtract, M holds the test-filter values; otherwise the differences."""
+    ctx.dynamic_after_dev(p.alpha, p.rlxf, p.minC, p.maxC, zeta0, fld.gam, fld.sig, fld.J, fld.SFS, fld.C, fld.M,
+                          force_positive=p.force_positive, clip_backscatter=p.clip_backscatter, subtract=subtract,
+                          transposed=fld.transposed)
 
 
 def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSParams | None = None,
@@ -234,7 +208,6 @@ def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSP
     """One rungekutta3 step (+ relaxation when relax_rlxf is given) of the device state."""
     zeta0 = _zeta0(fld.kernel)
     f, g = fld.f, fld.g
-    Uinf = torch.tensor(Uinf, dtype=torch.float64, device=fld.x.device)
     fld.M.zero_()
     fused = sfs is not None and sfs.fused and fld.precision == _lib.FP32COMP
     for a, b in STAGES:
@@ -245,28 +218,14 @@ def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSP
         if sfs is not None and first:
             if fused:
                 _dynamic_fused(fld, ctx, sfs)
-            _dynamic_after(fld, sfs, zeta0, subtract=not fused)
-        # update_particle_states (src/FLOWVPM_timeintegration.jl:463-532)
-        M, G, s = fld.M, fld.gam, fld.sig
-        C = fld.C[:, 0]
-        S = fld.SFS
-        M[:, 0:3] = a * M[:, 0:3] + dt * (fld.U + Uinf)
-        fld.x += b * M[:, 0:3]
-        MM = _stretch(fld.J, G, fld.transposed)
-        Gn2 = (G * G).sum(1)
-        s3 = s * s * s
-        MM4 = (f + g) / (1 + 3 * f) * (MM * G).sum(1)
-        MM4 = MM4 - f / (1 + 3 * f) * (C * S[:, 0] * G[:, 0] + C * S[:, 1] * G[:, 1] + C * S[:, 2] * G[:, 2]) * s3 / zeta0
-        pos = Gn2 > 0
-        MM4 = torch.where(pos, MM4 / torch.where(pos, Gn2, torch.ones_like(Gn2)), torch.zeros_like(Gn2))
-        M[:, 3:6] = a * M[:, 3:6] + dt * (MM - 3 * MM4[:, None] * G - C[:, None] * S * s3[:, None] / zeta0)
-        M[:, 7] = a * M[:, 7] - dt * (s * MM4)
-        G += b * M[:, 3:6]
-        s += b * M[:, 7]
-        # core spreading (src/FLOWVPM_viscous.jl:175-220)
-        if viscous is not None:
-            M[:, 6] = a * M[:, 6] + dt * 2 * viscous.nu
-            fld.sig.copy_(torch.sqrt(fld.sig ** 2 + b * M[:, 6]))
+            _dynamic_after(fld, ctx, sfs, zeta0, subtract=not fused)
+        # update_particle_states (src/FLOWVPM_timeintegration.jl:463-532) and core spreading's
+        # stage (src/FLOWVPM_viscous.jl:175-192): one fused kernel
+        with_sfs = sfs is not None
+        ctx.rk3_stage_dev(a, b, dt, Uinf, f, g, zeta0, fld.x, fld.gam, fld.sig, fld.U, fld.J, fld.M,
+                          SFS=fld.SFS if with_sfs else None, C=fld.C if with_sfs else None,
+                          nu=viscous.nu if viscous is not None else None, transposed=fld.transposed)
+        if viscous is not None:   # core spreading's growth timer, after the last stage
             if abs(b - 8 / 15) <= 1e-7:
                 viscous.t_sgm += dt
                 beta = math.sqrt(2 * viscous.nu * viscous.t_sgm / viscous.sgm0 ** 2 + 1)
@@ -275,15 +234,9 @@ def rk3_step(fld: DeviceField, dt: float, ctx: _lib.Context, *, sfs: DynamicSFSP
                     fld.sig.fill_(viscous.sgm0)
                     rbf_conjugategradient(fld, ctx, target, viscous)
                     viscous.t_sgm = 0.0
-    if relax_rlxf is not None:
+    if relax_rlxf is not None:   # relax_pedrizzetti (src/FLOWVPM_relaxation.jl:62-81)
         uj(fld, ctx)
-        J = fld.J
-        w = torch.stack([J[:, 5] - J[:, 7], J[:, 6] - J[:, 2], J[:, 1] - J[:, 3]], dim=1)
-        nw = torch.sqrt((w * w).sum(1))
-        nG = torch.sqrt((fld.gam * fld.gam).sum(1))
-        ok = nw != 0
-        newg = (1 - relax_rlxf) * fld.gam + relax_rlxf * (nG / torch.where(ok, nw, torch.ones_like(nw)))[:, None] * w
-        fld.gam.copy_(torch.where(ok[:, None], newg, fld.gam))
+        ctx.relax_dev(relax_rlxf, fld.J, fld.gam)
     fld.t += dt
     fld.nt += 1
 

@@ -79,6 +79,14 @@ enum {
     VPM_CHECK_FINITE = 16 /* scan outputs for NaN/Inf and return VPM_ERR_NONFINITE */
 };
 
+/* flags of vpm_dynamic_after_dev (with VPM_TRANSPOSED), the settings of
+ * DynamicSFS (src/FLOWVPM_subfilterscale.jl:204-268) */
+enum {
+    VPM_DYN_FORCE_POSITIVE   = 32,  /* force_positive: C = |C| */
+    VPM_DYN_CLIP_BACKSCATTER = 64,  /* clipping_backscatter: C = 0 where C Gamma . SFS < 0 */
+    VPM_DYN_SUBTRACT         = 128  /* M holds the test-filter values: subtract S(J) and SFS first */
+};
+
 /* Work per pair used for all throughput and roofline figures (flop: add, sub,
  * mul = 1, fma = 2; sqrt/exp/erf/reciprocals counted separately). */
 #define VPM_FLOP_PER_UJ_PAIR   74
@@ -181,6 +189,37 @@ int vpm_uj_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* g
 int vpm_dynamic_diff_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
                          const double* J, double alpha, double* dJ, double* dSFS, int kernel, int precision,
                          int flags);
+
+/* ------------------------------------------ per-particle work of a step */
+/* The per-particle work of the rVPM RK3 step on device arrays (x, gam, U, SFS,
+ * C [n,3]; J, M [n,9], J column-major 3x3 per particle; sig [n]), one fused
+ * FP64 kernel each, in the reference's operation order.
+ *
+ * vpm_rk3_stage_dev: one stage (a, b) of update_particle_states
+ * (src/FLOWVPM_timeintegration.jl:463-532) for ReformulatedVPM(f, g): M[0:3],
+ * x from U + Uinf; M[3:6], gam from the stretching of J (flags: VPM_TRANSPOSED)
+ * and, when SFS is given, the SFS term C[:,0] SFS sigma^3/zeta0 (C may then not
+ * be NULL); M[7], sig.  nu >= 0 adds core spreading's stage
+ * (src/FLOWVPM_viscous.jl:175-192): M[6] and sig = sqrt(sig^2 + b M[6]).
+ * Uinf is a host array of 3.  No counterpart call in the reference (its loop). */
+int vpm_rk3_stage_dev(vpm_ctx* ctx, int64_t n, double a, double b, double dt, const double* Uinf, double f,
+                      double g, double zeta0, double nu, int flags, double* x, double* gam, double* sig,
+                      const double* U, const double* J, const double* SFS, const double* C, double* M);
+
+/* relax_pedrizzetti (src/FLOWVPM_relaxation.jl:62-81): gam = (1 - rlxf) gam +
+ * rlxf |gam| w/|w|, w the vorticity of J, where |w| > 0. */
+int vpm_relax_dev(vpm_ctx* ctx, int64_t n, double rlxf, const double* J, double* gam);
+
+/* dynamicprocedure_pseudo3level_afterUJ (src/FLOWVPM_subfilterscale.jl:541-673)
+ * with clipping_backscatter (:287-296): from the test-filter differences in
+ * M[0:6] (or, with VPM_DYN_SUBTRACT, from the test-filter values there minus
+ * the stretching of J and SFS) the coefficients C[:,0:3] are updated with
+ * Lagrangian averaging (rlxf) and the bounds [minC, maxC]; M is zeroed.
+ * flags: VPM_TRANSPOSED, VPM_DYN_*.  A NaN coefficient returns
+ * VPM_ERR_NONFINITE (the reference's error()). */
+int vpm_dynamic_after_dev(vpm_ctx* ctx, int64_t n, double alpha, double rlxf, double minC, double maxC,
+                          double zeta0, int flags, const double* gam, const double* sig, const double* J,
+                          const double* SFS, double* C, double* M);
 
 /* zeta_direct(pfield) (src/FLOWVPM_viscous.jl:467-488), the RBF basis field of
  * core spreading: rows 16:18 (J[1:3]) of every particle, statics included, are

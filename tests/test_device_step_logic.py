@@ -29,6 +29,74 @@ class OracleCtx:
         SFS += torch.from_numpy(S)
 
 
+    # the per-particle kernels of the step (csrc/step.cu), restated on CPU tensors in the
+    # reference's operation order (src/FLOWVPM_timeintegration.jl:463-532,
+    # src/FLOWVPM_viscous.jl:175-192, src/FLOWVPM_relaxation.jl:62-81,
+    # src/FLOWVPM_subfilterscale.jl:541-673 and :287-296)
+    def rk3_stage_dev(self, a, b, dt, Uinf, f, g, zeta0, x, gam, sig, U, J, M, *, SFS=None, C=None, nu=None,
+                      transposed=True):
+        from vpm_gb300.autodiff import _stretch
+        G, s = gam, sig
+        Cc = C[:, 0] if C is not None else torch.zeros_like(s)
+        S = SFS if SFS is not None else torch.zeros_like(G)
+        M[:, 0:3] = a * M[:, 0:3] + dt * (U + torch.tensor(Uinf, dtype=torch.float64))
+        x += b * M[:, 0:3]
+        MM = _stretch(J, G, transposed)
+        Gn2 = (G * G).sum(1)
+        s3 = s * s * s
+        MM4 = (f + g) / (1 + 3 * f) * (MM * G).sum(1)
+        MM4 = MM4 - f / (1 + 3 * f) * (Cc * S[:, 0] * G[:, 0] + Cc * S[:, 1] * G[:, 1] + Cc * S[:, 2] * G[:, 2]) * \
+            s3 / zeta0
+        pos = Gn2 > 0
+        MM4 = torch.where(pos, MM4 / torch.where(pos, Gn2, torch.ones_like(Gn2)), torch.zeros_like(Gn2))
+        M[:, 3:6] = a * M[:, 3:6] + dt * (MM - 3 * MM4[:, None] * G - Cc[:, None] * S * s3[:, None] / zeta0)
+        M[:, 7] = a * M[:, 7] - dt * (s * MM4)
+        G += b * M[:, 3:6]
+        s += b * M[:, 7]
+        if nu is not None:
+            M[:, 6] = a * M[:, 6] + dt * 2 * nu
+            sig.copy_(torch.sqrt(sig ** 2 + b * M[:, 6]))
+
+    def relax_dev(self, rlxf, J, gam):
+        w = torch.stack([J[:, 5] - J[:, 7], J[:, 6] - J[:, 2], J[:, 1] - J[:, 3]], dim=1)
+        nw = torch.sqrt((w * w).sum(1))
+        nG = torch.sqrt((gam * gam).sum(1))
+        ok = nw != 0
+        newg = (1 - rlxf) * gam + rlxf * (nG / torch.where(ok, nw, torch.ones_like(nw)))[:, None] * w
+        gam.copy_(torch.where(ok[:, None], newg, gam))
+
+    def dynamic_after_dev(self, alpha, rlxf, minC, maxC, zeta0, G, s, J, SFS, Cp, M, *, force_positive=True,
+                          clip_backscatter=True, subtract=False, transposed=True):
+        from vpm_gb300.autodiff import _stretch
+        if subtract:
+            M[:, 0:3] -= _stretch(J, G, transposed)
+            M[:, 3:6] -= SFS
+        nume = (M[:, 0] * G[:, 0] + M[:, 1] * G[:, 1] + M[:, 2] * G[:, 2]) * (3 * alpha - 2)
+        deno = (M[:, 3] * G[:, 0] + M[:, 4] * G[:, 1] + M[:, 5] * G[:, 2]) / (zeta0 / (s * s * s))
+        C3 = torch.where(Cp[:, 2] == 0, deno, Cp[:, 2])
+        C3 = torch.where(C3 == 0, torch.full_like(C3, ds.EPS), C3)
+        nume = rlxf * nume + (1 - rlxf) * Cp[:, 1]
+        deno = rlxf * deno + (1 - rlxf) * C3
+        ratio = (nume / deno).abs()
+        big = ratio > maxC
+        deno = torch.where(big & (deno.abs() < C3.abs()), torch.sign(deno) * C3.abs(), deno)
+        nume = torch.where(big & ((nume / deno).abs() >= maxC), torch.sign(nume) * deno.abs() * maxC, nume)
+        small = (~big) & (ratio < minC)
+        nume = torch.where(small, torch.sign(nume) * deno.abs() * minC, nume)
+        C1 = nume / deno
+        if bool(torch.isnan(C1).any()):
+            raise FloatingPointError("NaN in dynamicprocedure_pseudo3level_afterUJ")
+        if force_positive:
+            C1 = C1 * torch.sign(C1)
+        Cp[:, 0] = C1
+        Cp[:, 1] = nume
+        Cp[:, 2] = deno
+        M.zero_()
+        if clip_backscatter:
+            clip = Cp[:, 0] * (G * SFS).sum(1) < 0
+            Cp[:, 0] = torch.where(clip, Cp[:, 0] * 0, Cp[:, 0])
+
+
 class OracleZetaCtx(OracleCtx):
     def zeta_dev(self, xt, xs, gs, sgs, W, kernel, precision):
         W += torch.from_numpy(oracle.zeta_pairs(xt.numpy(), xs.numpy(), gs.numpy(), sgs.numpy(), kernel))

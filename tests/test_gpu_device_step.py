@@ -229,3 +229,46 @@ def test_nearfield_core_size_reset_theta_zero_equals_all_pairs(ctx):
     for name in ("x", "gam", "sig"):
         ta, tb = getattr(a, name), getattr(b, name)
         assert normwise(tb.cpu().numpy(), ta.cpu().numpy())[0] <= 1e-11, name
+
+
+@pytest.mark.parametrize("transposed", [True, False])
+def test_step_kernels_match_their_restatement(ctx, transposed):
+    """vpm_rk3_stage_dev, vpm_relax_dev and vpm_dynamic_after_dev against the torch
+    restatement of the same arithmetic (the CPU stand-in of tests/test_device_step_logic.py)
+    on random states: the same values to FP64 rounding."""
+    import torch
+    from test_device_step_logic import OracleCtx
+    ref = OracleCtx()
+    rng = np.random.default_rng(11 + int(transposed))
+    n = 3000
+    r = lambda *sh: rng.normal(size=sh)
+    st = dict(x=r(n, 3), gam=r(n, 3) * 1e-2, sig=rng.uniform(0.01, 0.05, n), U=r(n, 3), J=r(n, 9), SFS=r(n, 3),
+              C=r(n, 3) * 1e-3, M=r(n, 9) * 1e-3)
+    st["gam"][:7] = 0.0                         # |Gamma| = 0: the stretching split is skipped
+    st["C"][::5, 2] = 0.0                       # no earlier denominator
+    st["J"][3, 5] = st["J"][3, 7]; st["J"][3, 6] = st["J"][3, 2]; st["J"][3, 1] = st["J"][3, 3]   # w = 0
+    cpu = {k: torch.tensor(v) for k, v in st.items()}
+    dev = {k: torch.tensor(v, device="cuda") for k, v in st.items()}
+    for a, b in ((0.0, 1 / 3), (-5 / 9, 15 / 16), (-153 / 128, 8 / 15)):
+        for side, c in ((cpu, ref), (dev, ctx)):
+            c.rk3_stage_dev(a, b, 0.01, (0.1, -0.2, 0.3), 0.0, 0.2, 0.8, side["x"], side["gam"], side["sig"],
+                            side["U"], side["J"], side["M"], SFS=side["SFS"], C=side["C"], nu=1e-3,
+                            transposed=transposed)
+    for side, c in ((cpu, ref), (dev, ctx)):
+        c.relax_dev(0.3, side["J"], side["gam"])
+        side["M"][:, 0:6] += 1e-4
+        c.dynamic_after_dev(0.999, 0.005, 0.0, 1.0, 0.8, side["gam"], side["sig"], side["J"], side["SFS"], side["C"],
+                            side["M"], subtract=True, transposed=transposed)
+    for k in ("x", "gam", "sig", "C", "M"):
+        e = normwise(dev[k].cpu().numpy(), cpu[k].numpy())[0]
+        assert e <= 1e-13, (k, e)
+    assert (dev["M"] == 0).all()
+
+
+def test_dynamic_after_rejects_bad_bounds(ctx):
+    """The reference's error cases of the C bounds (src/FLOWVPM_subfilterscale.jl:549-556)."""
+    import torch
+    z = lambda k: torch.zeros(10, k, dtype=torch.float64, device="cuda")
+    for lo, hi in ((-0.1, 1.0), (0.0, -1.0), (0.5, 0.1)):
+        with pytest.raises(vpm._lib.VPMError, match="Invalid C bounds"):
+            ctx.dynamic_after_dev(0.999, 0.005, lo, hi, 0.8, z(3), z(1)[:, 0] + 0.05, z(9), z(3), z(3), z(9))
