@@ -38,6 +38,13 @@ for p in (ROOT, os.path.join(ROOT, "flowvpm.jl_gb300")):
 N_PARTICLES = 1 << 20
 KERNEL = 2            # gaussianerf
 FLOP_PER_PAIR = 74    # VPM_FLOP_PER_UJ_PAIR
+# DRAM bytes of one uj_mixed_kernel<gaussianerf> launch at N = 2^20, measured by ncu
+# (`ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#  --clock-control none -k regex:uj_mixed_kernel -c 1 python bench.py --kernel-only --n 1048576
+#  --warmup 0 --steps 1`): 394,715,392 read + 153,797,376 written.  The compulsory traffic is
+# ~0.16 GB (56 B in, 96 B out a particle); the rest is re-reads of the 50 MB source pack that
+# miss L2.  Either way it is ~0.35 GB/s over the 1.55 s launch: the kernel is FP32-bound.
+UJ_DRAM_BYTES_2P20 = 394_715_392 + 153_797_376
 # the headline metric as the reference's benchmark definition names it; `value` is the
 # FP32-comp rate, `fp64_gpu` / `mixed_over_fp64` and `adjoint` carry the other two parts
 METRIC = "UJ pair-interactions/s, FP32-comp vs FP64 GPU @≤1e-6 rel err; adjoint/fwd ratio"
@@ -292,7 +299,11 @@ def run_gpu(args, rank, world):
                     "d2h_bytes_per_step": 12 * 8 * n, "ms_per_step": 1e3 * statistics.mean(e2e_times),
                     "call": "vpm_uj(ctx, host 46xN matrix, RESET) = UJ_gb300_mixed(pfield)"},
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops,
-                         "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved_tflops / peak_tflops,
+                         "traffic": UJ_DRAM_BYTES_2P20 if n == 1 << 20 else None,
+                         "traffic_unit": "bytes per launch",
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one N=2^20 launch "
+                                           "(394.7 + 153.8 MB; 1 pass, --clock-control none)",
                          "kernel": "uj_mixed_kernel<gaussianerf>",
                          "flop_per_pair": FLOP_PER_PAIR,
                          "peak_source": "FFMA-loop kernel measured in this run (no FP32 figure in "
@@ -400,25 +411,39 @@ def measure_ffma_peak(ctx) -> float:
 
 
 def run_kernel_only(args):
-    """Profiling helper: only the UJ (or Estr) kernels on an n-particle cloud,
-    `warmup` + `steps` evaluations, no other work (for ncu captures)."""
+    """Profiling helper: only the UJ (or Estr, or with --adjoint the UJ adjoint)
+    kernels on an n-particle cloud -- for --adjoint, the 32,000-particle ring of
+    the rollout workload -- `warmup` + `steps` evaluations, no other work (for
+    ncu captures)."""
     import torch
     import vpm_gb300 as vpm
     n = args.n
     prec = vpm.FP64 if args.precision == "fp64" else vpm.FP32COMP
     kern = {"singular": 0, "gaussian": 1, "gaussianerf": 2, "winckelmans": 3}[args.kernel]
     ctx = vpm.Context(0)
-    X, G, s = random_cloud(n, seed=1)
+    if args.adjoint:
+        import vpm_gb300.rings as rings
+        X, G, s, _ = rings.ring_sections(1.0, 1.0, 0.1, 1000, 32, 0.05)
+        n = X.shape[0]
+    else:
+        X, G, s = random_cloud(n, seed=1)
     d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
     xt, gs, sg = d(X), d(G), d(s)
     U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
     J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
     SFS = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    if args.adjoint:   # cotangents of U and J: seeded, O(1)
+        rng = np.random.default_rng(7)
+        U.copy_(torch.from_numpy(rng.normal(size=(n, 3))))
+        J.copy_(torch.from_numpy(rng.normal(size=(n, 9))))
+        xb, gb, sb = torch.zeros_like(xt), torch.zeros_like(gs), torch.zeros_like(sg)
     times = []
     for k in range(args.warmup + args.steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        if args.estr:
+        if args.adjoint:
+            ctx.uj_adjoint_dev(xt, gs, sg, U, J, xb, gb, sb, kern, prec)
+        elif args.estr:
             ctx.estr_dev(xt, J, xt, gs, sg, J, SFS, kern, prec, True)
         else:
             ctx.uj_dev(xt, xt, gs, sg, U, J, kern, prec)
@@ -428,7 +453,8 @@ def run_kernel_only(args):
             times.append(a.elapsed_time(b))
     ms = statistics.mean(times) if times else float("nan")
     print(json.dumps({"mode": "kernel-only", "n": n, "precision": args.precision, "kernel": args.kernel,
-                      "estr": bool(args.estr), "ms": ms, "pairs_per_s": n * n / (ms / 1e3),
+                      "estr": bool(args.estr), "adjoint": bool(args.adjoint), "ms": ms,
+                      "pairs_per_s": n * n / (ms / 1e3),
                       "launches": ctx.launches}))
 
 
@@ -733,6 +759,7 @@ def main():
     ap.add_argument("--kernel", default="gaussianerf", choices=["singular", "gaussian", "gaussianerf", "winckelmans"])
     ap.add_argument("--estr", action="store_true")
     ap.add_argument("--jet-call", default="uj", choices=["uj", "dynamic"])
+    ap.add_argument("--adjoint", action="store_true")
     # the other workloads (one JSON line each, not the bench line)
     ap.add_argument("--workload", default="cloud", choices=["cloud", "leapfrog", "jet", "rollout"])
     ap.add_argument("--lf-n", type=int, default=200_000)

@@ -289,6 +289,71 @@ __device__ __forceinline__ void adj_coeffs_f32(float s, float& G, float& H, floa
     }
 }
 
+// adj_coeffs_f32 for four pairs of one lane with the forms chosen for the whole
+// warp, so that the four pairs' chains interleave: the singular form for all
+// four, then (Gaussian-erf) the s >= 6 form where any lane of the warp has such a
+// pair within the kernel's reach and the series where any has s < 6, each kept
+// per pair by its range.  s must be positive and finite (callers pass 1 for
+// pairs that contribute nothing).  All 32 lanes must call it.
+template <int K>
+__device__ __forceinline__ void adj_coeffs4_f32(const float (&s)[4], float (&G)[4], float (&H)[4], float (&Kc)[4],
+                                                float (&a)[4], float (&b)[4])
+{
+    if constexpr (K == K_GAUSERF) {
+        float rs[4], rs2[4];
+        bool anyser = false, anymid = false;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            rs[q] = rsqrtf(s[q]);
+            rs2[q] = rs[q] * rs[q];
+            G[q] = rs[q] * rs2[q];
+            H[q] = -3.0f * G[q] * rs2[q];
+            Kc[q] = -5.0f * H[q] * rs2[q];
+            a[q] = 0.0f;
+            b[q] = 0.0f;
+            anyser = anyser || s[q] < S_SERIES_ADJ;
+            anymid = anymid || (s[q] >= S_SERIES_ADJ && s[q] <= S_FAR_GERF);
+        }
+        anyser = __any_sync(0xffffffffu, anyser);
+        anymid = __any_sync(0xffffffffu, anymid);
+        if (!anyser && !anymid) return;
+        float e[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            e[q] = exp2f(s[q] * -0.72134752044448170f);
+            const bool near = s[q] <= S_FAR_GERF;
+            a[q] = near ? F_C2 * e[q] : 0.0f;
+            b[q] = a[q];
+        }
+        if (anymid) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float g = gerf_G_erfcx(s[q], e[q], rs[q]);
+                const float h = (a[q] - 3.0f * g) * rs2[q];
+                const float k = fmaf(15.0f, g, -a[q] * (5.0f + s[q])) * rs2[q] * rs2[q];
+                const bool mid = s[q] >= S_SERIES_ADJ && s[q] <= S_FAR_GERF;
+                G[q] = mid ? g : G[q];
+                H[q] = mid ? h : H[q];
+                Kc[q] = mid ? k : Kc[q];
+            }
+        }
+        if (anyser) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float p3 = gerf_S3_series(s[q]);
+                const float p2 = fmaf(s[q], p3, 0.066666666666666667f);
+                const bool ser = s[q] < S_SERIES_ADJ;
+                G[q] = ser ? a[q] * fmaf(s[q], p2, 0.33333333333333333f) : G[q];
+                H[q] = ser ? -3.0f * a[q] * p2 : H[q];
+                Kc[q] = ser ? 15.0f * a[q] * p3 : Kc[q];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) adj_coeffs_f32<K>(s[q], G[q], H[q], Kc[q], a[q], b[q]);
+    }
+}
+
 // The seven derivatives of phi for one pair in FP32 (o[0..2] d/d(dx), o[3..5]
 // d/dGamma, o[6] d/dsigma), from the coefficients of the pair.
 __device__ __forceinline__ void adj_pair_f32(float dx, float dy, float dz, float Gx, float Gy, float Gz, float A,
@@ -412,53 +477,70 @@ uj_adjoint_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double
                 far = far && r2[q] > h.w;
             }
             const bool allfar = __all_sync(0xffffffffu, far);
+            float ex[4], ey[4], ez[4], i2[4], sq[4];
+            bool on[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const SrcAdjMixed& sp = tile[j0 + q];
+                ex[q] = dx[q]; ey[q] = dy[q]; ez[q] = dz[q];
+                float e2 = r2[q];
+                if (!allfar) {   // double-float displacement
+                    ex[q] = (th.x - sp.a.x) + (tl.x - sp.b.x);
+                    ey[q] = (th.y - sp.a.y) + (tl.y - sp.b.y);
+                    ez[q] = (th.z - sp.a.z) + (tl.z - sp.b.z);
+                    e2 = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+                }
+                on[q] = valid && e2 > 0.0f;
+                i2[q] = sp.a.w * sp.a.w;
+                sq[q] = on[q] ? e2 * i2[q] : 1.0f;
+            }
+            float G[4], H[4], Kc[4], ca[4], cb[4];
+            if (allfar) {   // singular form (no sigma derivative)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float rs = rsqrtf(sq[q]), rs2 = rs * rs;
+                    G[q] = rs * rs2; H[q] = -3.0f * G[q] * rs2; Kc[q] = -5.0f * H[q] * rs2; ca[q] = 0.0f; cb[q] = 0.0f;
+                }
+            } else {
+                adj_coeffs4_f32<K>(sq, G, H, Kc, ca, cb);
+            }
+            float o[4][7];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const SrcAdjMixed& sp = tile[j0 + q];
                 const float isig = sp.a.w;
-                float ex = dx[q], ey = dy[q], ez = dz[q], e2 = r2[q];
-                if (!allfar) {   // double-float displacement
-                    ex = (th.x - sp.a.x) + (tl.x - sp.b.x);
-                    ey = (th.y - sp.a.y) + (tl.y - sp.b.y);
-                    ez = (th.z - sp.a.z) + (tl.z - sp.b.z);
-                    e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                }
-                float o[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                if (e2 > 0.0f) {
-                    const float i2 = isig * isig;
-                    const float s = e2 * i2;
-                    float G, H, Kc, a, b;
-                    if (allfar) {   // singular form (no sigma derivative)
-                        const float rs = rsqrtf(s), rs2 = rs * rs;
-                        G = rs * rs2; H = -3.0f * G * rs2; Kc = -5.0f * H * rs2; a = 0.0f; b = 0.0f;
-                    } else {
-                        adj_coeffs_f32<K>(s, G, H, Kc, a, b);
-                    }
-                    const float i3 = i2 * isig;
-                    const float A = -F_C4 * i3 * G;
-                    const float B = -F_C4 * i3 * i2 * H;
-                    const float Bpr = -F_C4 * i3 * i2 * i2 * Kc;
-                    const float dA = F_C4 * i2 * i2 * a;
-                    const float dB = -F_C4 * i3 * i3 * b;
-                    adj_pair_f32(ex, ey, ez, sp.g.x, sp.g.y, sp.g.z, A, B, Bpr, dA, dB, Ub, Jb, wb, o);
-                }
-                if (!valid) {
+                const float w = on[q] ? 1.0f : 0.0f;
+                const float i3 = i2[q] * isig;
+                const float A = -F_C4 * i3 * G[q] * w;
+                const float B = -F_C4 * i3 * i2[q] * H[q] * w;
+                const float Bpr = -F_C4 * i3 * i2[q] * i2[q] * Kc[q] * w;
+                const float dA = F_C4 * i2[q] * i2[q] * ca[q] * w;
+                const float dB = -F_C4 * i3 * i3 * cb[q] * w;
 #pragma unroll
-                    for (int k = 0; k < 7; k++) o[k] = 0.f;
-                }
-                acc[0] += o[0]; acc[1] += o[1]; acc[2] += o[2];
-                o[0] = -o[0]; o[1] = -o[1]; o[2] = -o[2];
+                for (int k = 0; k < 7; k++) o[q][k] = 0.f;
+                adj_pair_f32(ex[q], ey[q], ez[q], sp.g.x, sp.g.y, sp.g.z, A, B, Bpr, dA, dB, Ub, Jb, wb, o[q]);
+                acc[0] += o[q][0]; acc[1] += o[q][1]; acc[2] += o[q][2];
+                o[q][0] = -o[q][0]; o[q][1] = -o[q][1]; o[q][2] = -o[q][2];
+            }
+            // source-side sums of the four sources over the warp's 32 targets, by reduce-scatter:
+            // lanes 16-31 / 0-15 keep sources {2,3} / {0,1}, then lanes with bit 3 set / clear
+            // keep the odd / even one, then a butterfly over the remaining 8 lanes; lane 8 g
+            // ends with source g's seven sums (21 + 21 shuffles per four sources, not 4 x 35)
+            const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+            float r[7];
 #pragma unroll
-                for (int k = 0; k < 7; k++) {
-                    float v = o[k];
+            for (int k = 0; k < 7; k++) {
+                const float p0 = (b4 ? o[2][k] : o[0][k]) + __shfl_xor_sync(0xffffffffu, b4 ? o[0][k] : o[2][k], 16);
+                const float p1 = (b4 ? o[3][k] : o[1][k]) + __shfl_xor_sync(0xffffffffu, b4 ? o[1][k] : o[3][k], 16);
+                float v = (b3 ? p1 : p0) + __shfl_xor_sync(0xffffffffu, b3 ? p0 : p1, 8);
 #pragma unroll
-                    for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-                    o[k] = v;
-                }
-                if (lane == 0) {
+                for (int m = 4; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+                r[k] = v;
+            }
+            if ((lane & 7) == 0) {
+                const int q = (b4 ? 2 : 0) + (b3 ? 1 : 0);
 #pragma unroll
-                    for (int k = 0; k < 7; k++) red[warp][j0 + q][k] = o[k];
-                }
+                for (int k = 0; k < 7; k++) red[warp][j0 + q][k] = r[k];
             }
             if ((j0 & 63) == 60) {
 #pragma unroll

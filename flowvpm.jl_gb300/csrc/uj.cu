@@ -232,7 +232,10 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 constexpr int WT = 32;                      // sources per warp tile (one per lane)
 constexpr int BLOCK_TILES = UJ_BLOCK / WT;  // warp tiles per FP32 block
-constexpr int MID_BLOCKS = 4;               // FP32 blocks per FP32 mid-level sum
+#ifndef VPM_UJ_MID_BLOCKS
+#define VPM_UJ_MID_BLOCKS 4                 // FP32 blocks per FP32 mid-level sum
+#endif
+constexpr int MID_BLOCKS = VPM_UJ_MID_BLOCKS;
 #ifndef VPM_UJ_MIN_BLOCKS
 #define VPM_UJ_MIN_BLOCKS 5                 // resident blocks per SM the register budget targets
 #endif
