@@ -179,6 +179,15 @@ def run_reference(args, rank, world):
         times.append(time.perf_counter() - t0)
     pairs = nt * N_PARTICLES
     value = pairs * len(times) / sum(times)
+    # the small configuration in full: all pairs of a 2^14 cloud, median of 5 after one warm-up
+    Xs, Gs, ss = random_cloud(1 << 14, seed=0)
+    oracle.uj_pairs(Xs, Xs, Gs, ss, KERNEL)
+    small = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        oracle.uj_pairs(Xs, Xs, Gs, ss, KERNEL)
+        small.append(time.perf_counter() - t0)
+    small_rate = float(1 << 28) / statistics.median(small)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -187,6 +196,8 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
                              "sample": f"{nt} targets x {N_PARTICLES} sources per step, {args.steps} steps"},
             "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "n_2p14_all_pairs": {"value": small_rate, "unit": "pairs/s", "ms": 1e3 * statistics.median(small),
+                                 "note": "all 2^28 pairs of a 2^14 cloud, median of 5"},
             "note": "oracle port (oracle/vpm_oracle.c) of UJ_direct's pair loop: the reference (Julia + "
                     "FastMultipole.jl) cannot be installed in this environment"}
     print(json.dumps(line), flush=True)
@@ -283,6 +294,7 @@ def run_gpu(args, rank, world):
                "J_rms_rel": float(np.linalg.norm(Jh - Jr) / np.linalg.norm(Jr)),
                "targets_checked": 256}
         fp64 = fp64_rate(ctx, vpm, torch)
+        wnk = winckelmans_rate(ctx, vpm, torch, X, G, s)
         adjoint = adjoint_ratio(ctx, vpm, torch)
         base = cpu_baseline(X, G, s)
         mp = measured_peaks()
@@ -314,6 +326,7 @@ def run_gpu(args, rank, world):
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "fp64_gpu": fp64,
+            "winckelmans": wnk,
             "mixed_over_fp64": value / fp64["value"] if fp64 else None,
             "adjoint": adjoint,
             "error_vs_oracle": err,
@@ -344,6 +357,35 @@ def fp64_rate(ctx, vpm, torch):
     ms = a.elapsed_time(b)
     return {"value": float(n) * n / (ms / 1e3), "unit": "pairs/s", "n_particles": n, "ms": ms,
             "kernel": "uj_f64_kernel<gaussianerf>"}
+
+
+def winckelmans_rate(ctx, vpm, torch, X, G, s):
+    """The same cloud with the Winckelmans kernel, FP32-comp: one timed
+    evaluation and its error against the oracle on 256 seeded targets."""
+    import oracle
+    n = X.shape[0]
+    d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
+    xt, gs, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    ctx.uj_dev(xt[:4096], xt, gs, sg, U[:4096], J[:4096], vpm._lib.KERNEL_WINCKELMANS, vpm.FP32COMP)
+    U.zero_()
+    J.zero_()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    ctx.uj_dev(xt, xt, gs, sg, U, J, vpm._lib.KERNEL_WINCKELMANS, vpm.FP32COMP)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    sub = np.sort(np.random.default_rng(6).choice(n, 256, replace=False))
+    Ur, Jr = oracle.uj_pairs(X[sub], X, G, s, vpm._lib.KERNEL_WINCKELMANS)
+    Uh, Jh = U.cpu().numpy()[sub], J.cpu().numpy()[sub]
+    return {"value": float(n) * n / (ms / 1e3), "unit": "pairs/s", "n_particles": n, "ms": ms,
+            "kernel": "uj_mixed_kernel<winckelmans>",
+            "error_vs_oracle": {"U_max_rel": float(np.abs(Uh - Ur).max() / np.abs(Ur).max()),
+                                "J_max_rel": float(np.abs(Jh - Jr).max() / np.abs(Jr).max()),
+                                "targets_checked": 256}}
 
 
 def adjoint_ratio(ctx, vpm, torch, n=32000):
