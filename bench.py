@@ -554,7 +554,9 @@ def run_leapfrog(args):
     ctx = vpm.Context(0)
     dt = 0.005
     out = {"mode": "leapfrog", "steps": args.lf_steps, "dt": dt, "precision": "fp32comp"}
-    uj_per_step, estr_per_step = 5, 4     # dynamic SFS: test-filter UJ + 3 stages (with Estr), relaxation UJ
+    # pair passes per FP32-comp step: 3 stage UJ + Estr, the relaxation UJ, and the dynamic
+    # procedure's differences (one filter-difference pass over the J term, two Estr passes)
+    uj_per_step, estr_per_step = 5, 5
     if args.lf_n > 0:
         X, G, s = workloads.leapfrog_rings(args.lf_n, nper=10)
         n = X.shape[0]

@@ -14,6 +14,12 @@
 * `Uring` (vortexrings_functions.jl:47) and `calc_rings_weighted`
   (:275-315) are the reference's analytic ring speed and strength-weighted ring
   centroid / radius.
+* `analytic_coaxialrings` restates the reference's reference solution for
+  coaxial rings (examples/vortexrings/vortexrings_postprocessing.jl:110-320):
+  the thin-ring ODEs of Borisov, Kilin & Mamaev (2013), "The dynamics of vortex
+  rings: leapfrogging, choreographies and the stability problem", integrated
+  by forward Euler with its step, its one-sided differences of the stream
+  function and its elliptic integrals K(k), E(k) of parameter k^2.
 """
 from __future__ import annotations
 
@@ -129,3 +135,54 @@ def calc_rings_weighted(pfield: ParticleField, intervals):
         sg = (nG * s[sl]).sum() / tot
         out.append((Z, Rr, sg))
     return out
+
+
+def _stream_G(z, r, zt, rt):
+    """Stokes stream function of a thin ring of unit circulation at (zt, rt),
+    evaluated at (z, r) (vortexrings_postprocessing.jl:308-314)."""
+    from scipy.special import ellipe, ellipk
+    k = math.sqrt(4 * r * rt / ((z - zt) ** 2 + (r + rt) ** 2))
+    return math.sqrt(r * rt) / (2 * math.pi) * ((2 / k - k) * ellipk(k * k) - 2 / k * ellipe(k * k))
+
+
+def analytic_coaxialrings(Gammas, Rs, Zs, As, Deltas, *, tend: float, dtmax: float = 1e-3,
+                          dynamica: bool = True):
+    """Radii and centroids of coaxial thin rings at time tend (and every step):
+    dZ_i/dt = Gamma_i/(4 pi R_i) (ln(8 R_i/a_i) - 1/2 + Delta_i) + 1/R_i sum_j Gamma_j dG/dR_i,
+    dR_i/dt = -1/R_i sum_j Gamma_j dG/dZ_i,   da_i/dt = -a_i/(2 R_i) dR_i/dt (dynamica),
+    by forward Euler with step dtmax/10 and the last step cut to end at tend;
+    dG/d. by forward differences with h = 1e-5.  Returns (t, R[nt, nrings], Z[nt, nrings])."""
+    h = 1e-5
+    nr = len(Rs)
+    R = np.array(Rs, dtype=np.float64)
+    Z = np.array(Zs, dtype=np.float64)
+    a = np.array(As, dtype=np.float64)
+    Gam = np.array(Gammas, dtype=np.float64)
+    Dl = np.array(Deltas, dtype=np.float64)
+    dt = dtmax / 10
+    t = list(np.arange(0.0, tend + dt / 2, dt))      # the range (0 : dt : tend)
+    if t[-1] > tend:
+        t.pop()
+    if t[-1] != tend:
+        t.append(tend)
+    Rh, Zh = [R.copy()], [Z.copy()]
+    for k in range(1, len(t)):
+        step = t[k] - t[k - 1]
+        dR = np.zeros(nr)
+        dZ = Gam / (4 * math.pi * R) * (np.log(8 * R / a) - 0.5 + Dl)
+        for i in range(nr):
+            for j in range(nr):
+                if i == j:
+                    continue
+                g0 = _stream_G(Z[i], R[i], Z[j], R[j])
+                dGdZ = (_stream_G(Z[i] + h, R[i], Z[j], R[j]) - g0) / h
+                dGdR = (_stream_G(Z[i], R[i] + h, Z[j], R[j]) - g0) / h
+                dR[i] -= 1 / R[i] * Gam[j] * dGdZ
+                dZ[i] += 1 / R[i] * Gam[j] * dGdR
+        da = -a / (2 * R) * dR if dynamica else np.zeros(nr)
+        R = R + dR * step
+        Z = Z + dZ * step
+        a = a + da * step
+        Rh.append(R.copy())
+        Zh.append(Z.copy())
+    return np.array(t), np.array(Rh), np.array(Zh)

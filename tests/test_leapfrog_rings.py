@@ -1,0 +1,83 @@
+"""The reference's leapfrog verification (test/runtests_leapfrog.jl:21-171):
+two coaxial thin rings (R = 0.7906, 0.7906 apart, circulation 1, cross-section
+radius 0.1 R = sigma, 100 cross sections with one particle each, the
+Winckelmans kernel, corrected-Pedrizzetti relaxation every step) run for 350
+RK3 steps of dt = (0.35 / Uring) / 350; the strength-weighted centroid and
+radius of each ring (calc_rings_weighted) must match the thin-ring ODEs of
+Borisov, Kilin & Mamaev (analytic_coaxialrings, Delta = 0, constant cores) to
+5 % (centroid of the first ring) and 3 % (the others) -- the reference's
+bounds.  The reference runs UJ_fmm; with 200 particles its far-field
+truncation is immaterial, and UJ_direct is evaluated here: by the oracle on
+the CPU, by the library (FP64 and FP32-comp) on the GPU.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import vpm_gb300 as vpm
+import vpm_gb300.rings as rings
+
+R, DZ, NPHI, NSTEPS = 0.7906, 0.7906, 100, 350
+
+
+def _run(UJ, formulation, SFS=None):
+    Rcross = 0.10 * R
+    Uref = rings.Uring(1.0, R, Rcross, 0.5)
+    dt = (NSTEPS / 1000 / Uref) / NSTEPS
+    pf = vpm.ParticleField(2 * NPHI, kernel=vpm.winckelmans, UJ=UJ, formulation=formulation,
+                           relaxation=vpm.correctedpedrizzetti, SFS=SFS if SFS is not None else vpm.noSFS,
+                           transposed=True)
+    for ri in range(2):
+        rings.addvortexring(pf, 1.0, R, 1.0, Rcross, NPHI, 0, Rcross, O=(0.0, 0.0, DZ * ri))
+    vpm.run_vpm(pf, dt, NSTEPS)
+    (Z1, R1, _), (Z2, R2, _) = rings.calc_rings_weighted(pf, [0, NPHI, 2 * NPHI])
+    _, Ra, Za = rings.analytic_coaxialrings([1.0, 1.0], [R, R], [0.0, DZ], [Rcross, Rcross], [0.0, 0.0],
+                                            tend=pf.t, dynamica=False)
+    err = {"Z1": (Z1[2] - Za[-1, 0]) / Za[-1, 0], "Z2": (Z2[2] - Za[-1, 1]) / Za[-1, 1],
+           "R1": (R1 - Ra[-1, 0]) / Ra[-1, 0], "R2": (R2 - Ra[-1, 1]) / Ra[-1, 1]}
+    assert abs(pf.t - NSTEPS * dt) < 1e-12
+    return err
+
+
+def _check(err):
+    assert abs(err["Z1"]) < 0.05 and abs(err["Z2"]) < 0.03 and abs(err["R1"]) < 0.03 and abs(err["R2"]) < 0.03, err
+
+
+def test_analytic_rings_model():
+    """The thin-ring model on its own: an isolated ring moves at Kelvin's speed
+    (Delta = 0: ln(8R/a) - 1/2) and keeps its radius; two coaxial rings conserve
+    the total impulse sum Gamma R^2 (Euler with dt = 1e-4: to 1e-6) while the rear
+    ring contracts and the front ring widens."""
+    pytest.importorskip("scipy")
+    t, Rr, Zr = rings.analytic_coaxialrings([1.0], [1.0], [0.0], [0.1], [0.0], tend=0.5)
+    assert abs(Zr[-1, 0] - 0.5 / (4 * math.pi) * (math.log(80) - 0.5)) < 1e-12 and Rr[-1, 0] == 1.0
+    t, Rr, Zr = rings.analytic_coaxialrings([1.0, 1.0], [R, R], [0.0, DZ], [0.07906] * 2, [0.0, 0.0],
+                                            tend=0.9, dynamica=False)
+    imp = (Rr ** 2).sum(axis=1)
+    assert abs(imp[-1] - imp[0]) < 1e-6 * imp[0]
+    assert Rr[-1, 0] < R < Rr[-1, 1]          # the rear ring contracts (and speeds up), the front ring widens
+
+
+def test_leapfrog_matches_analytic_with_the_oracle():
+    pytest.importorskip("scipy")
+    import oracle
+
+    def UJ_oracle(pfield, rbf=False, sfs=False, reset=True, reset_sfs=False, **kw):
+        flags = (oracle.RESET if reset else 0) | (oracle.RESET_SFS if reset_sfs else 0) | \
+                (oracle.SFS if sfs else 0) | (oracle.TRANSPOSED if pfield.transposed else 0)
+        oracle.uj_direct(pfield.particles, pfield.np, pfield.kernel.kid, flags)
+    _check(_run(UJ_oracle, vpm.cVPM))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["cvpm", "rvpm", "rvpm_dynamic_sfs", "cvpm_fp32comp"])
+def test_leapfrog_matches_analytic_on_the_gpu(case):
+    """The reference's three test_error cases -- classic VPM, reformulated VPM,
+    reformulated VPM with the dynamic SFS model -- through UJ_gb300, and the
+    classic case through UJ_gb300_mixed."""
+    pytest.importorskip("scipy")
+    formulation = vpm.cVPM if case.startswith("cvpm") else vpm.rVPM
+    UJ = vpm.UJ_gb300_mixed if case.endswith("fp32comp") else vpm.UJ_gb300
+    SFS = vpm.DynamicSFS() if case == "rvpm_dynamic_sfs" else None
+    _check(_run(UJ, formulation, SFS))
