@@ -556,14 +556,14 @@ def run_leapfrog(args):
     out = {"mode": "leapfrog", "steps": args.lf_steps, "dt": dt, "precision": "fp32comp"}
     # pair passes per FP32-comp step: 3 stage UJ + Estr, the relaxation UJ, and the dynamic
     # procedure's differences (one filter-difference pass over the J term, two Estr passes)
-    uj_per_step, estr_per_step = 5, 5
+    passes = {"uj": 4, "estr": 5, "filter_difference": 1}
     if args.lf_n > 0:
         X, G, s = workloads.leapfrog_rings(args.lf_n, nper=10)
         n = X.shape[0]
         ms32, mon32, f32 = _leapfrog_run(ctx, X, G, s, vpm.FP32COMP, args.lf_steps, dt, 20, torch, ds)
         out.update({"n_particles": n, "ms_per_step": ms32, "particle_steps_per_s": n / (ms32 / 1e3),
-                    "pairs_per_s": (uj_per_step + estr_per_step) * float(n) * n / (ms32 / 1e3),
-                    "uj_calls_per_step": uj_per_step, "estr_calls_per_step": estr_per_step,
+                    "pairs_per_s": sum(passes.values()) * float(n) * n / (ms32 / 1e3),
+                    "pair_passes_per_step": passes,
                     "drift_fp32comp": _drift(mon32), "monitor_fp32comp": mon32})
     # FP64 vs FP32-comp on the full-size field over a few steps
     k64 = args.lf_f64_steps if args.lf_n > 0 else 0

@@ -369,7 +369,9 @@ int vpm_ctx_create(vpm_ctx** out, int device)
     vpm_ctx* c = new vpm_ctx();
     c->device = device;
     c->num_sms = prop.multiProcessorCount;
-    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+    // a blocking stream: ordered with the legacy default stream's work both ways, so that
+    // callers who queue their own work there (frameworks' default streams) need no events
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamDefault) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         delete c;

@@ -21,6 +21,7 @@ KERNEL_SINGULAR, KERNEL_GAUSSIAN, KERNEL_GAUSSIANERF, KERNEL_WINCKELMANS = 0, 1,
 FP64, FP32COMP = 0, 1
 RESET, RESET_SFS, SFS, TRANSPOSED, CHECK_FINITE = 1, 2, 4, 8, 16
 DYN_FORCE_POSITIVE, DYN_CLIP_BACKSCATTER, DYN_SUBTRACT = 32, 64, 128
+CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy, the legacy default stream's handle
 NFIELDS = 46
 FLOP_PER_UJ_PAIR = 74
 FLOP_PER_ESTR_PAIR = 25
@@ -283,8 +284,12 @@ class Context:
 
     # --------------------------------------------------- device-pointer API
     def _torch_stream(self):
+        """Run on torch's current stream.  torch reports its default stream (the legacy
+        default stream) as handle 0, which vpm_ctx_set_stream reads as "the context's own
+        stream": pass cudaStreamLegacy (handle 1) for it instead."""
         import torch
-        self.set_stream(torch.cuda.current_stream().cuda_stream)
+        h = torch.cuda.current_stream().cuda_stream
+        self.set_stream(h if h else CUDA_STREAM_LEGACY)
 
     def uj_dev(self, xt, xs, gs, sgs, U, J, kernel: int, precision: int):
         """U += and J += on CUDA float64 tensors x[n,3], gamma[n,3], sigma[n], U[n,3], J[n,9]."""

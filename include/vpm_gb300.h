@@ -103,7 +103,9 @@ int vpm_ctx_destroy(vpm_ctx* ctx);
  * vpm_uj_dev_noalloc).  Valid until the next call on the same context. */
 const char* vpm_last_error(const vpm_ctx* ctx);
 /* Use `stream` (a cudaStream_t) for all later work of this context.  NULL
- * selects the context's own stream. */
+ * selects the context's own stream, a blocking stream: it is ordered with the
+ * legacy default stream's work both ways.  To run on the legacy default stream
+ * itself (a framework's stream 0), pass cudaStreamLegacy, not NULL. */
 int vpm_ctx_set_stream(vpm_ctx* ctx, void* stream);
 /* Bound, in seconds, on every host wait for device work of this context
  * (default 3600).  A wait that runs out returns VPM_ERR_TIMEOUT and marks the

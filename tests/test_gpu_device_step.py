@@ -272,3 +272,43 @@ def test_dynamic_after_rejects_bad_bounds(ctx):
     for lo, hi in ((-0.1, 1.0), (0.0, -1.0), (0.5, 0.1)):
         with pytest.raises(vpm._lib.VPMError, match="Invalid C bounds"):
             ctx.dynamic_after_dev(0.999, 0.005, lo, hi, 0.8, z(3), z(1)[:, 0] + 0.05, z(9), z(3), z(3), z(9))
+
+
+@pytest.mark.parametrize("n", [40000, 200000])
+def test_dynamic_diff_fp32comp_follows_fp64_at_scale(ctx, n):
+    """vpm_dynamic_diff_dev at the leapfrog workload's sizes (split reductions,
+    many source tiles): the FP32-comp differences against FP64's two evaluations."""
+    import torch
+    X, G, s = workloads.leapfrog_rings(n, nper=10)
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    x, g, sg = d(X), d(G), d(s)
+    m = x.shape[0]
+    U, J = torch.zeros(m, 3, device="cuda", dtype=torch.float64), torch.zeros(m, 9, device="cuda", dtype=torch.float64)
+    ctx.uj_dev(x, x, g, sg, U, J, 2, 0)
+    out = []
+    for prec in (0, 1):
+        dJ = torch.zeros(m, 9, device="cuda", dtype=torch.float64)
+        dS = torch.zeros(m, 3, device="cuda", dtype=torch.float64)
+        ctx.dynamic_diff_dev(x, g, sg, J, 0.999, dJ, dS, 2, prec)
+        out.append((dJ.cpu().numpy(), dS.cpu().numpy()))
+    eJ = normwise(out[1][0], out[0][0])[0]
+    eS = normwise(out[1][1], out[0][1])[0]
+    assert eJ <= 2e-6 and eS <= 2e-5, (eJ, eS)
+
+
+def test_device_step_is_deterministic(ctx):
+    """Two FP32-comp steps from the same state (dynamic SFS, core spreading,
+    relaxation) give the same bits: the library's work is ordered with the torch
+    work around it (it runs on torch's stream, and its own stream is a blocking
+    one), and no pair sum depends on scheduling."""
+    import torch
+    X, G, s = workloads.leapfrog_rings(40000, nper=10)
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    outs = []
+    for _ in range(2):
+        fld = ds.DeviceField(d(X), d(G), d(s), kernel=vpm._lib.KERNEL_GAUSSIANERF, precision=1)
+        ds.rk3_step(fld, 0.005, ctx, sfs=ds.DynamicSFSParams(), viscous=ds.CoreSpreadingParams(1e-4, 0.05),
+                    relax_rlxf=0.3)
+        outs.append([t.clone() for t in (fld.x, fld.gam, fld.sig, fld.C, fld.J, fld.SFS)])
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
