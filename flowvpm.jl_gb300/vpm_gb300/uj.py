@@ -35,8 +35,8 @@ def _kernel_id(pfield: ParticleField) -> int:
 
 def _uj(pfield: ParticleField, precision: int, rbf: bool, sfs: bool, reset: bool, reset_sfs: bool,
         ctx: _lib.Context | None):
-    if rbf:
-        raise NotImplementedError("rbf=true (zeta evaluation for the RBF solve) is not part of UJ_gb300")
+    # rbf is accepted and ignored, as UJ_direct does (src/FLOWVPM_UJ.jl:21-37); UJ_fmm's
+    # rbf=true evaluates zeta_fmm instead, which is zeta_fmm_gb300 here
     c = ctx if ctx is not None else _lib.default_context()
     c.uj(pfield.particles, pfield.np, _kernel_id(pfield), precision, _flags(pfield, sfs, reset, reset_sfs))
 
