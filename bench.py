@@ -683,7 +683,8 @@ def run_jet(args):
            "err_fp32comp_vs_fp64": {"U_max_rel": rel(U32, U64), "J_max_rel": rel(J32, J64)},
            "step_ms": ms_step, "steps_timed": nst, "particle_steps_per_s": n / (ms_step / 1e3),
            "step": "rVPM RK3 + dynamic SFS + Pedrizzetti relaxation: 4 near-field UJ calls (3 with Estr) and "
-                   "the near-field test-filter differences, tree rebuilt at each call",
+                   "the near-field test-filter differences; the tree is built at each UJ call and reused by "
+                   "the differences",
            "far_field": "not computed (FastMultipole.jl's multipole part is outside this library)"}
     print(json.dumps(out), flush=True)
 

@@ -75,6 +75,13 @@ struct vpm_ctx {
     // near-field: packed particles, and the lists (built on the device or uploaded)
     DevBuf leaf;
     NearScratch near;
+    // the lists (with warp groups) last built here from device positions, for VPM_REUSE_LISTS
+    NearLists near_last;
+    bool near_ok = false;
+    int64_t near_n = 0;
+    const double* near_x = nullptr;
+    int near_leaf = 0;
+    double near_theta = 0.0;
     int sync_rc = 0;     // VPM status of the last wait made for the list builder
 };
 
@@ -878,12 +885,32 @@ static int near_check(vpm_ctx* c, const char* fn, int64_t n, const double* x, co
     return VPM_OK;
 }
 
+// The near lists and warp groups of the positions x: the context's last ones when the
+// caller asks (VPM_REUSE_LISTS) and they were built from the same array, size, leaf size
+// and theta, else built now (and kept for the next call).
+static int near_lists(vpm_ctx* c, int64_t n, const double* x, int leaf_size, double theta, bool reuse,
+                      NearLists* L)
+{
+    if (reuse && c->near_ok && c->near_n == n && c->near_x == x && c->near_leaf == leaf_size &&
+        c->near_theta == theta) {
+        *L = c->near_last;
+        return VPM_OK;
+    }
+    c->near_ok = false;
+    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, L, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
+    e = near_groups(c->near, L, c->stream, near_sync, c, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
+    c->near_last = *L;
+    c->near_ok = true;
+    c->near_n = n; c->near_x = x; c->near_leaf = leaf_size; c->near_theta = theta;
+    return VPM_OK;
+}
+
 static int near_run(vpm_ctx* c, NearLists& L, int64_t n, const double* x, const double* gam, const double* sig,
                     const uint8_t* static_flags, double* U, double* J, double* SFS, int kernel, int precision,
                     int flags, int64_t* stats)
 {
-    cudaError_t e = near_groups(c->near, &L, c->stream, near_sync, c, &c->launches);
-    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
     RC(grow(c, c->leaf, leaf_work_bytes(n), "near-field packs"));
     LeafArgs a;
     a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = U; a.J = J; a.SFS = SFS; a.static_flags = static_flags;
@@ -912,12 +939,12 @@ int vpm_p2p_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
         return fail(c, VPM_ERR_ARG, "%s: leaf_size must be in 1..%d", fn, LEAF_SIZE_MAX);
     if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "%s: bad theta", fn);
     DeviceGuard dg(c->device);
-    RC(near_check(c, fn, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags));
+    RC(near_check(c, fn, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags & ~VPM_REUSE_LISTS));
     if (n == 0) return VPM_OK;
     NearLists L;
-    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, &L, &c->launches);
-    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
-    return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags, stats);
+    RC(near_lists(c, n, x, leaf_size, theta, (flags & VPM_REUSE_LISTS) != 0, &L));
+    return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags & ~VPM_REUSE_LISTS,
+                    stats);
 }
 
 int vpm_rk3_stage_dev(vpm_ctx* c, int64_t n, double a, double b, double dt, const double* Uinf, double f, double g,
@@ -1001,7 +1028,7 @@ int vpm_dynamic_after_dev(vpm_ctx* c, int64_t n, double alpha, double rlxf, doub
 }
 
 int vpm_zeta_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig, double* W,
-                          int leaf_size, double theta, int kernel, int precision, int64_t* stats)
+                          int leaf_size, double theta, int kernel, int precision, int flags, int64_t* stats)
 {
     const char* fn = "vpm_zeta_leaflist_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
@@ -1011,6 +1038,7 @@ int vpm_zeta_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* 
     if (leaf_size < 1 || leaf_size > LEAF_SIZE_MAX)
         return fail(c, VPM_ERR_ARG, "%s: leaf_size must be in 1..%d", fn, LEAF_SIZE_MAX);
     if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "%s: bad theta", fn);
+    if (flags & ~VPM_REUSE_LISTS) return fail(c, VPM_ERR_ARG, "%s: only VPM_REUSE_LISTS is accepted in flags", fn);
     if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     RC(check_kernel(c, kernel, precision));
     if (n == 0) return VPM_OK;
@@ -1018,10 +1046,7 @@ int vpm_zeta_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* 
     if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(W))
         return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
     NearLists L;
-    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, &L, &c->launches);
-    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
-    e = near_groups(c->near, &L, c->stream, near_sync, c, &c->launches);
-    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
+    RC(near_lists(c, n, x, leaf_size, theta, (flags & VPM_REUSE_LISTS) != 0, &L));
     RC(grow(c, c->leaf, leaf_work_bytes(n), "near-field packs"));
     LeafArgs a;
     a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.U = nullptr; a.J = nullptr; a.SFS = nullptr;
@@ -1050,7 +1075,8 @@ int vpm_dynamic_diff_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const 
         return fail(c, VPM_ERR_ARG, "%s: leaf_size must be in 1..%d", fn, LEAF_SIZE_MAX);
     if (!(theta >= 0.0 && theta <= 1.0e6)) return fail(c, VPM_ERR_ARG, "%s: bad theta", fn);
     if (!(alpha > 0.0 && alpha < 1.0)) return fail(c, VPM_ERR_ARG, "%s: alpha must be in (0, 1)", fn);
-    if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
+    if (flags & ~(VPM_TRANSPOSED | VPM_REUSE_LISTS))
+        return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED and VPM_REUSE_LISTS are accepted in flags", fn);
     if (n < 0 || n > (int64_t)1 << 30) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     RC(check_kernel(c, kernel, precision));
     if (n == 0) return VPM_OK;
@@ -1060,10 +1086,7 @@ int vpm_dynamic_diff_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const 
         return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
     cudaStream_t st = c->stream;
     NearLists L;
-    cudaError_t e = near_build(c->near, n, x, leaf_size, theta, st, near_sync, c, &L, &c->launches);
-    if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
-    e = near_groups(c->near, &L, st, near_sync, c, &c->launches);
-    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
+    RC(near_lists(c, n, x, leaf_size, theta, (flags & VPM_REUSE_LISTS) != 0, &L));
     RC(grow(c, c->leaf, leaf_work_bytes(n), "near-field packs"));
     RC(grow(c, c->s, n * sizeof(double), "test-filter core sizes"));
     double* sig_a = (double*)c->s.p;
@@ -1149,9 +1172,12 @@ int vpm_p2p_lists_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam,
         }
     }
     NearLists L;
+    c->near_ok = false;
     cudaError_t e = near_upload(c->near, n, perm, nl, leaf_begin, leaf_end, row, cs.data(), c->stream, near_sync, c,
                                 &L, &c->launches);
     if (e != cudaSuccess) return near_fail(c, e, "leaf-pair lists");
+    e = near_groups(c->near, &L, c->stream, near_sync, c, &c->launches);
+    if (e != cudaSuccess) return near_fail(c, e, "near-field warp groups");
     return near_run(c, L, n, x, gam, sig, static_flags, U, J, SFS, kernel, precision, flags, stats);
 }
 
@@ -1168,6 +1194,7 @@ int vpm_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, int leaf_size, doub
     DeviceGuard dg(c->device);
     if (!is_device_ptr(x)) return fail(c, VPM_ERR_ARG, "%s: x must be a device pointer", fn);
     NearLists L;
+    c->near_ok = false;
     cudaError_t e = near_build(c->near, n, x, leaf_size, theta, c->stream, near_sync, c, &L, &c->launches);
     if (e != cudaSuccess) return near_fail(c, e, "octree and leaf-pair lists");
     sizes[0] = L.nleaves;

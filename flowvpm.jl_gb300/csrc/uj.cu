@@ -242,6 +242,9 @@ constexpr int MID_BLOCKS = 16;
 #define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
 #endif
 constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
+#ifndef VPM_UJ_SMEM_ACC
+#define VPM_UJ_SMEM_ACC 0                   // 1: the FP64 sums live in shared memory, not registers
+#endif
 
 // Each warp streams the sources on its own: 32 per tile, double-buffered with
 // cp.async, so warps never wait for each other (no block-wide barrier).
@@ -281,10 +284,23 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
     const float sfar = s_far<K>();
 
+#if VPM_UJ_SMEM_ACC
+    // FP64 sums of this thread: [0..2] U, [3..5] W, [6..13] J' (touched once per mid-level flush)
+    __shared__ double acc64[14][UJ_THREADS];
+#pragma unroll
+    for (int k = 0; k < 14; k++) acc64[k][threadIdx.x] = 0.0;
+#define ACC_DU(k) acc64[k][threadIdx.x]
+#define ACC_DW(k) acc64[3 + (k)][threadIdx.x]
+#define ACC_DJ(k) acc64[6 + (k)][threadIdx.x]
+#else
     double dU[3] = {0.0, 0.0, 0.0}, dW[3] = {0.0, 0.0, 0.0};
     double dJ[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) dJ[k] = 0.0;
+#define ACC_DU(k) dU[k]
+#define ACC_DW(k) dW[k]
+#define ACC_DJ(k) dJ[k]
+#endif
     float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
     float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
 #pragma unroll
@@ -334,19 +350,28 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
             in_block = 0;
             if (++in_mid == MID_BLOCKS) {
 #pragma unroll
-                for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
+                for (int k = 0; k < 3; k++) {
+                    ACC_DU(k) += (double)mu[k]; ACC_DW(k) += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f;
+                }
 #pragma unroll
-                for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
+                for (int k = 0; k < 8; k++) { ACC_DJ(k) += (double)mj[k]; mj[k] = 0.f; }
                 in_mid = 0;
             }
         }
         __syncwarp();   // every lane is done with `buf` before it is refilled
     }
     // remaining partial block and mid-level sums
+    double dU[3], dW[3], dJ[8];
 #pragma unroll
-    for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k] + (double)u[k]; dW[k] += (double)mw[k] + (double)w[k]; }
+    for (int k = 0; k < 3; k++) {
+        dU[k] = ACC_DU(k) + ((double)mu[k] + (double)u[k]);
+        dW[k] = ACC_DW(k) + ((double)mw[k] + (double)w[k]);
+    }
 #pragma unroll
-    for (int k = 0; k < 8; k++) dJ[k] += (double)mj[k] + (double)jq[k];
+    for (int k = 0; k < 8; k++) dJ[k] = ACC_DJ(k) + ((double)mj[k] + (double)jq[k]);
+#undef ACC_DU
+#undef ACC_DW
+#undef ACC_DJ
     if (!valid) return;
     // J = -3 J' (J'_33 = -J'_11 - J'_22) plus the Kronecker term of
     // src/FLOWVPM_fmm.jl:148-159 (W = sum aux2 Gamma)

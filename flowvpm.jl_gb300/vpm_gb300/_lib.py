@@ -19,7 +19,7 @@ LIB_PATH = os.environ.get("VPM_GB300_LIB", os.path.join(PKG_ROOT, "lib", "libvpm
 OK, ERR_ARG, ERR_CAPACITY, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NODEVICE, ERR_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 KERNEL_SINGULAR, KERNEL_GAUSSIAN, KERNEL_GAUSSIANERF, KERNEL_WINCKELMANS = 0, 1, 2, 3
 FP64, FP32COMP = 0, 1
-RESET, RESET_SFS, SFS, TRANSPOSED, CHECK_FINITE = 1, 2, 4, 8, 16
+RESET, RESET_SFS, SFS, TRANSPOSED, CHECK_FINITE, REUSE_LISTS = 1, 2, 4, 8, 16, 256
 DYN_FORCE_POSITIVE, DYN_CLIP_BACKSCATTER, DYN_SUBTRACT = 32, 64, 128
 CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy, the legacy default stream's handle
 NFIELDS = 46
@@ -58,7 +58,7 @@ SIGNATURES = {
                                  _vp, _vp, _vp, _vp]),
     "vpm_relax_dev": (_int, [_vp, _i64, _dbl, _vp, _vp]),
     "vpm_dynamic_after_dev": (_int, [_vp, _i64, _dbl, _dbl, _dbl, _dbl, _dbl, _int, _vp, _vp, _vp, _vp, _vp, _vp]),
-    "vpm_zeta_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _vp]),
+    "vpm_zeta_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int, _vp]),
     "vpm_dynamic_diff_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _dbl, _int,
                                              _int, _int, _vp]),
     "vpm_p2p_leaflist_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _dbl, _int, _int, _int,
@@ -248,20 +248,20 @@ class Context:
         self._check(rc)
 
     def zeta_leaflist_dev(self, x, gam, sig, W, *, leaf_size: int = 64, theta: float = 0.4,
-                          kernel: int = KERNEL_GAUSSIANERF, precision: int = FP64):
+                          kernel: int = KERNEL_GAUSSIANERF, precision: int = FP64, reuse: bool = False):
         """zeta_fmm's near-field sum, W[n,3] += (CUDA float64 tensors); returns
-        (leaves, leaf pairs, particle pairs)."""
+        (leaves, leaf pairs, particle pairs).  reuse: VPM_REUSE_LISTS."""
         _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(W, 3)
         self._torch_stream()
         stats = np.zeros(3, dtype=np.int64)
         self._check(self._L.vpm_zeta_leaflist_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(W),
                                                   int(leaf_size), float(theta), int(kernel), int(precision),
-                                                  stats.ctypes.data))
+                                                  REUSE_LISTS if reuse else 0, stats.ctypes.data))
         return tuple(int(v) for v in stats)
 
     def dynamic_diff_leaflist_dev(self, x, gam, sig, J, alpha: float, dJ, dSFS, *, leaf_size: int = 64,
                                   theta: float = 0.4, kernel: int = KERNEL_GAUSSIANERF, precision: int = FP32COMP,
-                                  transposed: bool = True, static=None):
+                                  transposed: bool = True, static=None, reuse: bool = False):
         """dynamic_diff_dev over the near field of p2p_leaflist_dev (same leaf_size, theta; J the
         near-field J at sigma); dJ, dSFS set.  Returns (leaves, leaf pairs, particle pairs)."""
         _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(J, 9); _check_dev(dJ, 9)
@@ -271,7 +271,7 @@ class Context:
         self._check(self._L.vpm_dynamic_diff_leaflist_dev(
             self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(static), _ptr(J), float(alpha), _ptr(dJ),
             _ptr(dSFS), int(leaf_size), float(theta), int(kernel), int(precision),
-            TRANSPOSED if transposed else 0, stats.ctypes.data))
+            (TRANSPOSED if transposed else 0) | (REUSE_LISTS if reuse else 0), stats.ctypes.data))
         return tuple(int(v) for v in stats)
 
     def uj_cross(self, src: np.ndarray, ns: int, tgt: np.ndarray, nt: int, kernel: int, precision: int):
@@ -310,7 +310,7 @@ class Context:
 
     def p2p_leaflist_dev(self, x, gam, sig, U, J, sfs_out=None, *, leaf_size: int = 64, theta: float = 0.4,
                          kernel: int = KERNEL_GAUSSIANERF, precision: int = FP32COMP, sfs: bool = False,
-                         transposed: bool = True, static=None):
+                         transposed: bool = True, static=None, reuse: bool = False):
         """Near-field P2P (UJ, and Estr into sfs_out with sfs=True) over octree leaf pairs;
         returns (leaves, leaf pairs, particle pairs)."""
         _check_dev(x, 3); _check_dev(gam, 3); _check_dev(sig, 1); _check_dev(U, 3); _check_dev(J, 9)
@@ -318,7 +318,7 @@ class Context:
             _check_dev(sfs_out, 3)
         self._torch_stream()
         stats = np.zeros(3, dtype=np.int64)
-        flags = (SFS if sfs else 0) | (TRANSPOSED if transposed else 0)
+        flags = (SFS if sfs else 0) | (TRANSPOSED if transposed else 0) | (REUSE_LISTS if reuse else 0)
         self._check(self._L.vpm_p2p_leaflist_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(static),
                                                  _ptr(U), _ptr(J), _ptr(sfs_out) if sfs else None, int(leaf_size),
                                                  float(theta), int(kernel), int(precision), flags,

@@ -113,18 +113,19 @@ class CoreSpreadingParams:
     iterror: bool = True
 
 
-def zeta(fld: DeviceField, ctx: _lib.Context) -> torch.Tensor:
+def zeta(fld: DeviceField, ctx: _lib.Context, reuse: bool = False) -> torch.Tensor:
     """zeta_direct: W[n,3] = sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s (self pair included);
     for a near-field state, zeta_fmm's sum over the near leaf pairs, into a zeroed W
     (the reference's zeta_fmm adds to J[1:3] without zeroing them; the conjugate
-    gradient here takes each evaluation on its own, as with zeta_direct)."""
+    gradient here takes each evaluation on its own, as with zeta_direct).  reuse: the
+    positions are those of the previous near-field call (VPM_REUSE_LISTS)."""
     W = torch.zeros_like(fld.gam)
     if fld.leaflist is None:
         ctx.zeta_dev(fld.x, fld.x, fld.gam, fld.sig, W, fld.kernel, fld.precision)
     else:
         leaf_size, theta = fld.leaflist
         ctx.zeta_leaflist_dev(fld.x, fld.gam, fld.sig, W, leaf_size=leaf_size, theta=theta, kernel=fld.kernel,
-                              precision=fld.precision)
+                              precision=fld.precision, reuse=reuse)
     return W
 
 
@@ -136,7 +137,7 @@ def rbf_conjugategradient(fld: DeviceField, ctx: _lib.Context, target: torch.Ten
     tiny = 2 * EPS
     x = target * fld.vol[:, None]                 # x0 = omega_targ * vol
     fld.gam.copy_(x)
-    r = target - zeta(fld, ctx)                   # r0 = b - A x0
+    r = target - zeta(fld, ctx)                   # r0 = b - A x0 (builds the lists at these positions)
     fld.gam.copy_(r)                              # p0 = r0
     rr0s = (r * r).sum(0).tolist()
     rrs = list(rr0s)
@@ -144,7 +145,7 @@ def rbf_conjugategradient(fld: DeviceField, ctx: _lib.Context, target: torch.Ten
     for it in range(1, int(p.itmax) + 1):
         if not any(flags):
             break
-        Ap = zeta(fld, ctx)
+        Ap = zeta(fld, ctx, reuse=True)           # the positions do not move during the solve
         pAps = (fld.gam * Ap).sum(0).tolist()
         alphas = torch.tensor([rrs[i] / pAps[i] * flags[i] if flags[i] else 0.0 for i in range(3)],
                               dtype=torch.float64, device=x.device)
@@ -186,9 +187,10 @@ def _dynamic_fused(fld, ctx, p: DynamicSFSParams):
                              fld.transposed)
     else:
         leaf_size, theta = fld.leaflist
+        # the stage's UJ call has just built the lists at these positions
         ctx.dynamic_diff_leaflist_dev(fld.x, fld.gam, fld.sig, fld.J, p.alpha, dJ, dS, leaf_size=leaf_size,
                                       theta=theta, kernel=fld.kernel, precision=fld.precision,
-                                      transposed=fld.transposed)
+                                      transposed=fld.transposed, reuse=True)
     fld.M.zero_()
     fld.M[:, 0:3] = _stretch(dJ, fld.gam, fld.transposed)
     fld.M[:, 3:6] = dS

@@ -76,7 +76,11 @@ enum {
     VPM_RESET_SFS  = 2,  /* reset_sfs=true: zero rows 40:42 of non-static particles */
     VPM_SFS        = 4,  /* sfs=true: accumulate Estr into rows 40:42 after U,J */
     VPM_TRANSPOSED = 8,  /* transposed stretching scheme (pfield.transposed) */
-    VPM_CHECK_FINITE = 16 /* scan outputs for NaN/Inf and return VPM_ERR_NONFINITE */
+    VPM_CHECK_FINITE = 16, /* scan outputs for NaN/Inf and return VPM_ERR_NONFINITE */
+    /* near-field calls: reuse the context's last octree and leaf-pair lists when they were
+     * built from the same x array, n, leaf_size and theta; the caller asserts that the
+     * positions have not changed since (within one RK3 stage, for instance) */
+    VPM_REUSE_LISTS = 256
 };
 
 /* flags of vpm_dynamic_after_dev (with VPM_TRANSPOSED), the settings of
@@ -240,7 +244,7 @@ int vpm_zeta_dev(vpm_ctx* ctx, int64_t nt, const double* xt, int64_t ns, const d
  * multipole acceptance criterion theta * r < R1 + R2 (r: distance of the cell
  * centres, R: cell radii; src/FLOWVPM_particlefield.jl:28-36), as
  * FastMultipole's direct_list does.  The far field is not computed.  flags:
- * VPM_SFS, VPM_TRANSPOSED.  Device pointers; static_flags may be NULL.  stats
+ * VPM_SFS, VPM_TRANSPOSED, VPM_REUSE_LISTS.  Device pointers; static_flags may be NULL.  stats
  * (may be NULL) receives {leaves, leaf pairs, particle pairs}.  The lists are
  * the ones vpm_leaflist_host builds, entry for entry. */
 int vpm_p2p_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
@@ -254,16 +258,18 @@ int vpm_p2p_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double*
  * pairs of vpm_p2p_leaflist_dev (same leaf_size, theta) of
  * zeta(r/sigma_s)/sigma_s^3 Gamma_s, every particle a target and the self pair
  * included.  Like the reference's loop it adds to W (the reference adds into
- * J[1:3] without zeroing them, unlike zeta_direct).  Device pointers; stats as
- * vpm_p2p_leaflist_dev. */
+ * J[1:3] without zeroing them, unlike zeta_direct).  Device pointers; flags:
+ * VPM_REUSE_LISTS; stats as vpm_p2p_leaflist_dev. */
 int vpm_zeta_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
-                          double* W, int leaf_size, double theta, int kernel, int precision, int64_t* stats);
+                          double* W, int leaf_size, double theta, int kernel, int precision, int flags,
+                          int64_t* stats);
 
 /* vpm_dynamic_diff_dev over the near field only: the differences of the two
  * evaluations of the near-field leg (vpm_p2p_leaflist_dev with VPM_SFS, same
  * leaf_size and theta) at core sizes alpha sigma and sigma, as the dynamic
  * procedure (src/FLOWVPM_subfilterscale.jl:447-673) takes them when UJ is
  * UJ_fmm.  J is the near-field J at sigma; dJ[n,9] and dSFS[n,3] are set.
+ * flags: VPM_TRANSPOSED, VPM_REUSE_LISTS.
  * Static particles (static_flags, may be NULL) get no SFS, as in
  * vpm_p2p_leaflist_dev.  stats as there.  FP64 evaluates and subtracts;
  * FP32COMP evaluates the differences directly. */

@@ -290,3 +290,32 @@ def test_zeta_fmm_hook_adds_to_rows_16_18():
     assert normwise(pf.particles[15:18, :n].T - 0.5, ref)[0] <= 1e-12
     other = [r for r in range(46) if r not in (15, 16, 17)]
     assert np.array_equal(pf.particles[other, :], Q[other, :])
+
+
+def test_reused_lists_give_the_same_sums(ctx):
+    """VPM_REUSE_LISTS: a call that reuses the lists of the previous call on the
+    same positions gives the same bits as one that builds them; a call on other
+    positions (another array) builds its own."""
+    n = 6000
+    X, G, s = random_cloud(n, seed=88, box=0.5)
+    x, g, sg = _dev(X), _dev(G), _dev(s)
+    out = []
+    for reuse in (False, True):
+        U, J, S = _zeros(n, 3), _zeros(n, 9), _zeros(n, 3)
+        st = ctx.p2p_leaflist_dev(x, g, sg, U, J, S, leaf_size=32, theta=0.4, kernel=2, precision=1, sfs=True,
+                                  reuse=reuse)
+        out.append((st, U.cpu().numpy(), J.cpu().numpy(), S.cpu().numpy()))
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1:], out[1][1:]):
+        assert np.array_equal(a, b)
+    dJ, dS = _zeros(n, 9), _zeros(n, 3)
+    dJ2, dS2 = _zeros(n, 9), _zeros(n, 3)
+    Jd = _dev(out[0][2])
+    ctx.dynamic_diff_leaflist_dev(x, g, sg, Jd, 0.999, dJ, dS, leaf_size=32, theta=0.4, reuse=True)
+    ctx.dynamic_diff_leaflist_dev(x, g, sg, Jd, 0.999, dJ2, dS2, leaf_size=32, theta=0.4, reuse=False)
+    assert torch_equal(dJ, dJ2) and torch_equal(dS, dS2)
+    Y = random_cloud(n, seed=89, box=0.5)[0]
+    W1, W2 = _zeros(n, 3), _zeros(n, 3)
+    st_y = ctx.zeta_leaflist_dev(_dev(Y), g, sg, W1, leaf_size=32, theta=0.4, kernel=2, reuse=True)
+    ctx.zeta_leaflist_dev(_dev(Y), g, sg, W2, leaf_size=32, theta=0.4, kernel=2)
+    assert torch_equal(W1, W2) and st_y[1] > 0
