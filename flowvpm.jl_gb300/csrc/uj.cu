@@ -361,14 +361,14 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
         __syncwarp();   // every lane is done with `buf` before it is refilled
     }
     // remaining partial block and mid-level sums
-    double dU[3], dW[3], dJ[8];
+    double fU[3], fW[3], fJ[8];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        dU[k] = ACC_DU(k) + ((double)mu[k] + (double)u[k]);
-        dW[k] = ACC_DW(k) + ((double)mw[k] + (double)w[k]);
+        fU[k] = ACC_DU(k) + ((double)mu[k] + (double)u[k]);
+        fW[k] = ACC_DW(k) + ((double)mw[k] + (double)w[k]);
     }
 #pragma unroll
-    for (int k = 0; k < 8; k++) dJ[k] = ACC_DJ(k) + ((double)mj[k] + (double)jq[k]);
+    for (int k = 0; k < 8; k++) fJ[k] = ACC_DJ(k) + ((double)mj[k] + (double)jq[k]);
 #undef ACC_DU
 #undef ACC_DW
 #undef ACC_DJ
@@ -377,15 +377,15 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     // src/FLOWVPM_fmm.jl:148-159 (W = sum aux2 Gamma)
     double j9[9];
 #pragma unroll
-    for (int k = 0; k < 8; k++) j9[k] = -3.0 * dJ[k];
-    j9[8] = 3.0 * (dJ[0] + dJ[4]);
-    j9[1] -= dW[2];
-    j9[2] += dW[1];
-    j9[3] += dW[2];
-    j9[5] -= dW[0];
-    j9[6] -= dW[1];
-    j9[7] += dW[0];
-    double acc[12] = {dU[0], dU[1], dU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
+    for (int k = 0; k < 8; k++) j9[k] = -3.0 * fJ[k];
+    j9[8] = 3.0 * (fJ[0] + fJ[4]);
+    j9[1] -= fW[2];
+    j9[2] += fW[1];
+    j9[3] += fW[2];
+    j9[5] -= fW[0];
+    j9[6] -= fW[1];
+    j9[7] += fW[0];
+    double acc[12] = {fU[0], fU[1], fU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
     write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
 // --------------------------------------------------------------- launcher
