@@ -236,14 +236,16 @@ constexpr int BLOCK_TILES = UJ_BLOCK / WT;  // warp tiles per FP32 block
 // slower -- the FP64 pipe runs at 1/64 rate -- with the same U, J error against the oracle)
 constexpr int MID_BLOCKS = 16;
 #ifndef VPM_UJ_MIN_BLOCKS
-#define VPM_UJ_MIN_BLOCKS 5                 // resident blocks per SM the register budget targets
+#define VPM_UJ_MIN_BLOCKS 7                 // resident blocks per SM the register budget targets (72 registers)
 #endif
 #ifndef VPM_UJ_UNROLL
 #define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
 #endif
 constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
 #ifndef VPM_UJ_SMEM_ACC
-#define VPM_UJ_SMEM_ACC 0                   // 1: the FP64 sums live in shared memory, not registers
+// 1: the FP64 sums (touched once per 1,024 sources) live in shared memory, which frees the
+// registers for 7 resident blocks per SM instead of 5 -- measured 3.6 % faster at N = 2^20
+#define VPM_UJ_SMEM_ACC 1
 #endif
 
 // Each warp streams the sources on its own: 32 per tile, double-buffered with
