@@ -211,11 +211,15 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
     const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
     const float sfar = s_far<K>();
 
-    double dU[3] = {0.0, 0.0, 0.0}, dW[3] = {0.0, 0.0, 0.0}, dJ[8];
+    // FP64 sums of this lane in shared memory ([0..2] U, [3..5] W, [6..13] J'), touched once per
+    // NF_MID_BLKS blocks: the registers go to occupancy instead
+    __shared__ double acc64[14][NF_THREADS];
+#pragma unroll
+    for (int k = 0; k < 14; k++) acc64[k][threadIdx.x] = 0.0;
     float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
     float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) { dJ[k] = 0.0; mj[k] = 0.f; jq[k] = 0.f; }
+    for (int k = 0; k < 8; k++) { mj[k] = 0.f; jq[k] = 0.f; }
     int tiles = 0, blks = 0;
     IntervalWalk walk;
     walk.init(ivs, grp_row[grp], grp_row[grp + 1], lane);
@@ -251,16 +255,24 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
             if (++blks == NF_MID_BLKS) {
                 blks = 0;
 #pragma unroll
-                for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k]; dW[k] += (double)mw[k]; mu[k] = 0.f; mw[k] = 0.f; }
+                for (int k = 0; k < 3; k++) {
+                    acc64[k][threadIdx.x] += (double)mu[k];
+                    acc64[3 + k][threadIdx.x] += (double)mw[k];
+                    mu[k] = 0.f; mw[k] = 0.f;
+                }
 #pragma unroll
-                for (int k = 0; k < 8; k++) { dJ[k] += (double)mj[k]; mj[k] = 0.f; }
+                for (int k = 0; k < 8; k++) { acc64[6 + k][threadIdx.x] += (double)mj[k]; mj[k] = 0.f; }
             }
         }
     }
+    double dU[3], dW[3], dJ[8];
 #pragma unroll
-    for (int k = 0; k < 3; k++) { dU[k] += (double)mu[k] + (double)u[k]; dW[k] += (double)mw[k] + (double)w[k]; }
+    for (int k = 0; k < 3; k++) {
+        dU[k] = acc64[k][threadIdx.x] + ((double)mu[k] + (double)u[k]);
+        dW[k] = acc64[3 + k][threadIdx.x] + ((double)mw[k] + (double)w[k]);
+    }
 #pragma unroll
-    for (int k = 0; k < 8; k++) dJ[k] += (double)mj[k] + (double)jq[k];
+    for (int k = 0; k < 8; k++) dJ[k] = acc64[6 + k][threadIdx.x] + ((double)mj[k] + (double)jq[k]);
     if (!me.valid) return;
     double j9[9];
 #pragma unroll
