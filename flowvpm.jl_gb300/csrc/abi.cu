@@ -147,8 +147,9 @@ int bounded_wait(vpm_ctx* c)
             c->broken = true;
             return fail(c, VPM_ERR_TIMEOUT, "device work did not finish within %.1f s", c->timeout_s);
         }
+        // short sleeps: a wait ends at most ~50 us after the work (a step makes dozens of waits)
         std::this_thread::sleep_for(std::chrono::microseconds(sleep_us));
-        if (sleep_us < 1000) sleep_us *= 2;
+        if (sleep_us < 50) sleep_us *= 2;
     }
 }
 
