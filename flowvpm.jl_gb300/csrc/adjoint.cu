@@ -254,10 +254,10 @@ __device__ __forceinline__ void adj_coeffs_f32(float s, float& G, float& H, floa
 {
     if constexpr (K == K_GAUSERF) {
         if (s > S_FAR_GERF) {
-            const float rs = rsqrtf(s), rs2 = rs * rs;
+            const float rs = frsqrt(s), rs2 = rs * rs;
             G = rs * rs2; H = -3.0f * G * rs2; Kc = -5.0f * H * rs2; a = 0.0f; b = 0.0f;
         } else {
-            const float e = exp2f(s * -0.72134752044448170f);
+            const float e = fexp2(s * -0.72134752044448170f);
             a = F_C2 * e;
             b = a;
             if (s < S_SERIES_ADJ) {
@@ -267,7 +267,7 @@ __device__ __forceinline__ void adj_coeffs_f32(float s, float& G, float& H, floa
                 H = -3.0f * a * p2;
                 Kc = 15.0f * a * p3;
             } else {
-                const float rs = rsqrtf(s), rs2 = rs * rs;
+                const float rs = frsqrt(s), rs2 = rs * rs;
                 G = gerf_G_erfcx(s, e, rs);
                 H = (a - 3.0f * G) * rs2;
                 Kc = fmaf(15.0f, G, -a * (5.0f + s)) * rs2 * rs2;
@@ -275,8 +275,8 @@ __device__ __forceinline__ void adj_coeffs_f32(float s, float& G, float& H, floa
         }
     } else if constexpr (K == K_WNKLMNS) {
         const float q = s + 1.0f;
-        const float iq = __frcp_rn(q);
-        const float iq25 = iq * iq * rsqrtf(q);
+        const float iq = frcp(q);
+        const float iq25 = iq * iq * frsqrt(q);
         const float iq35 = iq25 * iq, iq45 = iq35 * iq;
         G = (s + 2.5f) * iq25;
         H = -3.0f * (s + 3.5f) * iq35;
@@ -284,7 +284,7 @@ __device__ __forceinline__ void adj_coeffs_f32(float s, float& G, float& H, floa
         a = 7.5f * iq35;
         b = 52.5f * iq45;
     } else {   // singular
-        const float rs = rsqrtf(s), rs2 = rs * rs;
+        const float rs = frsqrt(s), rs2 = rs * rs;
         G = rs * rs2; H = -3.0f * G * rs2; Kc = -5.0f * H * rs2; a = 0.0f; b = 0.0f;
     }
 }
@@ -304,7 +304,7 @@ __device__ __forceinline__ void adj_coeffs4_f32(const float (&s)[4], float (&G)[
         bool anyser = false, anymid = false;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            rs[q] = rsqrtf(s[q]);
+            rs[q] = frsqrt(s[q]);
             rs2[q] = rs[q] * rs[q];
             G[q] = rs[q] * rs2[q];
             H[q] = -3.0f * G[q] * rs2[q];
@@ -320,7 +320,7 @@ __device__ __forceinline__ void adj_coeffs4_f32(const float (&s)[4], float (&G)[
         float e[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            e[q] = exp2f(s[q] * -0.72134752044448170f);
+            e[q] = fexp2(s[q] * -0.72134752044448170f);
             const bool near = s[q] <= S_FAR_GERF;
             a[q] = near ? F_C2 * e[q] : 0.0f;
             b[q] = a[q];
@@ -498,7 +498,7 @@ uj_adjoint_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double
             if (allfar) {   // singular form (no sigma derivative)
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const float rs = rsqrtf(sq[q]), rs2 = rs * rs;
+                    const float rs = frsqrt(sq[q]), rs2 = rs * rs;
                     G[q] = rs * rs2; H[q] = -3.0f * G[q] * rs2; Kc[q] = -5.0f * H[q] * rs2; ca[q] = 0.0f; cb[q] = 0.0f;
                 }
             } else {

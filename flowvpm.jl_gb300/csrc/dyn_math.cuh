@@ -16,18 +16,18 @@ template <int K>
 __device__ __forceinline__ void g_d1_d2_f32(float t, float& d1, float& d2)
 {
     if constexpr (K == K_GAUSERF) {
-        const float e = F_C2 * exp2f(t * t * -0.72134752044448170f);   // sqrt(2/pi) e^{-t^2/2}
+        const float e = F_C2 * fexp2(t * t * -0.72134752044448170f);   // sqrt(2/pi) e^{-t^2/2}
         d1 = t * t * e;
         d2 = t * (2.0f - t * t) * e;
     } else if constexpr (K == K_GAUS) {
         const float t3 = t * t * t;
-        const float e = exp2f(t3 * -1.4426950408889634f);              // e^{-t^3}
+        const float e = fexp2(t3 * -1.4426950408889634f);              // e^{-t^3}
         d1 = 3.0f * t * t * e;
         d2 = t * (6.0f - 9.0f * t3) * e;
     } else if constexpr (K == K_WNKLMNS) {
         const float q = fmaf(t, t, 1.0f);
-        const float iq = __frcp_rn(q);
-        const float iq35 = iq * iq * iq * rsqrtf(q);                   // q^-3.5
+        const float iq = frcp(q);
+        const float iq35 = iq * iq * iq * frsqrt(q);                   // q^-3.5
         d1 = 7.5f * t * t * iq35;
         d2 = 7.5f * t * (2.0f - 5.0f * t * t) * iq35 * iq;
     } else {
@@ -134,7 +134,7 @@ template <int K, int M = 0>
 __device__ __forceinline__ void filter_diff_pair(float ex, float ey, float ez, float r2, float isig, float4 gam,
                                                  float hm, int m, bool on, float (&f)[9])
 {
-    const float rinv = rsqrtf(r2);
+    const float rinv = frsqrt(r2);
     const float rho = r2 * rinv * isig;
     float dg, dg1;
     filter_diff<K, M>(rho, hm, m, dg, dg1);

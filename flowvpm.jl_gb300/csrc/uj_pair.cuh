@@ -76,7 +76,7 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
         for (int q = 0; q < 4; q++) {
             float G, Q;
             if constexpr (singular_tail<K>()) {
-                const float rs = rsqrtf(r2[q]);
+                const float rs = frsqrt(r2[q]);
                 const float rs2 = rs * rs;
                 G = rs * rs2;
                 Q = G * rs2;

@@ -85,6 +85,46 @@ constexpr float S_SERIES = 2.0f;      // positive series below this s (Gaussian-
 constexpr float S_FAR_GERF = 50.0f;   // singular form above this s (rho > 7.07)
 constexpr float S_FAR_GAUS = 8.0f;    // singular form above this s (rho^3 > 22.6)
 
+#ifndef VPM_FTZ_UNARY
+#define VPM_FTZ_UNARY 1
+#endif
+// 1/sqrt(x), 2^x and 1/x of the FP32 pair forms: the hardware approximations with
+// subnormal arguments and results flushed to zero (PTX rsqrt.approx.ftz.f32,
+// ex2.approx.ftz.f32, rcp.approx.ftz.f32).  The arguments on the pair paths are
+// normal numbers (s, r^2 and 1 + s are at least 1e-30, or the pair is masked out),
+// and a 2^x flushed below 2^-126 is far under the FP32 resolution of the sums; the
+// forms that keep subnormals guard every call.  0 selects rsqrtf, exp2f, __frcp_rn.
+__device__ __forceinline__ float frsqrt(float x)
+{
+#if VPM_FTZ_UNARY
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return rsqrtf(x);
+#endif
+}
+__device__ __forceinline__ float fexp2(float x)
+{
+#if VPM_FTZ_UNARY
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return exp2f(x);
+#endif
+}
+__device__ __forceinline__ float frcp(float x)
+{
+#if VPM_FTZ_UNARY
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return __frcp_rn(x);
+#endif
+}
+
 // Gaussian kernel, t = rho^3: G = (1 - e^-t)/t = sum (-t)^k/(k+1)!,
 // H = 3 rho sum_{k>=2} (-1)^(k+1) (k-1)/k! t^(k-2).
 __device__ __forceinline__ float gaus_G_series(float t)
@@ -137,7 +177,7 @@ __host__ __device__ constexpr float s_far()
 // Singular form: G = s^-1.5, Q = G / r^2 = G s^-1 / sigma^2.
 __device__ __forceinline__ void far_GQ(float s, float isig2, float& G, float& Q)
 {
-    const float rs = rsqrtf(s);
+    const float rs = frsqrt(s);
     const float rs2 = rs * rs;
     G = rs * rs2;
     Q = G * (rs2 * isig2);
@@ -180,7 +220,7 @@ __device__ __forceinline__ void gerf_GQ(float s, float isig2, float& G, float& Q
         far_GQ(s, isig2, G, Q);
         return;
     }
-    const float e = exp2f(s * -0.72134752044448170f);
+    const float e = fexp2(s * -0.72134752044448170f);
     if (s < S_SERIES) {
         float p = 3.1622138893727926e-12f;
         p = fmaf(p, s, 7.273091945557423e-11f);
@@ -196,7 +236,7 @@ __device__ __forceinline__ void gerf_GQ(float s, float isig2, float& G, float& Q
         G = ce * fmaf(s, p, 0.33333333333333333f);
         Q = ce * p * isig2;
     } else {
-        const float rs = rsqrtf(s);
+        const float rs = frsqrt(s);
         const float rs2 = rs * rs;
         G = gerf_G_erfcx(s, e, rs);
         Q = fmaf(F_C2 * -0.33333333333333333f, e, G) * rs2 * isig2;
@@ -225,8 +265,8 @@ __device__ __forceinline__ void gerf_GQ4(const float (&s)[4], const float (&isig
     float e[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        e[q] = exp2f(s[q] * -0.72134752044448170f);
-        const float rs = rsqrtf(s[q]);
+        e[q] = fexp2(s[q] * -0.72134752044448170f);
+        const float rs = frsqrt(s[q]);
         G[q] = gerf_G_erfcx(s[q], e[q], rs);
         Q[q] = fmaf(F_C2 * -0.33333333333333333f, e[q], G[q]) * (rs * rs) * isig2[q];
     }
@@ -258,8 +298,8 @@ __device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q
     if constexpr (K == K_WNKLMNS) {
         // g/rho^3 = (s+2.5)(s+1)^-2.5 ; -H/3 = (s+3.5)(s+1)^-3.5
         const float q = s + 1.0f;
-        const float t = __frcp_rn(q);
-        const float t2u = t * t * rsqrtf(q);
+        const float t = frcp(q);
+        const float t2u = t * t * frsqrt(q);
         G = (s + 2.5f) * t2u;
         Q = (s + 3.5f) * t * t2u * isig2;
     } else if constexpr (K == K_SING) {
@@ -270,7 +310,7 @@ __device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q
         if (s > S_FAR_GAUS) {
             far_GQ(s, isig2, G, Q);
         } else {
-            const float rs = rsqrtf(s);
+            const float rs = frsqrt(s);
             const float rho = s * rs;
             const float t = s * rho;
             if (t < 1.0f) {
@@ -278,7 +318,7 @@ __device__ __forceinline__ void near_GQ(float s, float isig2, float& G, float& Q
                 Q = -rho * gaus_H_series(t) * isig2;
             } else {
                 const float e = expf(-t);
-                G = (1.0f - e) * __frcp_rn(t);
+                G = (1.0f - e) * frcp(t);
                 const float rs2 = rs * rs;
                 Q = fmaf(-t, e, 1.0f - e) * rs2 * rs2 * rs * isig2;   // -H/3 = (1 - e - t e)/rho^5
             }
@@ -337,11 +377,11 @@ __device__ __forceinline__ float zhat_f32(float s)
 {
     if constexpr (K == K_SING) return s == 0.0f ? 1.0f : 0.0f;
     else if constexpr (K == K_GAUS) { const float rho = sqrtf(s); return expf(-s * rho); }
-    else if constexpr (K == K_GAUSERF) return exp2f(s * -0.72134752044448170f);  // e^{-s/2}
+    else if constexpr (K == K_GAUSERF) return fexp2(s * -0.72134752044448170f);  // e^{-s/2}
     else {
         const float q = s + 1.0f;
-        const float t = __frcp_rn(q);
-        return t * t * t * rsqrtf(q);
+        const float t = frcp(q);
+        return t * t * t * frsqrt(q);
     }
 }
 
