@@ -569,14 +569,43 @@ uj_adjoint_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double
     }
 }
 
+// Source splits of the mixed adjoint launch.  The adjoint kernels add their target and source
+// sums with atomics (no split partials), so the count is free: the one that minimises the
+// launch's length in block slots, ceil(blocks / resident slots) x (tiles per block + 1), where
+// the + 1 is a block's fixed cost.  The 127-register mixed kernel holds 4 blocks per SM; at
+// 32,000 particles the forward's rule (8 splits: 2,000 blocks, 3.3 waves of 608) leaves the last
+// wave 29 % full, and this rule's 12 splits (3,000 blocks, 4.9 waves) measured 3.4 % faster.
+// The FP64 adjoint keeps the forward's rule: under this one it measured 6 % slower.
+template <typename Kern>
+static int adj_splits(Kern kern, int64_t tblocks, int64_t tiles, int num_sms)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, UJ_THREADS, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const int64_t slots = (int64_t)per_sm * num_sms;
+    int64_t max_split = tiles / 4 > 1 ? tiles / 4 : 1;         // at least 4 tiles per split
+    if (max_split > 65535) max_split = 65535;                   // gridDim.y
+    int64_t best = 1, best_cost = INT64_MAX;
+    for (int64_t s = 1; s <= max_split; s++) {
+        const int64_t per = (tiles + s - 1) / s;
+        const int64_t used = (tiles + per - 1) / per;              // no empty splits
+        const int64_t cost = ((tblocks * used + slots - 1) / slots) * (per + 1);
+        if (cost < best_cost) { best_cost = cost; best = used; }
+    }
+    return (int)best;
+}
+
 template <int K>
 static cudaError_t launch_adj_k(const AdjArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
                                 int64_t* launches)
 {
     const int64_t ns_pad = (a.n + UJ_TILE - 1) / UJ_TILE * UJ_TILE;
     const int64_t nt_pad = (a.n + UJ_THREADS - 1) / UJ_THREADS * UJ_THREADS;
-    const int nsplit = uj_num_splits(a.n, a.n, num_sms);
     const int64_t tiles = ns_pad / UJ_TILE;
+    const int nsplit = a.precision ? adj_splits(uj_adjoint_mixed_kernel<K>, nt_pad / UJ_THREADS, tiles, num_sms)
+                                   : uj_num_splits(a.n, a.n, num_sms);
     const int64_t per_split = ((tiles + nsplit - 1) / nsplit) * UJ_TILE;
     const TgtPos* tgt = nullptr;
     cudaError_t e = order_targets(a.n, a.x, w.order, w.order_bytes, st, launches, &tgt);
