@@ -17,9 +17,10 @@
 //    G and H are smooth at s = 0, so the cancellation of erf(rho/sqrt2) against
 //    sqrt(2/pi)*rho*exp(-rho^2/2) that the literal formula suffers for small
 //    rho in FP32 never happens.  For the Gaussian-erf kernel G and H come from
-//    their Taylor series for s < 2 (11 terms, < 1e-8 relative), from erf/exp for
-//    2 <= s <= 50, and from the singular form G = s^-1.5, H = -3 s^-2.5 for
-//    s > 50 (rho > 7.07), where the neglected terms are below 2e-9 relative.
+//    their series of positive terms for s < 2 (< 1e-8 relative), from
+//    e^{-s/2} and a fit of erfcx for 2 <= s <= 50 (no erf call), and from the
+//    singular form G = s^-1.5, H = -3 s^-2.5 for s > 50 (rho > 7.07), where the
+//    neglected terms are below 2e-9 relative (gerf_GQ below).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
