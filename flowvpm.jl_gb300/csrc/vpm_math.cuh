@@ -339,29 +339,6 @@ __device__ __forceinline__ void near_GQ4(const float (&s)[4], const float (&isig
     }
 }
 
-// (G, Q) of one pair for the whole warp: the singular form when every lane is
-// past s_far (no divergence), else each lane's full form; pairs with r^2 == 0
-// contribute nothing (src/FLOWVPM_fmm.jl:118).  All 32 lanes must call it.
-template <int K>
-__device__ __forceinline__ void pair_GQ(float r2, float s, float isig2, float& G, float& Q)
-{
-    if constexpr (K == K_WNKLMNS) {
-        near_GQ<K>(s, isig2, G, Q);
-        const bool nz = r2 > 0.0f;
-        G = nz ? G : 0.0f;
-        Q = nz ? Q : 0.0f;
-    } else {
-        if (__all_sync(0xffffffffu, s > s_far<K>())) {
-            far_GQ(s, isig2, G, Q);
-        } else {
-            near_GQ<K>(s, isig2, G, Q);
-            const bool nz = r2 > 0.0f;
-            G = nz ? G : 0.0f;
-            Q = nz ? Q : 0.0f;
-        }
-    }
-}
-
 // s += y, with the rounding error of the addition accumulated in c (Fast2Sum;
 // exact when |s| >= |y|, which a running sum of like terms keeps after its
 // first additions).  s + c is the compensated sum.
