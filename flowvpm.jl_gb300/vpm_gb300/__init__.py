@@ -13,7 +13,7 @@ from .particlefield import (ParticleField, ClassicVPM, ReformulatedVPM, Kernel, 
                             kernel_default, standard_kernels, const1, const2, const3, const4)
 from .timeintegration import (AfterUJ, BeforeUJ, ConstantSFS, CoreSpreading, DynamicSFS, Inviscid,
                               NoSFS, Relaxation, SFS_Cd_twolevel_nobackscatter, SFS_Cs_nobackscatter,
-                              clipping_backscatter, correctedpedrizzetti, isSFSenabled, noSFS,
+                              clipping_backscatter, correctedpedrizzetti, euler, isSFSenabled, noSFS,
                               norelaxation, pedrizzetti, rbf_conjugategradient, rungekutta3, run_vpm,
                               update_particle_states)
 from .uj import UJ_gb300, UJ_gb300_cross, UJ_gb300_mixed, zeta_fmm_gb300, zeta_gb300, zeta_gb300_mixed

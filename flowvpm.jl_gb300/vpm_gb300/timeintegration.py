@@ -1,5 +1,5 @@
 """Host-side mirror of the reference's consumers of UJ: the rVPM low-storage RK3
-(src/FLOWVPM_timeintegration.jl:388-532), relaxation
+(src/FLOWVPM_timeintegration.jl:388-532) and first-order Euler (:23-37,103-173), relaxation
 (src/FLOWVPM_relaxation.jl), the SFS schemes with the pseudo-three-level dynamic
 procedure (src/FLOWVPM_subfilterscale.jl) and the core-spreading viscous scheme
 (src/FLOWVPM_viscous.jl:152-223).
@@ -114,15 +114,22 @@ def viscousdiffusion(pfield: ParticleField, dt: float, aux1: float = 0.0, aux2: 
         return
     if not isinstance(scheme, CoreSpreading):
         raise NotImplementedError(f"viscous scheme {type(scheme).__name__} is not supported")
-    if pfield.integration is not rungekutta3:
-        raise NotImplementedError("core spreading is mirrored for rungekutta3 only")
     idx = _live(pfield)
     P = pfield.particles
-    M7 = aux1 * P[27 + 6, idx] + dt * 2 * scheme.nu
-    P[27 + 6, idx] = M7
-    s = P[SIGMA_INDEX, idx]
-    P[SIGMA_INDEX, idx] = np.sqrt(s ** 2 + aux2 * M7)
-    if abs(aux2 - 8 / 15) <= 1e-7:
+    if pfield.integration is euler:                                 # src/FLOWVPM_viscous.jl:155-162
+        s = P[SIGMA_INDEX, idx]
+        P[SIGMA_INDEX, idx] = np.sqrt(s * s + 2 * scheme.nu * dt)
+        proceed = True
+    elif pfield.integration is rungekutta3:                         # :165-178
+        M7 = aux1 * P[27 + 6, idx] + dt * 2 * scheme.nu
+        P[27 + 6, idx] = M7
+        s = P[SIGMA_INDEX, idx]
+        P[SIGMA_INDEX, idx] = np.sqrt(s ** 2 + aux2 * M7)
+        proceed = abs(aux2 - 8 / 15) <= 1e-7
+    else:
+        raise NotImplementedError(f"time integration scheme {pfield.integration} is not implemented in the "
+                                  "core spreading viscous scheme")
+    if proceed:
         scheme.t_sgm += dt
         beta_cur = math.sqrt(2 * scheme.nu * scheme.t_sgm / scheme.sgm0 ** 2 + 1)
         if beta_cur >= scheme.beta:
@@ -377,6 +384,49 @@ def rungekutta3(pfield: ParticleField, dt: float, *, relax: bool = False, custom
         _reset_particles(pfield)
         pfield.UJ(pfield)
         pfield.relaxation(pfield)
+
+
+def euler(pfield: ParticleField, dt: float, *, relax: bool = False, custom_UJ=None):
+    """First-order Euler step, src/FLOWVPM_timeintegration.jl:23-37 (the SFS
+    model's hooks around one UJ) and the reformulated-VPM update of :103-173:
+    X += dt (U + Uinf); Gamma += dt (S - 3 Z Gamma - C SFS sigma^3/zeta0);
+    sigma -= dt sigma Z; then relaxation with the step's J, and viscous diffusion."""
+    if not isinstance(pfield.formulation, ReformulatedVPM):
+        raise NotImplementedError("euler is mirrored for ReformulatedVPM formulations")
+    sfs_on = isSFSenabled(pfield.SFS)
+    pfield.SFS(pfield, BeforeUJ)
+    UJ = pfield.UJ if custom_UJ is None else custom_UJ
+    UJ(pfield, reset_sfs=sfs_on, reset=True, sfs=sfs_on)
+    pfield.SFS(pfield, AfterUJ)
+    Uinf = np.asarray(pfield.Uinf(pfield.t), dtype=np.float64)
+    f, g = pfield.formulation.f, pfield.formulation.g
+    zeta0 = pfield.kernel.zeta(0.0)
+    P = pfield.particles
+    idx = _live(pfield)
+    C = P[C_INDEX.start, idx]
+    X = P[X_INDEX, idx]
+    U = P[U_INDEX, idx]
+    for k in range(3):
+        X[k] += dt * (U[k] + Uinf[k])
+    G = P[GAMMA_INDEX, idx]
+    SFS = P[SFS_INDEX, idx]
+    sigma = P[SIGMA_INDEX, idx]
+    MM = _stretch(P[J_INDEX, idx], G, pfield.transposed)
+    Gnorm2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2]
+    pos = Gnorm2 > 0
+    MM4 = (f + g) / (1 + 3 * f) * (MM[0] * G[0] + MM[1] * G[1] + MM[2] * G[2])
+    sigma3 = sigma * sigma * sigma                 # Julia's literal power
+    MM4 = MM4 - f / (1 + 3 * f) * (C * SFS[0] * G[0] + C * SFS[1] * G[1] + C * SFS[2] * G[2]) * sigma3 / zeta0
+    MM4 = np.where(pos, MM4 / np.where(pos, G[0] * G[0] + G[1] * G[1] + G[2] * G[2], 1.0), 0.0)
+    for k in range(3):
+        G[k] += dt * (MM[k] - 3 * MM4 * G[k] - C * SFS[k] * sigma3 / zeta0)
+    sigma = sigma - dt * (sigma * MM4)
+    P[X_INDEX, idx] = X
+    P[GAMMA_INDEX, idx] = G
+    P[SIGMA_INDEX, idx] = sigma
+    if relax:   # per particle in the reference, with this step's J: the same as one pass over all
+        pfield.relaxation(pfield, idx)
+    viscousdiffusion(pfield, dt)
 
 
 def run_vpm(pfield: ParticleField, dt: float, nsteps: int, *, runtime_function=None):

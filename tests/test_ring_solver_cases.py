@@ -1,0 +1,125 @@
+"""The reference's single-vortex-ring solver matrix
+(test/runtests_singlevortexring.jl:21-32, criteria :141-149) through the host
+mirror, with the oracle as pfield.UJ: R = 1, Nphi = 100, sigma = Rcross =
+0.15 R, faux = 0.25, Pedrizzetti relaxation every step, transposed scheme,
+50 steps over 2 radii of travel; Winckelmans when inviscid, Gaussian-erf with
+core spreading (nu = 1.48e-5, sgm0 = 2 pi R/100/2 (1 + 0.3)).  The ring's
+speed must be within 2 % of Uring (inviscid) or below it by less than 50 %
+(viscous); the two Euler + SFS cases only have to run, as in the reference.
+The reference runs UJ_fmm in eight of the ten; with 100 to 900 particles its
+far-field truncation is immaterial, and UJ_direct is evaluated here, so its
+"Euler + direct UJ" and "FMM UJ" cases coincide.  Forward Euler at this dt
+does not keep the ring axisymmetric: a rounding-level asymmetry grows about
+100x every 5 steps and deforms the ring by the last steps (radius spread 0.3
+at step 50); the circulation-weighted centroid still moves within 1 % of
+Uring.  The oracle sums in a fixed order, so every case is deterministic.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import vpm_gb300 as vpm
+import vpm_gb300.rings as rings
+
+R, NPHI, NSTEPS, RTOT, BETA = 1.0, 100, 50, 2.0, 0.5
+NU, SGM0 = 1.48e-5, 2 * math.pi * R / 100 / 2 * (1 + 0.3)
+
+
+def _uj_oracle(pfield, rbf=False, sfs=False, reset=True, reset_sfs=False, **kw):
+    flags = (oracle.RESET if reset else 0) | (oracle.RESET_SFS if reset_sfs else 0) | \
+            (oracle.SFS if sfs else 0) | (oracle.TRANSPOSED if pfield.transposed else 0)
+    oracle.uj_direct(pfield.particles, pfield.np, pfield.kernel.kid, flags)
+
+
+def _zeta_oracle(pfield):
+    """zeta_direct: rows 16:18 of every particle receive the basis field."""
+    n, P = pfield.np, pfield.particles
+    P[15:18, :n] = oracle.zeta_pairs(P[0:3, :n].T, P[0:3, :n].T, P[3:6, :n].T, P[6, :n], pfield.kernel.kid).T
+
+
+CASES = [  # (description, integration, nc, formulation, viscous, SFS, test_error)
+    ("Euler time-integration + direct UJ", "euler", 0, "cVPM", False, None, True),
+    ("Runge-Kutta time-integration + direct UJ", "rk3", 0, "cVPM", False, None, True),
+    ("Full inviscid scheme", "rk3", 1, "cVPM", False, None, True),
+    ("Reformulation", "rk3", 1, "rVPM", False, None, True),
+    ("Viscous scheme", "rk3", 1, "cVPM", True, None, True),
+    ("Constant SFS + Euler", "euler", 0, "rVPM", False, "constant", False),
+    ("Constant SFS + RK3", "rk3", 0, "rVPM", False, "constant", True),
+    ("Dynamic SFS + Euler", "euler", 0, "rVPM", False, "dynamic", False),
+    ("Dynamic SFS + RK3", "rk3", 0, "rVPM", False, "dynamic", True),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_reference_ring_solver_case(case):
+    _, integ, nc, form, viscous, sfs, test_error = case
+    Rcross = 0.15 * R
+    visc = vpm.CoreSpreading(NU, SGM0, zeta=_zeta_oracle) if viscous else vpm.Inviscid()
+    SFS = {None: vpm.noSFS, "constant": vpm.ConstantSFS(), "dynamic": vpm.DynamicSFS()}[sfs]
+    pf = vpm.ParticleField(rings.number_particles(NPHI, nc), formulation=getattr(vpm, form),
+                           kernel=vpm.gaussianerf if viscous else vpm.winckelmans, UJ=_uj_oracle,
+                           relaxation=vpm.pedrizzetti, viscous=visc, SFS=SFS, transposed=True,
+                           integration=vpm.euler if integ == "euler" else vpm.rungekutta3)
+    rings.addvortexring(pf, 1.0, R, 1.0, 0.25 * Rcross, NPHI, nc, Rcross)
+    Uref = rings.Uring(1.0, R, Rcross, BETA)
+    dt = (RTOT / Uref) / NSTEPS
+    vpm.run_vpm(pf, dt, NSTEPS)
+    assert abs(pf.t - NSTEPS * dt) < 1e-12
+    P = pf.particles[:, :pf.np]
+    assert np.isfinite(P[0:7]).all()
+    Z = rings.calc_rings_weighted(pf, [0, pf.np])[0][0]
+    err = (np.linalg.norm(Z) / pf.t - Uref) / Uref
+    if test_error:
+        if viscous:
+            assert err < 0 and abs(err) < 0.5, err
+        else:
+            assert abs(err) < 0.02, err
+
+
+def test_euler_step_matches_the_reference_update():
+    """One Euler step of a small rVPM field with the SFS term on, against the
+    reformulated update of src/FLOWVPM_timeintegration.jl:103-173 written out
+    per particle (the reference's loop) on a copy of the same UJ output."""
+    rng = np.random.default_rng(5)
+    n = 24
+    pf = vpm.ParticleField(n, formulation=vpm.rVPM, kernel=vpm.gaussianerf, UJ=_uj_oracle,
+                           SFS=vpm.ConstantSFS(), integration=vpm.euler, transposed=True)
+    for i in range(n):
+        pf.add_particle(rng.uniform(-1, 1, 3), rng.normal(0, 0.1, 3), rng.uniform(0.2, 0.4), vol=0.01,
+                        static=(i == 3))                                # one static particle
+    dt = 0.01
+    # the UJ and C the step will see
+    ref = vpm.ParticleField(n, formulation=vpm.rVPM, kernel=vpm.gaussianerf, UJ=_uj_oracle,
+                            SFS=vpm.ConstantSFS(), transposed=True)
+    ref.particles[:] = pf.particles
+    ref.np = pf.np
+    _uj_oracle(ref, sfs=True, reset=True, reset_sfs=True)
+    ref.SFS(ref, vpm.AfterUJ)
+    P = ref.particles.copy()
+    f, g = 0.0, 1 / 5
+    zeta0 = ref.kernel.zeta(0.0)
+    for i in range(n):
+        if P[42, i] != 0:
+            continue
+        C = P[36, i]
+        P[0:3, i] += dt * P[9:12, i]
+        J, G = P[15:24, i], P[3:6, i]
+        MM = [J[0] * G[0] + J[1] * G[1] + J[2] * G[2], J[3] * G[0] + J[4] * G[1] + J[5] * G[2],
+              J[6] * G[0] + J[7] * G[1] + J[8] * G[2]]
+        MM4 = (f + g) / (1 + 3 * f) * (MM[0] * G[0] + MM[1] * G[1] + MM[2] * G[2])
+        MM4 -= f / (1 + 3 * f) * (C * P[39, i] * G[0] + C * P[40, i] * G[1] + C * P[41, i] * G[2]) * \
+            P[6, i] ** 3 / zeta0
+        MM4 /= G[0] ** 2 + G[1] ** 2 + G[2] ** 2
+        s3 = P[6, i] ** 3
+        G0 = G.copy()
+        for k in range(3):
+            P[3 + k, i] = G0[k] + dt * (MM[k] - 3 * MM4 * G0[k] - C * P[39 + k, i] * s3 / zeta0)
+        P[6, i] -= dt * (P[6, i] * MM4)
+    vpm.euler(pf, dt)
+    live = pf.particles[42, :n] == 0
+    for rows in (slice(0, 3), slice(3, 6), slice(6, 7)):
+        a, b = pf.particles[rows, :n][:, live], P[rows, :n][:, live]
+        assert np.abs(a - b).max() <= 1e-15 * max(1.0, np.abs(b).max())
+    assert np.array_equal(pf.particles[0:7, 3], ref.particles[0:7, 3])    # the static particle stays
