@@ -9,7 +9,8 @@ CPU fallback.
 from . import _lib
 from ._lib import (FP32COMP, FP64, Context, VPMError, default_context, load)
 from .particlefield import (ParticleField, ClassicVPM, ReformulatedVPM, Kernel, cVPM, rVPM,
-                            formulation_default, gaussian, gaussianerf, singular, winckelmans,
+                            formulation_classic, formulation_default, gaussian, gaussianerf, singular,
+                            winckelmans,
                             kernel_default, standard_kernels, const1, const2, const3, const4)
 from .timeintegration import (AfterUJ, BeforeUJ, ConstantSFS, CoreSpreading, DynamicSFS, Inviscid,
                               NoSFS, Relaxation, SFS_Cd_twolevel_nobackscatter, SFS_Cs_nobackscatter,

@@ -92,7 +92,8 @@ class ReformulatedVPM:
         return (1 - 3 * self.g) / (1 + 3 * self.f)
 
 
-formulation_cVPM = cVPM = ReformulatedVPM(0.0, 0.0)          # src/FLOWVPM.jl:85
+formulation_classic = ClassicVPM()                            # src/FLOWVPM.jl:83
+formulation_cVPM = cVPM = ReformulatedVPM(0.0, 0.0)          # :84
 formulation_rVPM = rVPM = ReformulatedVPM(0.0, 1 / 5)         # :86
 formulation_tube_continuity = ReformulatedVPM(1 / 2, 0.0)     # :94
 formulation_tube_momentum = ReformulatedVPM(1 / 4, 1 / 4)     # :102

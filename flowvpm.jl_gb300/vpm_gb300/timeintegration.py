@@ -17,8 +17,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .particlefield import (C_INDEX, GAMMA_INDEX, J_INDEX, M_INDEX, SFS_INDEX, SIGMA_INDEX,
-                            STATIC_INDEX, U_INDEX, VOL_INDEX, X_INDEX, ParticleField, ReformulatedVPM,
-                            _reset_particles)
+                            STATIC_INDEX, U_INDEX, VOL_INDEX, X_INDEX, ClassicVPM, ParticleField,
+                            ReformulatedVPM, _reset_particles)
 
 EPS = 2.220446049250313e-16  # Julia eps()
 
@@ -365,6 +365,10 @@ def update_particle_states(pfield: ParticleField, a, b, dt, Uinf, f, g, zeta0):
 
 def rungekutta3(pfield: ParticleField, dt: float, *, relax: bool = False, custom_UJ=None):
     """Low-storage RK3 for the reformulated VPM, src/FLOWVPM_timeintegration.jl:388-461."""
+    if isinstance(pfield.formulation, ClassicVPM):
+        raise NotImplementedError(
+            "rungekutta3 with ClassicVPM: the reference's method (src/FLOWVPM_timeintegration.jl:185-262) "
+            "passes f and g, which it never defines, to update_particle_states and fails with UndefVarError")
     if not isinstance(pfield.formulation, ReformulatedVPM):
         raise NotImplementedError("rungekutta3 is mirrored for ReformulatedVPM formulations")
     Uinf = np.asarray(pfield.Uinf(pfield.t), dtype=np.float64)
@@ -386,19 +390,56 @@ def rungekutta3(pfield: ParticleField, dt: float, *, relax: bool = False, custom
         pfield.relaxation(pfield)
 
 
+def _euler_classic(pfield: ParticleField, dt: float, relax: bool, Uinf, zeta0):
+    """The ClassicVPM update of src/FLOWVPM_timeintegration.jl:42-91.  The
+    reference adds the stretching to Gamma one component at a time, in place,
+    so the second component's stretching already sees the updated first and
+    the third sees both; that order is kept."""
+    P = pfield.particles
+    idx = _live(pfield)
+    C = P[C_INDEX.start, idx]
+    X = P[X_INDEX, idx]
+    U = P[U_INDEX, idx]
+    for k in range(3):
+        X[k] += dt * (U[k] + Uinf[k])
+    J = P[J_INDEX, idx]
+    G = P[GAMMA_INDEX, idx]
+    if pfield.transposed:
+        G[0] += dt * (J[0] * G[0] + J[1] * G[1] + J[2] * G[2])
+        G[1] += dt * (J[3] * G[0] + J[4] * G[1] + J[5] * G[2])
+        G[2] += dt * (J[6] * G[0] + J[7] * G[1] + J[8] * G[2])
+    else:
+        G[0] += dt * (J[0] * G[0] + J[3] * G[1] + J[6] * G[2])
+        G[1] += dt * (J[1] * G[0] + J[4] * G[1] + J[7] * G[2])
+        G[2] += dt * (J[2] * G[0] + J[5] * G[1] + J[8] * G[2])
+    sigma = P[SIGMA_INDEX, idx]
+    SFS = P[SFS_INDEX, idx]
+    for k in range(3):
+        G[k] -= dt * C * SFS[k] * (sigma * sigma * sigma) / zeta0
+    P[X_INDEX, idx] = X
+    P[GAMMA_INDEX, idx] = G
+    if relax:
+        pfield.relaxation(pfield, idx)
+    viscousdiffusion(pfield, dt)
+
+
 def euler(pfield: ParticleField, dt: float, *, relax: bool = False, custom_UJ=None):
     """First-order Euler step, src/FLOWVPM_timeintegration.jl:23-37 (the SFS
     model's hooks around one UJ) and the reformulated-VPM update of :103-173:
     X += dt (U + Uinf); Gamma += dt (S - 3 Z Gamma - C SFS sigma^3/zeta0);
-    sigma -= dt sigma Z; then relaxation with the step's J, and viscous diffusion."""
-    if not isinstance(pfield.formulation, ReformulatedVPM):
-        raise NotImplementedError("euler is mirrored for ReformulatedVPM formulations")
+    sigma -= dt sigma Z; then relaxation with the step's J, and viscous diffusion.
+    ClassicVPM takes the update of :42-91 (_euler_classic)."""
+    if not isinstance(pfield.formulation, (ReformulatedVPM, ClassicVPM)):
+        raise NotImplementedError(f"euler: unknown formulation {type(pfield.formulation).__name__}")
     sfs_on = isSFSenabled(pfield.SFS)
     pfield.SFS(pfield, BeforeUJ)
     UJ = pfield.UJ if custom_UJ is None else custom_UJ
     UJ(pfield, reset_sfs=sfs_on, reset=True, sfs=sfs_on)
     pfield.SFS(pfield, AfterUJ)
     Uinf = np.asarray(pfield.Uinf(pfield.t), dtype=np.float64)
+    if isinstance(pfield.formulation, ClassicVPM):
+        _euler_classic(pfield, dt, relax, Uinf, pfield.kernel.zeta(0.0))
+        return
     f, g = pfield.formulation.f, pfield.formulation.g
     zeta0 = pfield.kernel.zeta(0.0)
     P = pfield.particles

@@ -123,3 +123,56 @@ def test_euler_step_matches_the_reference_update():
         a, b = pf.particles[rows, :n][:, live], P[rows, :n][:, live]
         assert np.abs(a - b).max() <= 1e-15 * max(1.0, np.abs(b).max())
     assert np.array_equal(pf.particles[0:7, 3], ref.particles[0:7, 3])    # the static particle stays
+
+
+@pytest.mark.parametrize("transposed", [True, False])
+def test_classic_euler_step_matches_the_reference_loop(transposed):
+    """formulation_classic under Euler (src/FLOWVPM_timeintegration.jl:42-91):
+    Gamma's components take their stretching one at a time, in place, so the
+    second sees the updated first; then the SFS term.  Against that loop per
+    particle on the same UJ output."""
+    rng = np.random.default_rng(11)
+    n = 20
+    mk = lambda: vpm.ParticleField(n, formulation=vpm.formulation_classic, kernel=vpm.gaussianerf, UJ=_uj_oracle,
+                                   SFS=vpm.ConstantSFS(), integration=vpm.euler, transposed=transposed)
+    pf = mk()
+    for i in range(n):
+        pf.add_particle(rng.uniform(-1, 1, 3), rng.normal(0, 0.1, 3), rng.uniform(0.2, 0.4), vol=0.01,
+                        static=(i == 5))
+    ref = mk()
+    ref.particles[:] = pf.particles
+    ref.np = pf.np
+    _uj_oracle(ref, sfs=True, reset=True, reset_sfs=True)
+    ref.SFS(ref, vpm.AfterUJ)
+    P = ref.particles.copy()
+    dt, zeta0 = 0.02, ref.kernel.zeta(0.0)
+    for i in range(n):
+        if P[42, i] != 0:
+            continue
+        C = P[36, i]
+        P[0:3, i] += dt * P[9:12, i]
+        J = P[15:24, i]
+        if transposed:
+            P[3, i] += dt * (J[0] * P[3, i] + J[1] * P[4, i] + J[2] * P[5, i])
+            P[4, i] += dt * (J[3] * P[3, i] + J[4] * P[4, i] + J[5] * P[5, i])
+            P[5, i] += dt * (J[6] * P[3, i] + J[7] * P[4, i] + J[8] * P[5, i])
+        else:
+            P[3, i] += dt * (J[0] * P[3, i] + J[3] * P[4, i] + J[6] * P[5, i])
+            P[4, i] += dt * (J[1] * P[3, i] + J[4] * P[4, i] + J[7] * P[5, i])
+            P[5, i] += dt * (J[2] * P[3, i] + J[5] * P[4, i] + J[8] * P[5, i])
+        P[3:6, i] -= dt * C * P[39:42, i] * P[6, i] ** 3 / zeta0
+    vpm.euler(pf, dt)
+    live = pf.particles[42, :n] == 0
+    for rows in (slice(0, 3), slice(3, 6)):
+        a, b = pf.particles[rows, :n][:, live], P[rows, :n][:, live]
+        assert np.abs(a - b).max() <= 1e-15 * max(1.0, np.abs(b).max())
+    assert np.array_equal(pf.particles[6, :n], ref.particles[6, :n])      # sigma is not updated
+
+
+def test_classic_rk3_fails_as_the_reference_does():
+    """The reference's ClassicVPM rungekutta3 (src/FLOWVPM_timeintegration.jl:185-262)
+    passes f and g, which it never defines, and fails with UndefVarError."""
+    pf = vpm.ParticleField(4, formulation=vpm.formulation_classic, UJ=_uj_oracle)
+    pf.add_particle([0.0, 0.0, 0.0], [0.0, 0.0, 1.0], 0.1)
+    with pytest.raises(NotImplementedError, match="never defines"):
+        vpm.rungekutta3(pf, 0.01)
