@@ -176,3 +176,29 @@ def test_classic_rk3_fails_as_the_reference_does():
     pf.add_particle([0.0, 0.0, 0.0], [0.0, 0.0, 1.0], 0.1)
     with pytest.raises(NotImplementedError, match="never defines"):
         vpm.rungekutta3(pf, 0.01)
+
+
+@pytest.mark.parametrize("integ", ["euler", "rk3"])
+def test_core_spreading_reset_runs_the_rbf_solve(integ):
+    """With nu large enough that sigma/sgm0 passes beta = 1.5 in the first
+    step, core spreading resets the cores (src/FLOWVPM_viscous.jl:190-223): the
+    basis field of the current strengths becomes the target vorticity, sigma
+    returns to sgm0, and the RBF conjugate gradient (:314-454, with the oracle's
+    zeta) finds new strengths; it raises if it does not converge."""
+    Rcross = 0.15 * R
+    sgm0 = Rcross
+    dt = 0.05
+    nu = (1.5 ** 2 - 1) * sgm0 ** 2 / (2 * dt) * 1.01
+    cs = vpm.CoreSpreading(nu, sgm0, zeta=_zeta_oracle)
+    pf = vpm.ParticleField(rings.number_particles(40, 0), formulation=vpm.cVPM, kernel=vpm.gaussianerf,
+                           UJ=_uj_oracle, viscous=cs, transposed=True,
+                           integration=vpm.euler if integ == "euler" else vpm.rungekutta3)
+    rings.addvortexring(pf, 1.0, R, 1.0, 0.25 * Rcross, 40, 0, Rcross)
+    G0 = pf.particles[3:6, :pf.np].copy()
+    pf.nextstep(dt)
+    P = pf.particles[:, :pf.np]
+    assert cs.t_sgm == 0.0                                   # the reset happened and restarted the timer
+    assert np.allclose(P[6], sgm0, rtol=0, atol=1e-15)
+    assert np.isfinite(P[3:6]).all()
+    # the new strengths represent the spread vorticity: same total circulation direction, larger cores
+    assert np.sum(P[3:6] * G0) > 0
