@@ -192,10 +192,13 @@ class ParticleField:
         from .timeintegration import isSFSenabled
         return isSFSenabled(self.SFS)
 
-    def nextstep(self, dt: float, *, relax: bool = False, update_U_prev: bool = True):
+    def nextstep(self, dt: float, *, relax: bool = False, update_U_prev: bool = True, custom_UJ=None):
         """src/FLOWVPM_particlefield.jl:435-460"""
         if self.np != 0:
-            self.integration(self, dt, relax=relax)
+            if custom_UJ is None:
+                self.integration(self, dt, relax=relax)
+            else:
+                self.integration(self, dt, relax=relax, custom_UJ=custom_UJ)
         if update_U_prev:
             U = self.particles[U_INDEX, :self.np]
             self.particles[U_PREV_INDEX, :self.np] = np.sqrt(U[0] * U[0] + U[1] * U[1] + U[2] * U[2])

@@ -470,13 +470,35 @@ def euler(pfield: ParticleField, dt: float, *, relax: bool = False, custom_UJ=No
     viscousdiffusion(pfield, dt)
 
 
-def run_vpm(pfield: ParticleField, dt: float, nsteps: int, *, runtime_function=None):
-    """The stepping loop of run_vpm! (src/FLOWVPM_utils.jl:89-136) without I/O."""
+def _kernel_compatibility(viscous) -> tuple:
+    """src/FLOWVPM.jl:259-267: the kernels each viscous scheme accepts."""
+    from .particlefield import gaussian, gaussianerf, singular, winckelmans
+    if isinstance(viscous, CoreSpreading):
+        return (gaussianerf,)
+    return (singular, gaussian, gaussianerf, winckelmans)
+
+
+def run_vpm(pfield: ParticleField, dt: float, nsteps: int, *, runtime_function=None,
+            static_particles_function=None, custom_UJ=None):
+    """The stepping loop of run_vpm! (src/FLOWVPM_utils.jl:41-136) without I/O:
+    the kernel/viscous-scheme check, relaxation every nsteps_relax steps, static
+    particles added by static_particles_function(pfield, t, dt) before each step
+    and removed after it (unless it returns False), and runtime_function(pfield,
+    t, dt) after each step, which ends the run by returning True."""
+    if not any(pfield.kernel is k for k in _kernel_compatibility(pfield.viscous)):
+        raise ValueError(f"Kernel {pfield.kernel} is not compatible with viscous scheme "
+                         f"{type(pfield.viscous).__name__}; compatible kernels are "
+                         f"{list(_kernel_compatibility(pfield.viscous))}")
     rlx = pfield.relaxation
     for i in range(nsteps + 1):
         relax = (rlx is not relaxation_none and rlx.nsteps_relax >= 1 and i > 0
                  and i % rlx.nsteps_relax == 0)
+        org_np = pfield.np
         if i != 0:
-            pfield.nextstep(dt, relax=relax)
+            remove = static_particles_function(pfield, pfield.t, dt) if static_particles_function else None
+            pfield.nextstep(dt, relax=relax, custom_UJ=custom_UJ)
+            if remove is None or remove:
+                for pi in range(pfield.np - 1, org_np - 1, -1):
+                    pfield.remove_particle(pi)
         if runtime_function is not None and runtime_function(pfield, pfield.t, dt):
             break

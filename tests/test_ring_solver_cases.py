@@ -202,3 +202,41 @@ def test_core_spreading_reset_runs_the_rbf_solve(integ):
     assert np.isfinite(P[3:6]).all()
     # the new strengths represent the spread vorticity: same total circulation direction, larger cores
     assert np.sum(P[3:6] * G0) > 0
+
+
+def test_run_vpm_static_particles_custom_UJ_and_kernel_check():
+    """run_vpm! (src/FLOWVPM_utils.jl:41-136): static particles added before each
+    step take part in that step's UJ and are removed after it; custom_UJ replaces
+    pfield.UJ; a kernel the viscous scheme does not accept is an error."""
+    Rcross = 0.15 * R
+
+    def field():
+        pf = vpm.ParticleField(rings.number_particles(40, 0) + 1, formulation=vpm.rVPM, kernel=vpm.winckelmans,
+                               UJ=_uj_oracle, relaxation=vpm.pedrizzetti, transposed=True)
+        rings.addvortexring(pf, 1.0, R, 1.0, 0.25 * Rcross, 40, 0, Rcross)
+        return pf
+
+    calls = []
+
+    def static(pfield, t, dt):      # one static particle on the axis, strength along x
+        pfield.add_particle([0.0, 0.0, 0.5], [0.05, 0.0, 0.0], 0.2, static=True)
+        calls.append(pfield.np)
+
+    a, b = field(), field()
+    vpm.run_vpm(a, 0.05, 4)
+    vpm.run_vpm(b, 0.05, 4, static_particles_function=static)
+    assert b.np == a.np == 40 and calls == [41] * 4
+    assert np.abs(b.particles[0:3, :40] - a.particles[0:3, :40]).max() > 1e-6     # the statics acted
+    n_uj = []
+
+    def counting_UJ(pfield, **kw):
+        n_uj.append(1)
+        _uj_oracle(pfield, **kw)
+
+    c = field()
+    vpm.run_vpm(c, 0.05, 2, custom_UJ=counting_UJ)
+    assert len(n_uj) == 2 * 3                                 # the stages' UJ; relaxation keeps pfield.UJ
+    assert np.array_equal(c.particles[:, :40], (lambda f: (vpm.run_vpm(f, 0.05, 2), f.particles[:, :40])[1])(field()))
+    d = vpm.ParticleField(4, kernel=vpm.winckelmans, UJ=_uj_oracle, viscous=vpm.CoreSpreading(1e-4, 0.1))
+    with pytest.raises(ValueError, match="not compatible"):
+        vpm.run_vpm(d, 0.01, 1)
