@@ -358,6 +358,7 @@ const char* vpm_build_info(void)
 
 int vpm_ctx_create(vpm_ctx** out, int device)
 {
+    vpm::TraceRange trace_("vpm_ctx_create");
     if (!out) return fail(nullptr, VPM_ERR_ARG, "vpm_ctx_create: out is NULL");
     *out = nullptr;
     int n = 0;
@@ -392,6 +393,7 @@ int vpm_ctx_create(vpm_ctx** out, int device)
 
 int vpm_ctx_destroy(vpm_ctx* c)
 {
+    vpm::TraceRange trace_("vpm_ctx_destroy");
     if (!c) return VPM_OK;
     {
         std::lock_guard<std::mutex> lk(c->mu);
@@ -431,10 +433,22 @@ int vpm_ctx_set_timeout(vpm_ctx* c, double seconds)
     return VPM_OK;
 }
 
+int vpm_ctx_set_near_capacity(vpm_ctx* c, int64_t frontier_pairs, int64_t near_pairs)
+{
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_ctx_set_near_capacity: ctx is NULL");
+    if (frontier_pairs < 1 || near_pairs < 1 || frontier_pairs > ((int64_t)1 << 34) || near_pairs > ((int64_t)1 << 34))
+        return fail(c, VPM_ERR_ARG, "vpm_ctx_set_near_capacity: capacities must be in 1..2^34 pairs");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->near.capF = (size_t)frontier_pairs;
+    c->near.capN = (size_t)near_pairs;
+    return VPM_OK;
+}
+
 int64_t vpm_launch_count(const vpm_ctx* c) { return c ? c->launches : 0; }
 
 int vpm_probe_ffma(vpm_ctx* c, double* tflops)
 {
+    vpm::TraceRange trace_("vpm_probe_ffma");
     if (!c || !tflops) return fail(c, VPM_ERR_ARG, "vpm_probe_ffma: NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -625,6 +639,7 @@ static int uj_staged(vpm_ctx* c, double* particles, int64_t np, int kernel, int 
 
 int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, int precision, int flags)
 {
+    vpm::TraceRange trace_("vpm_uj");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -643,6 +658,7 @@ int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, in
 int vpm_uj_cross(vpm_ctx* c, const double* src, int64_t ld_src, int64_t ns, double* tgt, int64_t ld_tgt,
                  int64_t nt, int kernel, int precision)
 {
+    vpm::TraceRange trace_("vpm_uj_cross");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_cross: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -690,6 +706,7 @@ int vpm_uj_cross(vpm_ctx* c, const double* src, int64_t ld_src, int64_t ns, doub
 int vpm_uj_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const double* xs, const double* gs,
                const double* sgs, double* U, double* J, int kernel, int precision)
 {
+    vpm::TraceRange trace_("vpm_uj_dev");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -715,6 +732,7 @@ int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, con
                  const double* xs, const double* gs, const double* sgs, const double* Js, const uint8_t* static_s,
                  double* SFS, int kernel, int precision, int flags)
 {
+    vpm::TraceRange trace_("vpm_estr_dev");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_estr_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -744,6 +762,7 @@ int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, con
 int vpm_zeta_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const double* xs, const double* gs,
                  const double* sgs, double* W, int kernel, int precision)
 {
+    vpm::TraceRange trace_("vpm_zeta_dev");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_zeta_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -767,6 +786,7 @@ int vpm_zeta_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const dou
 
 int vpm_zeta(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, int precision)
 {
+    vpm::TraceRange trace_("vpm_zeta");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_zeta: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
@@ -812,6 +832,7 @@ int vpm_dynamic_diff_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
                          const double* J, double alpha, double* dJ, double* dSFS, int kernel, int precision,
                          int flags)
 {
+    vpm::TraceRange trace_("vpm_dynamic_diff_dev");
     const char* fn = "vpm_dynamic_diff_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -931,6 +952,7 @@ int vpm_p2p_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
                          const uint8_t* static_flags, double* U, double* J, double* SFS, int leaf_size,
                          double theta, int kernel, int precision, int flags, int64_t* stats)
 {
+    vpm::TraceRange trace_("vpm_p2p_leaflist_dev");
     const char* fn = "vpm_p2p_leaflist_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -952,6 +974,7 @@ int vpm_rk3_stage_dev(vpm_ctx* c, int64_t n, double a, double b, double dt, cons
                       double zeta0, double nu, int flags, double* x, double* gam, double* sig, const double* U,
                       const double* J, const double* SFS, const double* C, double* M)
 {
+    vpm::TraceRange trace_("vpm_rk3_stage_dev");
     const char* fn = "vpm_rk3_stage_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -978,6 +1001,7 @@ int vpm_rk3_stage_dev(vpm_ctx* c, int64_t n, double a, double b, double dt, cons
 
 int vpm_relax_dev(vpm_ctx* c, int64_t n, double rlxf, const double* J, double* gam)
 {
+    vpm::TraceRange trace_("vpm_relax_dev");
     const char* fn = "vpm_relax_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -995,6 +1019,7 @@ int vpm_dynamic_after_dev(vpm_ctx* c, int64_t n, double alpha, double rlxf, doub
                           int flags, const double* gam, const double* sig, const double* J, const double* SFS,
                           double* C, double* M)
 {
+    vpm::TraceRange trace_("vpm_dynamic_after_dev");
     const char* fn = "vpm_dynamic_after_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -1031,6 +1056,7 @@ int vpm_dynamic_after_dev(vpm_ctx* c, int64_t n, double alpha, double rlxf, doub
 int vpm_zeta_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig, double* W,
                           int leaf_size, double theta, int kernel, int precision, int flags, int64_t* stats)
 {
+    vpm::TraceRange trace_("vpm_zeta_leaflist_dev");
     const char* fn = "vpm_zeta_leaflist_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -1067,6 +1093,7 @@ int vpm_dynamic_diff_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, const 
                                   double* dSFS, int leaf_size, double theta, int kernel, int precision, int flags,
                                   int64_t* stats)
 {
+    vpm::TraceRange trace_("vpm_dynamic_diff_leaflist_dev");
     const char* fn = "vpm_dynamic_diff_leaflist_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -1135,6 +1162,7 @@ int vpm_p2p_lists_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam,
                       int64_t nl, const int64_t* leaf_begin, const int64_t* leaf_end, const int64_t* row,
                       const int32_t* col, int kernel, int precision, int flags, int64_t* stats)
 {
+    vpm::TraceRange trace_("vpm_p2p_lists_dev");
     const char* fn = "vpm_p2p_lists_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -1185,6 +1213,7 @@ int vpm_p2p_lists_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam,
 int vpm_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
                      int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes)
 {
+    vpm::TraceRange trace_("vpm_leaflist_dev");
     const char* fn = "vpm_leaflist_dev";
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
@@ -1219,6 +1248,7 @@ int vpm_leaflist_dev(vpm_ctx* c, int64_t n, const double* x, int leaf_size, doub
 int vpm_leaflist_host(int64_t n, const double* x, int leaf_size, double theta, int32_t* perm,
                       int64_t* leaf_begin, int64_t* leaf_end, int64_t* row, int32_t* col, int64_t* sizes)
 {
+    vpm::TraceRange trace_("vpm_leaflist_host");
     if (!x || !sizes || n <= 0 || leaf_size < 1 || leaf_size > LEAF_SIZE_MAX || !(theta >= 0.0))
         return fail(nullptr, VPM_ERR_ARG, "vpm_leaflist_host: bad arguments");
     LeafLists L;
@@ -1241,6 +1271,7 @@ int vpm_uj_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam
                        const double* Ubar, const double* Jbar, double* xbar, double* gbar, double* sbar,
                        int kernel, int precision)
 {
+    vpm::TraceRange trace_("vpm_uj_adjoint_dev");
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_adjoint_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));

@@ -2,9 +2,20 @@
 // Not part of the public ABI (include/vpm_gb300.h).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 namespace vpm {
+
+// One NVTX range per library call, named after the entry point, so that a
+// profiler's timeline shows each UJ / Estr / adjoint call around its kernels.
+// Without a tool attached a push/pop is a null-pointer check.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // A target in Morton order: FP64 position and its index in the caller's arrays.
 struct __align__(16) TgtPos { double x, y, z; int32_t idx, pad; };

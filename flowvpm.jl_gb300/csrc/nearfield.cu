@@ -35,6 +35,7 @@
 
 #include <cub/cub.cuh>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -51,6 +52,7 @@ constexpr int GS_BLOCKS = 8 * 152;
 // counters in NearScratch::ctr (unsigned 64-bit)
 enum : int {
     C_NODES = 0, C_NEAR = 1, C_OVF = 2, C_PAIRS = 3, C_NL = 4,
+    C_OVFN = 5,                                 // the near list overflowed (the traversal itself stays valid)
     C_LVL = 8,                                  // [C_LVL + 2d, C_LVL + 2d + 1) = node ids of depth d
     C_F = C_LVL + 2 * (MAX_DEPTH + 2),          // C_F + s = frontier size of traversal step s
     C_COUNT = C_F + TRAV_STEPS + 2
@@ -346,6 +348,14 @@ __global__ void nt_trav(int step, double theta, const TravNode* __restrict__ cr,
 {
     __shared__ unsigned sw[GS_THREADS / 32];
     __shared__ ull sb;
+    __shared__ int stop;
+    // After an overflow in an earlier step, the slots of this step's frontier past the last
+    // write were counted but never written: read nothing, the host grows the buffers and
+    // repeats the traversal.  One read per block keeps the exit block-uniform (block_append
+    // holds barriers); the flag is read once, before this launch writes anything.
+    if (threadIdx.x == 0) stop = ctr[C_OVF] != 0ull;
+    __syncthreads();
+    if (stop) return;
     const float th2 = (float)(theta * theta);
     const ull raw = ctr[C_F + step];
     const int64_t cnt = (int64_t)(raw < capF ? raw : capF);
@@ -389,7 +399,7 @@ __global__ void nt_trav(int step, double theta, const TravNode* __restrict__ cr,
         const ull sn = block_append(&ctr[C_NEAR], knear, sw, &sb);
         if (knear) {
             if (sn < capN) near[sn] = ((uint64_t)(uint32_t)la_leaf << 32) | (uint32_t)lb_leaf;
-            else ctr[C_OVF] = 1;
+            else ctr[C_OVFN] = 1;
         }
         const ull sf = block_append(&ctr[C_F + step + 1], ksplit, sw, &sb);
         if (ksplit) {
@@ -412,6 +422,7 @@ __global__ void nt_trav_init(int2* __restrict__ fr0, ull* __restrict__ ctr)
     fr0[0] = make_int2(0, 0);
     ctr[C_NEAR] = 0;
     ctr[C_OVF] = 0;
+    ctr[C_OVFN] = 0;
     for (int k = 0; k < TRAV_STEPS + 2; k++) ctr[C_F + k] = 0;
     ctr[C_F] = 1;
 }
@@ -645,10 +656,16 @@ cudaError_t near_build(NearScratch& s, int64_t n, const double* x, int leaf_size
         NT_TRY(cudaGetLastError());
         NT_TRY(read_counters(s, st, sync, sync_ctx));
         const ull* h = (const ull*)s.hctr;
-        if (!h[C_OVF] && h[C_F + TRAV_STEPS] == 0) break;
-        if (attempt >= 8) return cudaErrorMemoryAllocation;
-        s.capF *= 2;
-        s.capN = h[C_NEAR] > s.capN ? (size_t)h[C_NEAR] + (size_t)h[C_NEAR] / 4 : s.capN * 2;
+        if (!h[C_OVF] && !h[C_OVFN] && h[C_F + TRAV_STEPS] == 0) break;
+        // The counters hold the full sizes of every frontier up to the one that overflowed
+        // (appends are counted even when they do not fit) and the near pairs found so far:
+        // grow past them, so that each retry gets at least one step further.
+        if (attempt >= TRAV_STEPS + 2) return cudaErrorMemoryAllocation;
+        ull maxF = 0;
+        for (int k = 0; k <= TRAV_STEPS; k++) maxF = h[C_F + k] > maxF ? h[C_F + k] : maxF;
+        const size_t needF = (size_t)maxF + (size_t)maxF / 4, needN = (size_t)h[C_NEAR] + (size_t)h[C_NEAR] / 4;
+        s.capF = std::max(2 * s.capF, needF);
+        s.capN = std::max(h[C_NEAR] >= s.capN ? 2 * s.capN : s.capN, needN);
     }
     const ull* h = (const ull*)s.hctr;
     L->nodes = (int64_t)h[C_NODES];

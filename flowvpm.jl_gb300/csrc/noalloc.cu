@@ -50,7 +50,10 @@ int nerr(int code, const char* fmt, ...)
 
 inline size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
-bool is_device_ptr(const void* p)
+// Device memory the kernels on device `dev` can use: managed memory, or device
+// memory of `dev` itself (memory of another GPU is rejected, since the kernels
+// run on the current device only).
+bool is_device_ptr(const void* p, int dev)
 {
     if (!p) return false;
     cudaPointerAttributes at;
@@ -58,7 +61,7 @@ bool is_device_ptr(const void* p)
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    return at.type == cudaMemoryTypeManaged || (at.type == cudaMemoryTypeDevice && at.device == dev);
 }
 
 // Address of the scratch array on the current device (looked up once per device).
@@ -87,6 +90,7 @@ extern "C" {
 int vpm_uj_dev_noalloc(int64_t nt, const double* xt, int64_t ns, const double* xs, const double* gs,
                        const double* sgs, double* U, double* J, int kernel, int precision, void* stream)
 {
+    vpm::TraceRange trace_("vpm_uj_dev_noalloc");
     if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
         return nerr(VPM_ERR_ARG, "vpm_uj_dev_noalloc: sizes out of range");
     if (kernel < VPM_KERNEL_SINGULAR || kernel > VPM_KERNEL_WINCKELMANS)
@@ -94,15 +98,16 @@ int vpm_uj_dev_noalloc(int64_t nt, const double* xt, int64_t ns, const double* x
     if (precision != VPM_FP64 && precision != VPM_FP32COMP)
         return nerr(VPM_ERR_ARG, "vpm_uj_dev_noalloc: unknown precision %d", precision);
     if (nt == 0 || ns == 0) return VPM_OK;
-    if (!is_device_ptr(xt) || !is_device_ptr(xs) || !is_device_ptr(gs) || !is_device_ptr(sgs) ||
-        !is_device_ptr(U) || !is_device_ptr(J))
-        return nerr(VPM_ERR_ARG, "vpm_uj_dev_noalloc: every array must be a device pointer");
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
         cudaGetLastError();
         return nerr(VPM_ERR_NODEVICE, "vpm_uj_dev_noalloc: no current CUDA device");
     }
+    if (!is_device_ptr(xt, dev) || !is_device_ptr(xs, dev) || !is_device_ptr(gs, dev) || !is_device_ptr(sgs, dev) ||
+        !is_device_ptr(U, dev) || !is_device_ptr(J, dev))
+        return nerr(VPM_ERR_ARG, "vpm_uj_dev_noalloc: every array must be device memory of the current device %d",
+                    dev);
     const int nsplit = vpm::uj_num_splits(nt, ns, sms);
     const size_t pack = align256(vpm::uj_src_pack_bytes(ns, precision));
     const size_t order = align256(vpm::order_bytes(nt));

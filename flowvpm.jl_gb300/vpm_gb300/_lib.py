@@ -41,6 +41,7 @@ SIGNATURES = {
     "vpm_last_error": (ctypes.c_char_p, [_vp]),
     "vpm_ctx_set_stream": (_int, [_vp, _vp]),
     "vpm_ctx_set_timeout": (_int, [_vp, _dbl]),
+    "vpm_ctx_set_near_capacity": (_int, [_vp, _i64, _i64]),
     "vpm_abi_version": (_int, []),
     "vpm_build_info": (ctypes.c_char_p, []),
     "vpm_launch_count": (_i64, [_vp]),
@@ -171,6 +172,10 @@ class Context:
 
     def set_timeout(self, seconds: float):
         self._check(self._L.vpm_ctx_set_timeout(self._h, float(seconds)))
+
+    def set_near_capacity(self, frontier_pairs: int, near_pairs: int):
+        """Initial traversal capacities of the next near-field list build (grown on overflow)."""
+        self._check(self._L.vpm_ctx_set_near_capacity(self._h, int(frontier_pairs), int(near_pairs)))
 
     # --------------------------------------------------- host-matrix drop-in
     def uj(self, particles: np.ndarray, np_: int, kernel: int, precision: int, flags: int):

@@ -115,6 +115,13 @@ int vpm_ctx_set_stream(vpm_ctx* ctx, void* stream);
  * (default 3600).  A wait that runs out returns VPM_ERR_TIMEOUT and marks the
  * context unusable. */
 int vpm_ctx_set_timeout(vpm_ctx* ctx, double seconds);
+/* Capacities, in pairs, of the near-field list builder's traversal buffers for
+ * the next build of this context: node pairs of one frontier and near leaf
+ * pairs (by default 40 n and 24 n, n >= 4096).  A build that overflows them
+ * doubles them and traverses again, so they only trade device memory for
+ * repeated traversals; the lists do not depend on them.  Library plumbing (the
+ * reference's FastMultipole sizes its own lists). */
+int vpm_ctx_set_near_capacity(vpm_ctx* ctx, int64_t frontier_pairs, int64_t near_pairs);
 /* Library and ABI identification. */
 int vpm_abi_version(void);
 const char* vpm_build_info(void);

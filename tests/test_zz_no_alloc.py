@@ -2,7 +2,8 @@
 device memory (their memory belongs to another allocator, or they must not
 allocate once running).  It keeps its scratch in a static 64 MiB device array
 instead of cudaMalloc'ed buffers; its results must equal those of the
-allocating entry point vpm_uj_dev, call after call.
+allocating entry point vpm_uj_dev bit for bit, call after call, and the
+oracle within the parity tolerance.
 
 Named test_zz_* so pytest collects it last.  It creates its own inputs and
 needs nothing from other test files, so it passes alone in a fresh process and
@@ -39,6 +40,10 @@ def _normwise(a, b):
 @pytest.mark.parametrize("kernel", [2, 3])
 @pytest.mark.parametrize("n", [3000, 40000])
 def test_noalloc_matches_allocating_entry_point_twice(kernel, precision, n):
+    """Both entry points run the same kernels with the same source-split rule
+    (the split depends only on the sizes and the SM count), so the results are
+    bit for bit equal, on the first call and on the second, which reuses the
+    static scratch the first one left behind."""
     import torch
     import vpm_gb300
     L = vpm_gb300.load()
@@ -50,14 +55,34 @@ def test_noalloc_matches_allocating_entry_point_twice(kernel, precision, n):
     Jref = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
     ctx.uj_dev(x, x, g, sg, Uref, Jref, kernel, precision)
     stream = torch.cuda.current_stream().cuda_stream
-    for call in range(2):   # two calls in a row share (and reuse) the static scratch
+    for call in range(2):
         U = torch.zeros_like(Uref)
         J = torch.zeros_like(Jref)
         rc = _noalloc(L, x, x, g, sg, U, J, kernel, precision, stream)
         assert rc == 0, L.vpm_last_error(None).decode()
-        assert _normwise(U, Uref) <= TOL[precision], call
-        assert _normwise(J, Jref) <= TOL[precision], call
+        assert torch.equal(U, Uref), call
+        assert torch.equal(J, Jref), call
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32COMP])
+def test_noalloc_matches_the_oracle(precision):
+    """One comparison against the FP64 CPU oracle (the reference's pair loop,
+    src/FLOWVPM_fmm.jl:102-168), within the tolerance of the other parity tests."""
+    import torch
+    import oracle
+    import vpm_gb300
+    L = vpm_gb300.load()
+    n = 2500
+    X, G, s = _cloud(n, seed=11)
+    d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
+    x, g, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    assert _noalloc(L, x, x, g, sg, U, J, 2, precision, torch.cuda.current_stream().cuda_stream) == 0
+    Ur, Jr = oracle.uj_pairs(X, X, G, s, 2)
+    assert np.abs(U.cpu().numpy() - Ur).max() / np.abs(Ur).max() <= TOL[precision]
+    assert np.abs(J.cpu().numpy() - Jr).max() / np.abs(Jr).max() <= TOL[precision]
 
 
 def test_noalloc_cross_targets_and_accumulation():
