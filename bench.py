@@ -431,15 +431,42 @@ def adjoint_ratio(ctx, vpm, torch, n=32000):
     t_roll = timed(roll_fwd)
     t_grad = timed(roll_grad(True))
     t_grad_rc = timed(roll_grad("recompute"))
+    # the SFS stretching pass Estr and its adjoint (vpm_estr_adjoint_dev) on the same ring, J from its UJ
+    Sb = d(rng.normal(size=(n, 3)))
+    SFS = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    Jb2 = torch.zeros_like(J)
+    estr = {}
+    for prec, tag in ((vpm.FP64, "fp64"), (vpm.FP32COMP, "fp32comp")):
+        U.zero_(); J.zero_()
+        ctx.uj_dev(x, x, g, sg, U, J, KERNEL, prec)
+        f = timed(lambda: ctx.estr_dev(x, J, x, g, sg, J, SFS, KERNEL, prec, True))
+        a_ = timed(lambda: ctx.estr_adjoint_dev(x, g, sg, J, Sb, xb, gb, sb, Jb2, KERNEL, prec, True))
+        estr.update({f"estr_fwd_ms_{tag}": f, f"estr_adjoint_ms_{tag}": a_, f"estr_adjoint_over_fwd_{tag}": a_ / f})
+    # a 5-step rollout with the ConstantSFS term: gradient (forward + backward) over forward
+    kw_sfs = dict(kw, sfs=ad.ConstantSFS(Cs=1.0))
+
+    def roll_fwd_sfs():
+        with torch.no_grad():
+            ad.ring_loss(*ad.rollout(x, g, sg, 0.01, steps, checkpoint=False, **kw_sfs), **kw)
+
+    def roll_grad_sfs():
+        xx, gg, ss = x.clone().requires_grad_(), g.clone().requires_grad_(), sg.clone().requires_grad_()
+        ad.ring_loss(*ad.rollout(xx, gg, ss, 0.01, steps, checkpoint=True, **kw_sfs), **kw).backward()
+    t_roll_sfs = timed(roll_fwd_sfs)
+    t_grad_sfs = timed(roll_grad_sfs)
+    estr.update({"sfs_rollout_fwd_ms": t_roll_sfs, "sfs_rollout_grad_ms": t_grad_sfs,
+                 "sfs_rollout_grad_over_fwd": t_grad_sfs / t_roll_sfs})
     return {"n_particles": n, "uj_fwd_ms": fwd, "uj_adjoint_ms": adj, "uj_adjoint_over_fwd": adj / fwd,
             "uj_fwd_ms_fp32comp": fwd32, "uj_adjoint_ms_fp32comp": adj32,
-            "uj_adjoint_over_fwd_fp32comp": adj32 / fwd32,
+            "uj_adjoint_over_fwd_fp32comp": adj32 / fwd32, **estr,
             "rollout_steps": steps, "rollout_fwd_ms": t_roll, "rollout_grad_ms": t_grad,
             "rollout_grad_over_fwd": t_grad / t_roll, "rollout_backward_over_fwd": (t_grad - t_roll) / t_roll,
             "rollout_grad_recompute_ms": t_grad_rc, "rollout_grad_recompute_over_fwd": t_grad_rc / t_roll,
             "note": "FP64 forward and adjoint, Gaussian-erf.  rollout_grad = forward + backward with per-step "
                     "checkpointing that keeps each step's UJ values; backward = rollout_grad - forward; "
-                    "_recompute re-runs each step's UJ evaluations in the backward pass"}
+                    "_recompute re-runs each step's UJ evaluations in the backward pass; estr_* = the Estr pass "
+                    "(vpm_estr_dev) and its adjoint (vpm_estr_adjoint_dev, gradients w.r.t. x, Gamma, sigma, J); "
+                    "sfs_rollout_* = the FP64 rollout with the ConstantSFS term (Cs = 1)"}
 
 
 def measure_ffma_peak(ctx) -> float:

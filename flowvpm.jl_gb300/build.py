@@ -21,7 +21,7 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvpm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["uj.cu", "estr.cu", "order.cu", "adjoint.cu", "dynamic.cu", "nearfield.cu", "leaflist.cu", "step.cu", "tree.cpp",
+SOURCES = ["uj.cu", "estr.cu", "order.cu", "adjoint.cu", "estr_adjoint.cu", "dynamic.cu", "nearfield.cu", "leaflist.cu", "step.cu", "tree.cpp",
            "abi.cu", "noalloc.cu"]
 
 

@@ -1294,4 +1294,38 @@ int vpm_uj_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam
     return bounded_wait(c);
 }
 
+int vpm_estr_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam, const double* sig,
+                         const double* J, const uint8_t* static_flags, const double* SFSbar, double* xbar,
+                         double* gbar, double* sbar, double* Jbar, int kernel, int precision, int flags)
+{
+    vpm::TraceRange trace_("vpm_estr_adjoint_dev");
+    const char* fn = "vpm_estr_adjoint_dev";
+    if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
+    std::lock_guard<std::mutex> lk(c->mu);
+    RC(enter(c));
+    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
+    RC(check_kernel(c, kernel, precision));
+    if (n == 0) return VPM_OK;
+    DeviceGuard dg(c->device);
+    if (!is_device_ptr(x) || !is_device_ptr(gam) || !is_device_ptr(sig) || !is_device_ptr(J) ||
+        !is_device_ptr(SFSbar) || !is_device_ptr(xbar) || !is_device_ptr(gbar) || !is_device_ptr(sbar) ||
+        !is_device_ptr(Jbar) || (static_flags && !is_device_ptr(static_flags)))
+        return fail(c, VPM_ERR_ARG, "%s: every array must be a device pointer", fn);
+    const EstrAdjSizes z = estr_adjoint_sizes(n, c->num_sms);
+    RC(grow(c, c->order, order_bytes(n), "Morton ordering"));
+    RC(grow(c, c->src_pack, 2 * z.pack, "adjoint packs"));
+    RC(grow(c, c->partial, z.partial, "adjoint partial sums"));
+    EstrAdjWork w;
+    w.order = c->order.p; w.order_bytes = c->order.cap;
+    w.pack1 = c->src_pack.p; w.pack2 = (char*)c->src_pack.p + z.pack;
+    w.partial = (double*)c->partial.p;
+    EstrAdjArgs a;
+    a.n = n; a.x = x; a.gam = gam; a.sig = sig; a.J = J; a.static_flags = static_flags; a.Sbar = SFSbar;
+    a.xbar = xbar; a.gbar = gbar; a.sbar = sbar; a.Jbar = Jbar; a.kernel = kernel; a.precision = precision;
+    a.transposed = (flags & VPM_TRANSPOSED) != 0;
+    CK(launch_estr_adjoint(a, w, c->num_sms, c->stream, &c->launches), "Estr adjoint kernels");
+    return bounded_wait(c);
+}
+
 }  // extern "C"

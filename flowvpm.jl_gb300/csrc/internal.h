@@ -81,6 +81,26 @@ struct AdjArgs {
     int kernel, precision;
 };
 
+// Reverse mode of the self-induced Estr of one particle set (estr_adjoint.cu).
+struct EstrAdjArgs {
+    int64_t n;
+    const double* x; const double* gam; const double* sig; const double* J;   // [n,3], [n,3], [n], [n,9]
+    const uint8_t* static_flags;                                              // [n] or null
+    const double* Sbar;                                                       // [n,3] = dL/dSFS
+    double* xbar; double* gbar; double* sbar; double* Jbar;                   // += outputs
+    int kernel, precision;
+    bool transposed;
+};
+struct EstrAdjWork {
+    void* order; size_t order_bytes;          // Morton ordering of the particles
+    void* pack1; void* pack2;                 // EstrAdjSizes::pack bytes each
+    double* partial;                          // EstrAdjSizes::partial bytes
+};
+struct EstrAdjSizes { size_t pack, partial; };
+EstrAdjSizes estr_adjoint_sizes(int64_t n, int num_sms);
+cudaError_t launch_estr_adjoint(const EstrAdjArgs& a, const EstrAdjWork& w, int num_sms, cudaStream_t st,
+                                int64_t* launches);
+
 // Near-field P2P over octree leaf pairs (leaflist.cu).
 struct LeafArgs {
     int64_t n;

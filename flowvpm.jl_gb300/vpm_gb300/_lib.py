@@ -52,6 +52,8 @@ SIGNATURES = {
     "vpm_estr_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int]),
     "vpm_uj_dev_noalloc": (_int, [_i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp]),
     "vpm_uj_adjoint_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int]),
+    "vpm_estr_adjoint_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int,
+                                    _int]),
     "vpm_zeta": (_int, [_vp, _vp, _i64, _i64, _int, _int]),
     "vpm_dynamic_diff_dev": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _int, _int, _int]),
     "vpm_zeta_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _int, _int]),
@@ -312,6 +314,17 @@ class Context:
         self._check(self._L.vpm_uj_adjoint_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(Ubar),
                                                _ptr(Jbar), _ptr(xbar), _ptr(gbar), _ptr(sbar), int(kernel),
                                                int(precision)))
+
+    def estr_adjoint_dev(self, x, gam, sig, J, Sbar, xbar, gbar, sbar, Jbar, kernel: int, precision: int = FP64,
+                         transposed: bool = True, static=None):
+        """vpm_estr_adjoint_dev: += dL/dx, dL/dGamma, dL/dsigma, dL/dJ of sum(Sbar * SFS)."""
+        for t, c in ((x, 3), (gam, 3), (sig, 1), (J, 9), (Sbar, 3), (xbar, 3), (gbar, 3), (sbar, 1), (Jbar, 9)):
+            _check_dev(t, c)
+        self._torch_stream()
+        self._check(self._L.vpm_estr_adjoint_dev(self._h, x.shape[0], _ptr(x), _ptr(gam), _ptr(sig), _ptr(J),
+                                                 _ptr(static), _ptr(Sbar), _ptr(xbar), _ptr(gbar), _ptr(sbar),
+                                                 _ptr(Jbar), int(kernel), int(precision),
+                                                 TRANSPOSED if transposed else 0))
 
     def p2p_leaflist_dev(self, x, gam, sig, U, J, sfs_out=None, *, leaf_size: int = 64, theta: float = 0.4,
                          kernel: int = KERNEL_GAUSSIANERF, precision: int = FP32COMP, sfs: bool = False,

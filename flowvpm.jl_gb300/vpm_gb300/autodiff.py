@@ -6,11 +6,23 @@ adjoint kernel, in the forward's precision).  It plays the role of the ChainRule
 src/FLOWVPM_rrules.jl:179-330 sketches but never wires in; a Julia binding
 would wrap the same two calls in an rrule.
 
+`EstrFunction` does the same for the SFS stretching pass Estr
+(src/FLOWVPM_subfilterscale_models.jl:16-92) over `vpm_estr_dev` and its
+adjoint `vpm_estr_adjoint_dev`, which also returns dL/dJ (J is an input of
+Estr, so the gradient flows on into UJFunction's backward).  The reference's
+rrule stops there ("SFS pullback not implemented yet!",
+src/FLOWVPM_rrules.jl:153-157).
+
 `rk3_step` is the reference's rVPM low-storage RK3 step
-(src/FLOWVPM_timeintegration.jl:388-532, no SFS, inviscid, no freestream)
-with Pedrizzetti relaxation (src/FLOWVPM_relaxation.jl:62-81), written with
-torch tensor operations on device-resident state so autograd can run through
-it; every particle-to-particle evaluation goes through `UJFunction`.
+(src/FLOWVPM_timeintegration.jl:388-532, inviscid, no freestream) with
+Pedrizzetti relaxation (src/FLOWVPM_relaxation.jl:62-81) and, optionally, the
+constant-coefficient SFS scheme (ConstantSFS, src/FLOWVPM_subfilterscale.jl:88-150:
+C = Cs set at the first stage of each step, with backscatter clipping
+:287-296), written with torch tensor operations on device-resident state so
+autograd can run through it; every particle-to-particle evaluation goes
+through `UJFunction` / `EstrFunction`.  The clipping sets C by a comparison, a
+piecewise-constant function of the state: C carries no gradient, as in any
+autodiff of the reference.
 `rollout` chains steps with per-step checkpointing.  The default keeps, per
 step, its input state and the U, J of its UJ evaluations (O(N) each); the
 backward pass re-runs the step's O(N) tensor algebra with autograd on those
@@ -20,6 +32,8 @@ checkpoint="recompute" keeps only each step's input state and re-runs the
 whole step, UJ evaluations included (torch.utils.checkpoint).
 """
 from __future__ import annotations
+
+import math
 
 import torch
 import torch.utils.checkpoint as ckpt
@@ -72,6 +86,63 @@ def _stretch(J, G, transposed: bool = True):
     return torch.einsum("nji,nj->ni", Jm, G)       # S_i = sum_j du_i/dx_j G_j
 
 
+class EstrFunction(torch.autograd.Function):
+    """SFS[n,3] = Estr of one particle set on itself (x[n,3], gamma[n,3], sigma[n], J[n,9]),
+    float64 CUDA tensors; no static particles."""
+
+    @staticmethod
+    def forward(ctx, x, gam, sig, J, kernel: int, precision: int, transposed: bool, vctx: _lib.Context):
+        x, gam, sig, J = x.contiguous(), gam.contiguous(), sig.contiguous(), J.contiguous()
+        SFS = torch.zeros_like(x)
+        vctx.estr_dev(x, J, x, gam, sig, J, SFS, kernel, precision, transposed)
+        ctx.save_for_backward(x, gam, sig, J)
+        ctx.kernel, ctx.precision, ctx.transposed, ctx.vctx = kernel, precision, transposed, vctx
+        return SFS
+
+    @staticmethod
+    def backward(ctx, Sbar):
+        x, gam, sig, J = ctx.saved_tensors
+        Sbar = torch.zeros_like(x) if Sbar is None else Sbar.contiguous()
+        xb, gb, sb, Jb = torch.zeros_like(x), torch.zeros_like(gam), torch.zeros_like(sig), torch.zeros_like(J)
+        ctx.vctx.estr_adjoint_dev(x, gam, sig, J, Sbar, xb, gb, sb, Jb, ctx.kernel, ctx.precision, ctx.transposed)
+        return xb, gb, sb, Jb, None, None, None, None
+
+
+def estr(x, gam, sig, J, kernel: int, precision: int = _lib.FP64, transposed: bool = True,
+         vctx: _lib.Context | None = None):
+    return EstrFunction.apply(x, gam, sig, J, kernel, precision, transposed, vctx or _lib.default_context())
+
+
+class _KeptEstr(torch.autograd.Function):
+    """Estr whose forward value was kept from an earlier evaluation on the same inputs."""
+
+    @staticmethod
+    def forward(ctx, x, gam, sig, J, SFS, kernel: int, precision: int, transposed: bool, vctx: _lib.Context):
+        ctx.save_for_backward(x, gam, sig, J)
+        ctx.kernel, ctx.precision, ctx.transposed, ctx.vctx = kernel, precision, transposed, vctx
+        return SFS.clone()
+
+    @staticmethod
+    def backward(ctx, Sbar):
+        xb, gb, sb, Jb, *_ = EstrFunction.backward(ctx, Sbar)
+        return xb, gb, sb, Jb, None, None, None, None, None
+
+
+class ConstantSFS:
+    """The constant-coefficient SFS scheme of src/FLOWVPM_subfilterscale.jl:88-150:
+    C = Cs on every particle at the first stage of a step, set to 0 where
+    clipping_backscatter (src/FLOWVPM_subfilterscale.jl:287-296) finds C Gamma . SFS < 0."""
+
+    def __init__(self, Cs: float = 1.0, clip_backscatter: bool = False):
+        self.Cs = float(Cs)
+        self.clip_backscatter = bool(clip_backscatter)
+
+
+# zeta(0) of each kernel (src/FLOWVPM_kernel.jl; constants src/FLOWVPM.jl:62-66): singular,
+# Gaussian, Gaussian-erf, Winckelmans
+ZETA0 = {0: 1.0, 1: 3.0 / (4.0 * math.pi), 2: 1.0 / (2.0 * math.pi) ** 1.5, 3: 7.5 / (4.0 * math.pi)}
+
+
 class _KeptUJ(torch.autograd.Function):
     """UJ whose forward values were kept from an earlier evaluation on the same
     inputs; its backward is the adjoint kernel, as for UJFunction."""
@@ -94,26 +165,49 @@ def _uj_default(x, gam, sig, kernel, precision, vctx):
     return UJFunction.apply(x, gam, sig, kernel, precision, vctx)
 
 
+def _estr_default(x, gam, sig, J, kernel, precision, transposed, vctx):
+    return EstrFunction.apply(x, gam, sig, J, kernel, precision, transposed, vctx)
+
+
 def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64, f: float = 0.0,
              g: float = 0.2, relax: bool = True, rlxf: float = 0.3, transposed: bool = True,
-             vctx: _lib.Context | None = None, uj_fn=None):
-    """One rVPM RK3 step (+ Pedrizzetti relaxation) on device tensors; differentiable.
-    uj_fn(x, gam, sig, kernel, precision, vctx) -> (U, J) replaces UJFunction (checkpointing)."""
+             sfs: ConstantSFS | None = None, vctx: _lib.Context | None = None, uj_fn=None, estr_fn=None):
+    """One rVPM RK3 step (+ Pedrizzetti relaxation, + the ConstantSFS term when `sfs`
+    is given) on device tensors; differentiable.  uj_fn(x, gam, sig, kernel, precision,
+    vctx) -> (U, J) and estr_fn(x, gam, sig, J, kernel, precision, transposed, vctx) -> SFS
+    replace UJFunction / EstrFunction (checkpointing)."""
     vctx = vctx or _lib.default_context()
     uj_fn = uj_fn or _uj_default
+    estr_fn = estr_fn or _estr_default
+    zeta0 = ZETA0[kernel]
     M0 = torch.zeros_like(x)
     M3 = torch.zeros_like(gam)
     M8 = torch.zeros_like(sig)
+    C = None
     for a, b in STAGES:
         U, J = uj_fn(x, gam, sig, kernel, precision, vctx)
+        Cterm = None
+        if sfs is not None:
+            SFS = estr_fn(x, gam, sig, J, kernel, precision, transposed, vctx)
+            if a == 0:   # the coefficient of ConstantSFS's AfterUJ, first stage only
+                with torch.no_grad():
+                    C = torch.full_like(sig, sfs.Cs)
+                    if sfs.clip_backscatter:
+                        C = torch.where(C * (gam * SFS).sum(1) < 0, torch.zeros_like(C), C)
+            Cterm = (C * sig ** 3 / zeta0)[:, None] * SFS            # C SFS sigma^3 / zeta0
         M0 = a * M0 + dt * U
         x = x + b * M0
         MM = _stretch(J, gam, transposed)
         Gn2 = (gam * gam).sum(1)
         pos = Gn2 > 0
-        MM4 = torch.where(pos, (f + g) / (1 + 3 * f) * (MM * gam).sum(1) / torch.where(pos, Gn2, 1.0),
-                          torch.zeros_like(Gn2))
-        M3 = a * M3 + dt * (MM - 3 * MM4[:, None] * gam)
+        num = (f + g) / (1 + 3 * f) * (MM * gam).sum(1)
+        if Cterm is not None and f != 0.0:
+            num = num - f / (1 + 3 * f) * (Cterm * gam).sum(1)
+        MM4 = torch.where(pos, num / torch.where(pos, Gn2, 1.0), torch.zeros_like(Gn2))
+        dG = MM - 3 * MM4[:, None] * gam
+        if Cterm is not None:
+            dG = dG - Cterm
+        M3 = a * M3 + dt * dG
         M8 = a * M8 - dt * (sig * MM4)
         gam = gam + b * M3
         sig = sig + b * M8
@@ -129,32 +223,40 @@ def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64,
 
 
 class _StepKeepUJ(torch.autograd.Function):
-    """One rk3_step with per-step checkpointing that keeps the step's U, J values."""
+    """One rk3_step with per-step checkpointing that keeps the step's U, J (and SFS) values."""
 
     @staticmethod
     def forward(ctx, x, gam, sig, dt, kw):
-        kept = []
+        kept, kept_sfs = [], []
 
         def record(x_, g_, s_, kernel, precision, vctx):
             U, J = UJFunction.apply(x_, g_, s_, kernel, precision, vctx)
             kept.append((U, J))
             return U, J
+
+        def record_sfs(x_, g_, s_, J_, kernel, precision, transposed, vctx):
+            S = EstrFunction.apply(x_, g_, s_, J_, kernel, precision, transposed, vctx)
+            kept_sfs.append(S)
+            return S
         with torch.no_grad():
-            out = rk3_step(x, gam, sig, dt, uj_fn=record, **kw)
+            out = rk3_step(x, gam, sig, dt, uj_fn=record, estr_fn=record_sfs, **kw)
         ctx.save_for_backward(x, gam, sig)
-        ctx.kept, ctx.dt, ctx.kw = kept, dt, kw
+        ctx.kept, ctx.kept_sfs, ctx.dt, ctx.kw = kept, kept_sfs, dt, kw
         return out
 
     @staticmethod
     def backward(ctx, gx, gg, gs):
         x, gam, sig = (t.detach().requires_grad_() for t in ctx.saved_tensors)
-        kept = iter(ctx.kept)
+        kept, kept_sfs = iter(ctx.kept), iter(ctx.kept_sfs)
 
         def replay(x_, g_, s_, kernel, precision, vctx):
             U, J = next(kept)
             return _KeptUJ.apply(x_, g_, s_, U, J, kernel, precision, vctx)
+
+        def replay_sfs(x_, g_, s_, J_, kernel, precision, transposed, vctx):
+            return _KeptEstr.apply(x_, g_, s_, J_, next(kept_sfs), kernel, precision, transposed, vctx)
         with torch.enable_grad():
-            out = rk3_step(x, gam, sig, ctx.dt, uj_fn=replay, **ctx.kw)
+            out = rk3_step(x, gam, sig, ctx.dt, uj_fn=replay, estr_fn=replay_sfs, **ctx.kw)
         grads = [gx, gg, gs]
         outs = [o for o, gr in zip(out, grads) if gr is not None]
         torch.autograd.backward(outs, [gr for gr in grads if gr is not None])

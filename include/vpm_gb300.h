@@ -186,6 +186,20 @@ int vpm_uj_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* g
                        const double* Ubar, const double* Jbar, double* xbar, double* gbar,
                        double* sbar, int kernel, int precision);
 
+/* Reverse mode of the self-induced Estr of one particle set (targets = sources,
+ * the pass of vpm_estr_dev): given SFSbar[n,3] = dL/dSFS, adds dL/dx to
+ * xbar[n,3], dL/dGamma to gbar[n,3], dL/dsigma to sbar[n] and dL/dJ to
+ * Jbar[n,9] (J enters Estr as an input: the caller chains Jbar into the UJ
+ * adjoint).  static_flags (may be NULL) as in vpm_estr_dev: static particles
+ * take no part and receive nothing.  flags: VPM_TRANSPOSED.  The reference's
+ * rrule stops at "SFS pullback not implemented yet!"
+ * (src/FLOWVPM_rrules.jl:153-157); this is that pullback, for
+ * src/FLOWVPM_subfilterscale_models.jl:16-92.  Two passes over all pairs,
+ * without atomics: results are deterministic.  Device pointers. */
+int vpm_estr_adjoint_dev(vpm_ctx* ctx, int64_t n, const double* x, const double* gam, const double* sig,
+                         const double* J, const uint8_t* static_flags, const double* SFSbar, double* xbar,
+                         double* gbar, double* sbar, double* Jbar, int kernel, int precision, int flags);
+
 /* The test-filter differences of the pseudo-three-level dynamic SFS procedure
  * (src/FLOWVPM_subfilterscale.jl:447-673) on device arrays, for one particle
  * set acting on itself (no static particles):

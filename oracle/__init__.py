@@ -89,6 +89,8 @@ def lib():
         L.oracle_uj_adjoint.argtypes = [_i64, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
                                         ctypes.c_int]
         L.oracle_g_d1_d2.argtypes = [ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]
+        L.oracle_estr_adjoint.argtypes = [_i64, _dp, _dp, _dp, _dp, _u8p, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int]
         L.oracle_rk3_step.restype = ctypes.c_int
         L.oracle_rk3_step.argtypes = [_dp, _i64, _i64, ctypes.c_double, ctypes.c_int,
                                       ctypes.POINTER(StepParams)]
@@ -179,6 +181,19 @@ def uj_adjoint(x, gam, sig, Ubar, Jbar, kernel: int, nthreads: int = 0):
     lib().oracle_uj_adjoint(n, _p(x), _p(gam), _p(sig), _p(Ubar), _p(Jbar), _p(xb), _p(gb), _p(sb),
                             int(kernel), int(nthreads))
     return xb, gb, sb
+
+
+def estr_adjoint(x, gam, sig, J, Sbar, kernel: int, transposed: bool = True, static=None, nthreads: int = 0):
+    """(xbar[n,3], gbar[n,3], sbar[n], Jbar[n,9]) = gradients of sum(Sbar * SFS) for the
+    self-induced Estr of one particle set (static particles: 0/1 flags, or None)."""
+    x, gam, sig, J, Sbar = map(_c, (x, gam, sig, J, Sbar))
+    n = x.shape[0]
+    st = None if static is None else _c(static, np.uint8)
+    xb = np.zeros((n, 3)); gb = np.zeros((n, 3)); sb = np.zeros(n); Jb = np.zeros((n, 9))
+    lib().oracle_estr_adjoint(n, _p(x), _p(gam), _p(sig), _p(J), None if st is None else st.ctypes.data_as(_u8p),
+                              _p(Sbar), _p(xb), _p(gb), _p(sb), _p(Jb), int(kernel), int(bool(transposed)),
+                              int(nthreads))
+    return xb, gb, sb, Jb
 
 
 def g_d1_d2(kernel: int, rho: float):

@@ -362,6 +362,107 @@ void oracle_estr_pairs(int64_t t0, int64_t t1, const double* xt, const double* J
     }
 }
 
+/* ---------------------------------------------------------- Estr adjoint
+ * Reverse mode of the self-induced Estr of one particle set
+ * (src/FLOWVPM_subfilterscale_models.jl:16-92): for
+ *     phi = sum_t Sbar_t . SFS_t,  SFS_t = sum_{s != t} zeta(r/sigma_s)/sigma_s^3 S_ts,
+ *     S_ts = (J_t - J_s)^T Gamma_s (transposed) or (J_t - J_s) Gamma_s (classic),
+ * over non-static targets and non-static sources (the reference's iterator),
+ * the gradients with respect to x, Gamma, sigma and J are added to xb, gb, sb,
+ * Jb.  Each pair is differentiated directly from the definition: with
+ * z = zeta/sigma^3, dz/dr = zeta'/sigma^4, dz/dsigma = -(rho zeta' + 3 zeta)/sigma^4,
+ * w = Sbar_t . S_ts and M = J_t - J_s (M[a][b] = J[a + 3b]):
+ *     d/dx_t = w dz/dr dx/r = -d/dx_s  (0 at r = 0: zeta'(0) = 0),
+ *     d/dsigma_s = w dz/dsigma,
+ *     d/dGamma_s = z M Sbar_t (transposed) or z M^T Sbar_t (classic),
+ *     d/dJ_t[a + 3b] = z Gamma_s[a] Sbar_t[b] (transposed) or z Sbar_t[a] Gamma_s[b]
+ *                      (classic) = -d/dJ_s[a + 3b].
+ * The self pair (zero in the forward, and with zero gradient) is skipped.  The
+ * target-side and the source-side sums run as two loops, each parallel over
+ * its own output particle. */
+static double zeta_d1(int kernel, double rho)
+{
+    switch (kernel) {
+    case VPM_KERNEL_GAUSSIAN: return -3.0 * rho * rho * oracle_zeta(kernel, rho);
+    case VPM_KERNEL_GAUSSIANERF: return -rho * oracle_zeta(kernel, rho);
+    case VPM_KERNEL_WINCKELMANS: return -7.0 * rho * oracle_zeta(kernel, rho) / (rho * rho + 1.0);
+    default: return 0.0;   /* singular: zeta is an indicator of r == 0 */
+    }
+}
+
+/* per-pair terms of the Estr adjoint (see above); t != s, both non-static */
+static void estr_adj_pair(const double* x, const double* gam, const double* sig, const double* J,
+                          const double* Sbar, int64_t t, int64_t s, int kernel, int transposed,
+                          double dxt[3], double* dsig, double dgam[3], double dJt[9])
+{
+    const double dx[3] = {x[3 * t] - x[3 * s], x[3 * t + 1] - x[3 * s + 1], x[3 * t + 2] - x[3 * s + 2]};
+    const double r = sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    const double sg = sig[s], rho = r / sg;
+    const double zt = oracle_zeta(kernel, rho), z1 = zeta_d1(kernel, rho);
+    const double z = zt / (sg * sg * sg);
+    const double z_r = z1 / (sg * sg * sg * sg);
+    const double z_s = -(rho * z1 + 3.0 * zt) / (sg * sg * sg * sg);
+    const double* G = gam + 3 * s;
+    const double* Sb = Sbar + 3 * t;
+    double M[3][3];
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) M[a][b] = J[9 * t + a + 3 * b] - J[9 * s + a + 3 * b];
+    double S[3];
+    for (int k = 0; k < 3; k++) {
+        S[k] = 0.0;
+        for (int i = 0; i < 3; i++) S[k] += (transposed ? M[i][k] : M[k][i]) * G[i];
+    }
+    const double w = Sb[0] * S[0] + Sb[1] * S[1] + Sb[2] * S[2];
+    for (int k = 0; k < 3; k++) dxt[k] = r > 0.0 ? w * z_r * dx[k] / r : 0.0;
+    *dsig = w * z_s;
+    for (int i = 0; i < 3; i++) {
+        dgam[i] = 0.0;
+        for (int k = 0; k < 3; k++) dgam[i] += z * (transposed ? M[i][k] : M[k][i]) * Sb[k];
+    }
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) dJt[a + 3 * b] = transposed ? z * G[a] * Sb[b] : z * Sb[a] * G[b];
+}
+
+void oracle_estr_adjoint(int64_t n, const double* x, const double* gam, const double* sig, const double* J,
+                         const uint8_t* st, const double* Sbar, double* xb, double* gb, double* sb, double* Jb,
+                         int kernel, int transposed, int nthreads)
+{
+    int nth = set_threads(nthreads);
+    (void)nth;
+    /* target side: x_t and J_t */
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth)
+    for (int64_t t = 0; t < n; t++) {
+        if (st && st[t]) continue;
+        double ax[3] = {0, 0, 0}, aJ[9] = {0};
+        for (int64_t s = 0; s < n; s++) {
+            if (s == t || (st && st[s])) continue;
+            double dxt[3], dsig, dgam[3], dJt[9];
+            estr_adj_pair(x, gam, sig, J, Sbar, t, s, kernel, transposed, dxt, &dsig, dgam, dJt);
+            for (int k = 0; k < 3; k++) ax[k] += dxt[k];
+            for (int k = 0; k < 9; k++) aJ[k] += dJt[k];
+        }
+        for (int k = 0; k < 3; k++) xb[3 * t + k] += ax[k];
+        for (int k = 0; k < 9; k++) Jb[9 * t + k] += aJ[k];
+    }
+    /* source side: x_s, Gamma_s, sigma_s and J_s */
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth)
+    for (int64_t s = 0; s < n; s++) {
+        if (st && st[s]) continue;
+        double ax[3] = {0, 0, 0}, ag[3] = {0, 0, 0}, as = 0.0, aJ[9] = {0};
+        for (int64_t t = 0; t < n; t++) {
+            if (t == s || (st && st[t])) continue;
+            double dxt[3], dsig, dgam[3], dJt[9];
+            estr_adj_pair(x, gam, sig, J, Sbar, t, s, kernel, transposed, dxt, &dsig, dgam, dJt);
+            for (int k = 0; k < 3; k++) { ax[k] -= dxt[k]; ag[k] += dgam[k]; }
+            as += dsig;
+            for (int k = 0; k < 9; k++) aJ[k] -= dJt[k];
+        }
+        for (int k = 0; k < 3; k++) { xb[3 * s + k] += ax[k]; gb[3 * s + k] += ag[k]; }
+        sb[s] += as;
+        for (int k = 0; k < 9; k++) Jb[9 * s + k] += aJ[k];
+    }
+}
+
 /* zeta_direct(sources, targets, zeta), src/FLOWVPM_viscous.jl:467-488: the
  * basis-function (vorticity) field W_t += sum_s zeta(r/sigma_s)/sigma_s^3 Gamma_s
  * over every source, the self pair (r = 0) included; statics take part. */

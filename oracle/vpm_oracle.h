@@ -73,6 +73,12 @@ void oracle_zeta_pairs(int64_t t0, int64_t t1, const double* xt, int64_t ns, con
 void oracle_uj_adjoint(int64_t n, const double* x, const double* gam, const double* sig,
                        const double* Ubar, const double* Jbar, double* xbar, double* gbar,
                        double* sbar, int kernel, int nthreads);
+/* Reverse mode of the self-induced Estr (src/FLOWVPM_subfilterscale_models.jl:16-92):
+ * given Sbar[n,3] = dL/dSFS, adds dL/dx, dL/dGamma, dL/dsigma and dL/dJ to
+ * xb[n,3], gb[n,3], sb[n], Jb[n,9]; st[n] static flags (may be NULL). */
+void oracle_estr_adjoint(int64_t n, const double* x, const double* gam, const double* sig, const double* J,
+                         const uint8_t* st, const double* Sbar, double* xb, double* gb, double* sb, double* Jb,
+                         int kernel, int transposed, int nthreads);
 /* (g, g', g'') of a kernel at rho (libm erf). */
 void oracle_g_d1_d2(int kernel, double rho, double* g, double* d1, double* d2);
 
