@@ -293,9 +293,11 @@ def run_gpu(args, rank, world):
                "U_rms_rel": float(np.linalg.norm(Uh - Ur) / np.linalg.norm(Ur)),
                "J_rms_rel": float(np.linalg.norm(Jh - Jr) / np.linalg.norm(Jr)),
                "targets_checked": 256}
-        fp64 = fp64_rate(ctx, vpm, torch)
+        fp64 = fp64_rate(ctx, vpm, torch, X, G, s, measure_dfma_peak(ffma))
         wnk = winckelmans_rate(ctx, vpm, torch, X, G, s)
         adjoint = adjoint_ratio(ctx, vpm, torch)
+        estr_b, lf_b = rings_blocks(ctx, vpm, torch, peak_tflops)
+        jet_b = jet_block(ctx, vpm, torch, peak_tflops)
         base = cpu_baseline(X, G, s)
         mp = measured_peaks()
         out = {
@@ -327,8 +329,11 @@ def run_gpu(args, rank, world):
             "gpu_launches": launches,
             "fp64_gpu": fp64,
             "winckelmans": wnk,
-            "mixed_over_fp64": value / fp64["value"] if fp64 else None,
+            "mixed_over_fp64": fp64["mixed_over_fp64_same_config"],
             "adjoint": adjoint,
+            "estr": estr_b,
+            "leapfrog_step": lf_b,
+            "jet": jet_b,
             "error_vs_oracle": err,
             "wall_s_timed_region": wall,
         }
@@ -339,24 +344,124 @@ def run_gpu(args, rank, world):
         print(json.dumps(out), flush=True)
 
 
-def fp64_rate(ctx, vpm, torch):
-    """Plain FP64 GPU form on a 2^17 cloud (one timed evaluation)."""
-    n = 1 << 17
-    X, G, s = random_cloud(n, seed=77)
-    d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
-    xt, gs, sg = d(X), d(G), d(s)
+def fp64_rate(ctx, vpm, torch, X, G, s, fp64_peak):
+    """The plain FP64 form and the FP32-comp form on the same configuration:
+    2^15 seeded targets of the 2^20 cloud against all of its sources (one timed
+    evaluation each, after a warm-up), and the FP64 form's fraction of the
+    DFMA-loop peak."""
+    n = X.shape[0]
+    nt = 1 << 15
+    sub = np.sort(np.random.default_rng(15).choice(n, nt, replace=False))
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    xt, xs, gs, sg = d(X[sub]), d(X), d(G), d(s)
+    U = torch.zeros(nt, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(nt, 9, device="cuda", dtype=torch.float64)
+    out = {"targets": nt, "sources": n, "pairs": float(nt) * n}
+    for prec, tag in ((vpm.FP64, "fp64"), (vpm.FP32COMP, "fp32comp")):
+        ctx.uj_dev(xt[:1024], xs, gs, sg, U[:1024], J[:1024], KERNEL, prec)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        ctx.uj_dev(xt, xs, gs, sg, U, J, KERNEL, prec)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        out[f"ms_{tag}"] = ms
+        out[f"pairs_per_s_{tag}"] = float(nt) * n / (ms / 1e3)
+    out["value"] = out["pairs_per_s_fp64"]
+    out["unit"] = "pairs/s"
+    out["mixed_over_fp64_same_config"] = out["pairs_per_s_fp32comp"] / out["pairs_per_s_fp64"]
+    ach = FLOP_PER_PAIR * out["pairs_per_s_fp64"] / 1e12
+    out["roofline_fp64"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                            "frac": ach / fp64_peak if fp64_peak else None, "kernel": "uj_f64_kernel<gaussianerf>",
+                            "peak_source": "DFMA-loop kernel measured in this run (vpm_probe_dfma)"}
+    return out
+
+
+def _timed_min(torch, fn, reps=3):
+    """Minimum CUDA-event time (ms) of `reps` calls after one warm-up call."""
+    fn()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
+def rings_blocks(ctx, vpm, torch, peak_tflops):
+    """The leapfrogging-rings workload (two coaxial rings, R = 1 and 0.7, 10
+    particles a section, 200,000 particles, Gaussian-erf, FP32-comp):
+    * `estr`: one Estr pass (vpm_estr_dev, J from the field's own UJ) at 25 flop
+      per pair over all N^2 pair slots;
+    * `leapfrog_step`: whole device-resident rVPM RK3 steps with the dynamic SFS
+      procedure, core spreading and relaxation, against the work of the
+      reference's own step: per step it evaluates 5 UJ and 4 Estr passes over
+      all pairs (3 stages of UJ + Estr, the test filter's UJ + Estr, the
+      relaxation's UJ), 5 x 74 + 4 x 25 = 470 flop per pair slot."""
+    from vpm_gb300 import device_step as ds, workloads
+    X, G, s = workloads.leapfrog_rings(200_000)
+    n = X.shape[0]
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    x, g, sg = d(X), d(G), d(s)
     U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
     J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
-    ctx.uj_dev(xt[:4096], xt[:4096], gs[:4096], sg[:4096], U[:4096], J[:4096], KERNEL, vpm.FP64)
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    ctx.uj_dev(xt, xt, gs, sg, U, J, KERNEL, vpm.FP64)
-    b.record()
-    torch.cuda.synchronize()
-    ms = a.elapsed_time(b)
-    return {"value": float(n) * n / (ms / 1e3), "unit": "pairs/s", "n_particles": n, "ms": ms,
-            "kernel": "uj_f64_kernel<gaussianerf>"}
+    S = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    ctx.uj_dev(x, x, g, sg, U, J, KERNEL, vpm.FP32COMP)
+    ms_estr = _timed_min(torch, lambda: ctx.estr_dev(x, J, x, g, sg, J, S, KERNEL, vpm.FP32COMP, True))
+    ms_uj = _timed_min(torch, lambda: ctx.uj_dev(x, x, g, sg, U, J, KERNEL, vpm.FP32COMP))
+    pairs = float(n) * n
+    estr_tf = 25 * pairs / (ms_estr / 1e3) / 1e12
+    uj_tf = FLOP_PER_PAIR * pairs / (ms_uj / 1e3) / 1e12
+    estr = {"workload": "leapfrog rings, 200,000 particles, FP32-comp", "n_particles": n, "ms": ms_estr,
+            "pairs_per_s": pairs / (ms_estr / 1e3), "flop_per_pair": 25, "achieved_tflops": estr_tf,
+            "frac_of_ffma_peak": estr_tf / peak_tflops, "kernel": "estr_mixed_kernel<gaussianerf>",
+            "uj_ms_same_field": ms_uj, "uj_frac_of_ffma_peak": uj_tf / peak_tflops,
+            "note": "all N^2 pair slots counted; tiles and 8-source sub-blocks whose every pair is past "
+                    "zeta/zeta(0) < 1e-13 are skipped (their terms are below FP32 resolution)"}
+    fld = ds.DeviceField(x.clone(), g.clone(), sg.clone(), kernel=KERNEL, precision=vpm.FP32COMP)
+    sfs = ds.DynamicSFSParams()
+    visc = ds.CoreSpreadingParams(nu=1e-4, sgm0=0.05)
+    step = lambda: ds.rk3_step(fld, 0.005, ctx, sfs=sfs, viscous=visc, relax_rlxf=0.3)
+    ms_step = _timed_min(torch, step, reps=3)
+    flop_step = (5 * 74 + 4 * 25) * pairs
+    ach = flop_step / (ms_step / 1e3) / 1e12
+    lf = {"workload": "leapfrog rings, 200,000 particles, FP32-comp, dynamic SFS, core spreading, relaxation",
+          "ms_per_step": ms_step, "particle_steps_per_s": n / (ms_step / 1e3),
+          "reference_flop_per_pair_slot": 470, "achieved_tflops": ach, "frac_of_ffma_peak": ach / peak_tflops,
+          "note": "UJ + stretching + SFS: the reference's step evaluates 5 UJ and 4 Estr passes over all pairs "
+                  "(74 and 25 flop a pair); this step evaluates 4 UJ, 3 Estr, and the test filter's differences "
+                  "directly (one J-difference pass and 2 Estr), and its time includes every kernel of the step"}
+    return estr, lf
+
+
+def jet_block(ctx, vpm, torch, peak_tflops):
+    """The jet-like cloud with the FMM near field (2^20 particles in a cylinder,
+    sigma = 0.02, leaf size 64, theta = 0.4): one near-field UJ call (octree,
+    lists and P2P on the GPU), and the P2P alone (lists reused)."""
+    from vpm_gb300 import workloads
+    X, G, s = workloads.jet_cloud(1 << 20)
+    n = X.shape[0]
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    x, g, sg = d(X), d(G), d(s)
+    U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
+    kw = dict(leaf_size=64, theta=0.4, kernel=KERNEL, precision=vpm.FP32COMP)
+    st = ctx.p2p_leaflist_dev(x, g, sg, U, J, **kw)
+    ms_call = _timed_min(torch, lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, **kw))
+    ms_p2p = _timed_min(torch, lambda: ctx.p2p_leaflist_dev(x, g, sg, U, J, reuse=True, **kw))
+    pairs = float(st[2])
+    ach = FLOP_PER_PAIR * pairs / (ms_p2p / 1e3) / 1e12
+    return {"workload": "jet-like cloud, 2^20 particles, near field (leaf 64, theta 0.4), FP32-comp UJ",
+            "leaves": st[0], "leaf_pairs": st[1], "pairs": pairs, "ms_per_call": ms_call,
+            "pairs_per_s_call": pairs / (ms_call / 1e3), "ms_p2p": ms_p2p, "pairs_per_s_p2p": pairs / (ms_p2p / 1e3),
+            "achieved_tflops_p2p": ach, "frac_of_ffma_peak_p2p": ach / peak_tflops,
+            "note": "ms_per_call builds the octree and lists and runs the P2P; ms_p2p reuses the lists "
+                    "(VPM_REUSE_LISTS): packs + P2P"}
 
 
 def winckelmans_rate(ctx, vpm, torch, X, G, s):
@@ -469,6 +574,15 @@ def adjoint_ratio(ctx, vpm, torch, n=32000):
                     "sfs_rollout_* = the FP64 rollout with the ConstantSFS term (Cs = 1)"}
 
 
+def measure_dfma_peak(ctx) -> float:
+    """TFLOP/s of a pure DFMA loop (vpm_probe_dfma in the library)."""
+    out = np.zeros(1)
+    rc = ctx._L.vpm_probe_dfma(ctx._h, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(ctx._L.vpm_last_error(ctx._h).decode())
+    return float(out[0])
+
+
 def measure_ffma_peak(ctx) -> float:
     """TFLOP/s of a pure FFMA loop (vpm_probe_ffma in the library)."""
     import vpm_gb300._lib as L
@@ -494,6 +608,10 @@ def run_kernel_only(args):
         import vpm_gb300.rings as rings
         X, G, s, _ = rings.ring_sections(1.0, 1.0, 0.1, 1000, 32, 0.05)
         n = X.shape[0]
+    elif args.cloud == "rings":   # the leapfrogging rings of n particles
+        from vpm_gb300 import workloads
+        X, G, s = workloads.leapfrog_rings(n)
+        n = X.shape[0]
     else:
         X, G, s = random_cloud(n, seed=1)
     d = lambda a: torch.tensor(a, device="cuda", dtype=torch.float64).contiguous()
@@ -501,6 +619,8 @@ def run_kernel_only(args):
     U = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
     J = torch.zeros(n, 9, device="cuda", dtype=torch.float64)
     SFS = torch.zeros(n, 3, device="cuda", dtype=torch.float64)
+    if args.estr:      # Estr reads the field's own J
+        ctx.uj_dev(xt, xt, gs, sg, U, J, kern, prec)
     if args.adjoint:   # cotangents of U and J: seeded, O(1)
         rng = np.random.default_rng(7)
         U.copy_(torch.from_numpy(rng.normal(size=(n, 3))))
@@ -734,12 +854,14 @@ def run_rollout(args):
     d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
     x0, g0, s0 = d(X), d(G), d(s)
     steps, dt = args.ro_steps, 0.01
+    sfs = ad.ConstantSFS(Cs=args.ro_sfs) if args.ro_sfs > 0 else None
     kw = dict(kernel=KERNEL, precision=vpm.FP64, vctx=ctx)
+    kw_step = dict(kw, sfs=sfs)
 
     def loss_at(x, g, sg, prec=vpm.FP64):
         k2 = dict(kernel=KERNEL, precision=prec, vctx=ctx)
         with torch.no_grad():
-            return float(ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=False, **k2), **k2))
+            return float(ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=False, sfs=sfs, **k2), **k2))
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -752,9 +874,18 @@ def run_rollout(args):
 
     def grad():
         x, g, sg = x0.clone().requires_grad_(), g0.clone().requires_grad_(), s0.clone().requires_grad_()
-        ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=True, **kw), **kw).backward()
+        ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=True, **kw_step), **kw).backward()
         return x.grad, g.grad, sg.grad
     ms_grad, (gx, gg, gs) = timed(grad)
+    # the same gradient with the FP32-comp forward and adjoints, against the FP64 one
+
+    def grad32():
+        k32 = dict(kernel=KERNEL, precision=vpm.FP32COMP, vctx=ctx)
+        x, g, sg = x0.clone().requires_grad_(), g0.clone().requires_grad_(), s0.clone().requires_grad_()
+        ad.ring_loss(*ad.rollout(x, g, sg, dt, steps, checkpoint=True, sfs=sfs, **k32), **k32).backward()
+        return x.grad, g.grad, sg.grad
+    ms_grad32, g32 = timed(grad32)
+    g32_rel = max(float((a - b).abs().max() / b.abs().max()) for a, b in zip(g32, (gx, gg, gs)))
     rng = np.random.default_rng(3)
     h = 1e-6
     worst = 0.0
@@ -770,6 +901,8 @@ def run_rollout(args):
         worst = max(worst, rel)
         checks.append({"fd": fd, "adjoint": an, "rel": rel})
     print(json.dumps({"mode": "rollout", "n_particles": X.shape[0], "steps": steps, "dt": dt,
+                      "sfs": None if sfs is None else f"ConstantSFS(Cs={sfs.Cs})",
+                      "gradient_ms_fp32comp": ms_grad32, "fp32comp_gradient_vs_fp64_max_rel": g32_rel,
                       "loss_fp64": L0, "loss_fp32comp": L32, "forward_ms_fp64": ms_fwd,
                       "forward_ms_fp32comp": ms_fwd32, "gradient_ms_fp64": ms_grad,
                       "gradient_over_forward": ms_grad / ms_fwd,
@@ -830,6 +963,8 @@ def main():
     ap.add_argument("--precision", default="fp32comp", choices=["fp64", "fp32comp"])
     ap.add_argument("--kernel", default="gaussianerf", choices=["singular", "gaussian", "gaussianerf", "winckelmans"])
     ap.add_argument("--estr", action="store_true")
+    ap.add_argument("--cloud", default="random", choices=["random", "rings"],
+                    help="--kernel-only: the random cloud or the leapfrogging rings of --n particles")
     ap.add_argument("--jet-call", default="uj", choices=["uj", "dynamic"])
     ap.add_argument("--adjoint", action="store_true")
     # the other workloads (one JSON line each, not the bench line)
@@ -842,6 +977,7 @@ def main():
     ap.add_argument("--jet-steps", type=int, default=3)
     ap.add_argument("--ro-steps", type=int, default=50)
     ap.add_argument("--ro-dirs", type=int, default=4)
+    ap.add_argument("--ro-sfs", type=float, default=0.0, help="Cs of a ConstantSFS term in the rollout (0: none)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))

@@ -46,6 +46,7 @@ SIGNATURES = {
     "vpm_build_info": (ctypes.c_char_p, []),
     "vpm_launch_count": (_i64, [_vp]),
     "vpm_probe_ffma": (_int, [_vp, _vp]),
+    "vpm_probe_dfma": (_int, [_vp, _vp]),
     "vpm_uj": (_int, [_vp, _vp, _i64, _i64, _int, _int, _int]),
     "vpm_uj_cross": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _i64, _int, _int]),
     "vpm_uj_dev": (_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _int, _int]),

@@ -138,6 +138,63 @@ class ConstantSFS:
         self.clip_backscatter = bool(clip_backscatter)
 
 
+class DynamicSFS:
+    """The dynamic-procedure SFS scheme of src/FLOWVPM_subfilterscale.jl:157-268 with the
+    pseudo-three-level procedure of :447-673, at each step's first stage: U, J and Estr
+    at the test filter alpha sigma and at sigma, the Lagrangian-averaged ratio
+    C = <nu>/<delta> with the bounds [minC, maxC] (:592-656), force_positive, and
+    backscatter clipping.  The per-particle state (C, numerator, denominator) is
+    carried from step to step.  The bounds, force_positive and the clipping select
+    branches by comparisons: the gradient follows the selected branch."""
+
+    def __init__(self, alpha: float = 0.667, rlxf: float = 0.005, minC: float = 0.0, maxC: float = 1.0,
+                 force_positive: bool = False, clip_backscatter: bool = False):
+        if minC < 0 or maxC < 0 or minC > maxC:
+            raise ValueError(f"invalid C bounds ({minC}, {maxC})")
+        self.alpha, self.rlxf, self.minC, self.maxC = float(alpha), float(rlxf), float(minC), float(maxC)
+        self.force_positive = bool(force_positive)
+        self.clip_backscatter = bool(clip_backscatter)
+
+
+EPS = 2.220446049250313e-16   # Julia eps(), the reference's guard of a zero denominator
+
+
+def _dynamic_coefficient(sfs: DynamicSFS, gam, sig, J, SFS, MS, MF, Cprev, zeta0, transposed):
+    """dynamicprocedure_pseudo3level_afterUJ (src/FLOWVPM_subfilterscale.jl:541-673) on
+    device tensors: (C, numerator, denominator) per particle from the test-filter values
+    MS = S(J_alpha), MF = SFS_alpha and the values J, SFS at sigma."""
+    dS = MS - _stretch(J, gam, transposed)
+    dF = MF - SFS
+    nume = (dS * gam).sum(1) * (3 * sfs.alpha - 2)
+    deno = (dF * gam).sum(1) / (zeta0 / sig ** 3)
+    C3 = Cprev[:, 2]
+    C3 = torch.where(C3 == 0, deno, C3)
+    C3 = torch.where(C3 == 0, torch.full_like(C3, EPS), C3)
+    nume = sfs.rlxf * nume + (1 - sfs.rlxf) * Cprev[:, 1]
+    deno = sfs.rlxf * deno + (1 - sfs.rlxf) * C3
+    with torch.no_grad():
+        ratio = (nume / deno).abs()
+        big = ratio > sfs.maxC
+        swap_deno = big & (deno.abs() < C3.abs())
+    deno = torch.where(swap_deno, torch.sign(deno) * C3.abs(), deno)
+    with torch.no_grad():
+        ratio2 = (nume / deno).abs()
+        cap = big & (ratio2 >= sfs.maxC)
+        floor = (~big) & (ratio < sfs.minC)
+    nume = torch.where(cap, torch.sign(nume) * deno.abs() * sfs.maxC, nume)
+    nume = torch.where(floor, torch.sign(nume) * deno.abs() * sfs.minC, nume)
+    C1 = nume / deno
+    if torch.isnan(C1).any():
+        raise FloatingPointError("NaN in the dynamic procedure's coefficient")
+    if sfs.force_positive:
+        C1 = C1.abs()
+    if sfs.clip_backscatter:
+        with torch.no_grad():
+            clip = C1 * (gam * SFS).sum(1) < 0
+        C1 = torch.where(clip, torch.zeros_like(C1), C1)
+    return torch.stack([C1, nume, deno], dim=1)
+
+
 # zeta(0) of each kernel (src/FLOWVPM_kernel.jl; constants src/FLOWVPM.jl:62-66): singular,
 # Gaussian, Gaussian-erf, Winckelmans
 ZETA0 = {0: 1.0, 1: 3.0 / (4.0 * math.pi), 2: 1.0 / (2.0 * math.pi) ** 1.5, 3: 7.5 / (4.0 * math.pi)}
@@ -171,30 +228,45 @@ def _estr_default(x, gam, sig, J, kernel, precision, transposed, vctx):
 
 def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64, f: float = 0.0,
              g: float = 0.2, relax: bool = True, rlxf: float = 0.3, transposed: bool = True,
-             sfs: ConstantSFS | None = None, vctx: _lib.Context | None = None, uj_fn=None, estr_fn=None):
-    """One rVPM RK3 step (+ Pedrizzetti relaxation, + the ConstantSFS term when `sfs`
-    is given) on device tensors; differentiable.  uj_fn(x, gam, sig, kernel, precision,
+             sfs: ConstantSFS | DynamicSFS | None = None, C=None, vctx: _lib.Context | None = None,
+             uj_fn=None, estr_fn=None):
+    """One rVPM RK3 step (+ Pedrizzetti relaxation, + the SFS term of `sfs`) on device
+    tensors; differentiable.  With a DynamicSFS, C[n,3] is the per-particle state
+    (coefficient, numerator, denominator; zeros at the start) and the step returns
+    (x, gam, sig, C); otherwise (x, gam, sig).  uj_fn(x, gam, sig, kernel, precision,
     vctx) -> (U, J) and estr_fn(x, gam, sig, J, kernel, precision, transposed, vctx) -> SFS
     replace UJFunction / EstrFunction (checkpointing)."""
     vctx = vctx or _lib.default_context()
     uj_fn = uj_fn or _uj_default
     estr_fn = estr_fn or _estr_default
     zeta0 = ZETA0[kernel]
+    dynamic = isinstance(sfs, DynamicSFS)
+    if dynamic and C is None:
+        C = torch.zeros(x.shape[0], 3, dtype=x.dtype, device=x.device)
     M0 = torch.zeros_like(x)
     M3 = torch.zeros_like(gam)
     M8 = torch.zeros_like(sig)
-    C = None
+    Cs = None
     for a, b in STAGES:
+        if dynamic and a == 0:   # BeforeUJ: the test filter alpha sigma
+            sig_a = sig * sfs.alpha
+            _, Ja = uj_fn(x, gam, sig_a, kernel, precision, vctx)
+            MF = estr_fn(x, gam, sig_a, Ja, kernel, precision, transposed, vctx)
+            MS = _stretch(Ja, gam, transposed)
         U, J = uj_fn(x, gam, sig, kernel, precision, vctx)
         Cterm = None
         if sfs is not None:
             SFS = estr_fn(x, gam, sig, J, kernel, precision, transposed, vctx)
-            if a == 0:   # the coefficient of ConstantSFS's AfterUJ, first stage only
-                with torch.no_grad():
-                    C = torch.full_like(sig, sfs.Cs)
-                    if sfs.clip_backscatter:
-                        C = torch.where(C * (gam * SFS).sum(1) < 0, torch.zeros_like(C), C)
-            Cterm = (C * sig ** 3 / zeta0)[:, None] * SFS            # C SFS sigma^3 / zeta0
+            if a == 0:   # AfterUJ, first stage only
+                if dynamic:
+                    C = _dynamic_coefficient(sfs, gam, sig, J, SFS, MS, MF, C, zeta0, transposed)
+                    Cs = C[:, 0]
+                else:
+                    with torch.no_grad():
+                        Cs = torch.full_like(sig, sfs.Cs)
+                        if sfs.clip_backscatter:
+                            Cs = torch.where(Cs * (gam * SFS).sum(1) < 0, torch.zeros_like(Cs), Cs)
+            Cterm = (Cs * sig ** 3 / zeta0)[:, None] * SFS            # C SFS sigma^3 / zeta0
         M0 = a * M0 + dt * U
         x = x + b * M0
         MM = _stretch(J, gam, transposed)
@@ -219,14 +291,15 @@ def rk3_step(x, gam, sig, dt: float, *, kernel: int, precision: int = _lib.FP64,
         ok = nw != 0
         newg = (1 - rlxf) * gam + rlxf * (nG / torch.where(ok, nw, 1.0))[:, None] * w
         gam = torch.where(ok[:, None], newg, gam)
-    return x, gam, sig
+    return (x, gam, sig, C) if dynamic else (x, gam, sig)
 
 
 class _StepKeepUJ(torch.autograd.Function):
-    """One rk3_step with per-step checkpointing that keeps the step's U, J (and SFS) values."""
+    """One rk3_step with per-step checkpointing that keeps the step's U, J (and SFS) values.
+    The state is (x, gam, sig) or, with a DynamicSFS, (x, gam, sig, C)."""
 
     @staticmethod
-    def forward(ctx, x, gam, sig, dt, kw):
+    def forward(ctx, dt, kw, *state):
         kept, kept_sfs = [], []
 
         def record(x_, g_, s_, kernel, precision, vctx):
@@ -239,14 +312,15 @@ class _StepKeepUJ(torch.autograd.Function):
             kept_sfs.append(S)
             return S
         with torch.no_grad():
-            out = rk3_step(x, gam, sig, dt, uj_fn=record, estr_fn=record_sfs, **kw)
-        ctx.save_for_backward(x, gam, sig)
+            out = rk3_step(*state[:3], dt, C=state[3] if len(state) > 3 else None, uj_fn=record,
+                           estr_fn=record_sfs, **kw)
+        ctx.save_for_backward(*state)
         ctx.kept, ctx.kept_sfs, ctx.dt, ctx.kw = kept, kept_sfs, dt, kw
         return out
 
     @staticmethod
-    def backward(ctx, gx, gg, gs):
-        x, gam, sig = (t.detach().requires_grad_() for t in ctx.saved_tensors)
+    def backward(ctx, *grads):
+        state = [t.detach().requires_grad_() for t in ctx.saved_tensors]
         kept, kept_sfs = iter(ctx.kept), iter(ctx.kept_sfs)
 
         def replay(x_, g_, s_, kernel, precision, vctx):
@@ -256,27 +330,33 @@ class _StepKeepUJ(torch.autograd.Function):
         def replay_sfs(x_, g_, s_, J_, kernel, precision, transposed, vctx):
             return _KeptEstr.apply(x_, g_, s_, J_, next(kept_sfs), kernel, precision, transposed, vctx)
         with torch.enable_grad():
-            out = rk3_step(x, gam, sig, ctx.dt, uj_fn=replay, estr_fn=replay_sfs, **ctx.kw)
-        grads = [gx, gg, gs]
+            out = rk3_step(*state[:3], ctx.dt, C=state[3] if len(state) > 3 else None, uj_fn=replay,
+                           estr_fn=replay_sfs, **ctx.kw)
         outs = [o for o, gr in zip(out, grads) if gr is not None]
         torch.autograd.backward(outs, [gr for gr in grads if gr is not None])
-        return x.grad, gam.grad, sig.grad, None, None
+        return (None, None) + tuple(t.grad for t in state)
 
 
-def rollout(x, gam, sig, dt: float, nsteps: int, *, checkpoint=True, **kw):
+def rollout(x, gam, sig, dt: float, nsteps: int, *, checkpoint=True, C=None, **kw):
     """nsteps of rk3_step.  checkpoint=True: per-step checkpointing that keeps
     each step's UJ values (no pair sum is evaluated twice); "recompute": per-step
     checkpointing that re-runs each step in the backward pass; False: autograd
-    keeps every intermediate."""
+    keeps every intermediate.  With a DynamicSFS (kw["sfs"]) the state includes the
+    coefficients C[n,3] (zeros when not given) and (x, gam, sig, C) is returned."""
+    dynamic = isinstance(kw.get("sfs"), DynamicSFS)
+    state = (x, gam, sig)
+    if dynamic:
+        state += (C if C is not None else torch.zeros(x.shape[0], 3, dtype=x.dtype, device=x.device),)
     for _ in range(nsteps):
         if checkpoint == "recompute":
-            x, gam, sig = ckpt.checkpoint(lambda a, b, c: rk3_step(a, b, c, dt, **kw), x, gam, sig,
-                                          use_reentrant=False)
+            def step(*st):
+                return rk3_step(*st[:3], dt, C=st[3] if len(st) > 3 else None, **kw)
+            state = ckpt.checkpoint(step, *state, use_reentrant=False)
         elif checkpoint:
-            x, gam, sig = _StepKeepUJ.apply(x, gam, sig, dt, kw)
+            state = _StepKeepUJ.apply(dt, kw, *state)
         else:
-            x, gam, sig = rk3_step(x, gam, sig, dt, **kw)
-    return x, gam, sig
+            state = rk3_step(*state[:3], dt, C=state[3] if dynamic else None, **kw)
+    return tuple(state)
 
 
 def ring_loss(x, gam, sig, *, kernel: int, precision: int = _lib.FP64, vctx: _lib.Context | None = None):

@@ -131,6 +131,9 @@ int64_t vpm_launch_count(const vpm_ctx* ctx);
  * of this device in TFLOP/s, from a pure FFMA-chain kernel timed with CUDA
  * events.  Used as the FP32-pipe roofline denominator. */
 int vpm_probe_ffma(vpm_ctx* ctx, double* tflops);
+/* The same for the FP64 pipe (pure DFMA chains): the roofline denominator of
+ * the plain FP64 form. */
+int vpm_probe_dfma(vpm_ctx* ctx, double* tflops);
 
 /* -------------------------------------------------- reference-facing drop-in */
 

@@ -169,3 +169,83 @@ def test_sfs_rollout_fp32comp_gradient_follows_fp64(ctx):
     g32, _ = _grad_and_fd(ctx, 3, 0, 0, sfs, FP32COMP)
     for a, b in zip(g32, g64):
         assert normwise(a.cpu().numpy(), b.cpu().numpy())[0] <= 1e-4
+
+
+def _two_rings():
+    import vpm_gb300.rings as rings
+    X1, G1, s1, _ = rings.ring_sections(1.0, 1.0, 0.1, 40, 10, 0.05)
+    X2, G2, s2, _ = rings.ring_sections(1.0, 0.7, 0.07, 28, 10, 0.035, O=(0, 0, 0.3))
+    return np.vstack([X1, X2]), np.vstack([G1, G2]), np.concatenate([s1, s2])
+
+
+@pytest.mark.parametrize("alpha,force_positive,clip", [(0.999, True, True), (0.667, False, False)])
+def test_dynamic_sfs_step_matches_oracle_step(ctx, alpha, force_positive, clip):
+    """rk3_step with the dynamic procedure (FP64: both filter widths evaluated and
+    subtracted, as the reference does) against the oracle's RK3 step with the same
+    scheme, 3 steps on a two-ring field; the coefficient state C is carried."""
+    from vpm_gb300 import autodiff as ad
+    X, G, s = _two_rings()
+    n = X.shape[0]
+    sfs = ad.DynamicSFS(alpha=alpha, rlxf=0.005, force_positive=force_positive, clip_backscatter=clip)
+    st = (_dev(X), _dev(G), _dev(s), None)
+    for _ in range(3):
+        st = ad.rk3_step(*st[:3], 0.005, kernel=2, precision=FP64, sfs=sfs, C=st[3], relax=True, vctx=ctx)
+    P = np.zeros((46, n), order="F")
+    P[0:3] = X.T; P[3:6] = G.T; P[6] = s
+    prm = oracle.StepParams(kernel=oracle.KERNEL_GAUSSIANERF, transposed=1, f=0.0, g=0.2, relaxation=1, rlxf=0.3,
+                            sfs=2, alpha=alpha, sfs_rlxf=0.005, minC=0.0, maxC=1.0,
+                            force_positive=int(force_positive), clip_backscatter=int(clip))
+    for _ in range(3):
+        assert oracle.rk3_step(P, n, 0.005, prm, relax=True) == 0
+    for name, a, b in (("x", st[0], P[0:3].T), ("Gamma", st[1], P[3:6].T), ("sigma", st[2], P[6]),
+                       ("C", st[3][:, 0], P[36])):
+        assert normwise(a.cpu().numpy(), b)[0] <= 1e-10, name
+
+
+def test_dynamic_sfs_rollout_gradient_on_32_directions(ctx):
+    """5 RK3 steps of the two-ring field with the dynamic procedure (alpha = 0.667, the
+    coefficient bounded to [0, 1], no clipping) and relaxation: the gradient of the loss
+    with respect to the initial X, Gamma, sigma (C starting at zero) against central
+    differences (h = 1e-6) of the FP64 forward on 32 seeded directions."""
+    import torch
+    from vpm_gb300 import autodiff as ad
+    X, G, s = _two_rings()
+    x0, g0, s0 = _dev(X), _dev(G), _dev(s)
+    kw = dict(kernel=2, precision=FP64, vctx=ctx, sfs=ad.DynamicSFS(alpha=0.667, rlxf=0.005))
+    x, g, sg = x0.clone().requires_grad_(), g0.clone().requires_grad_(), s0.clone().requires_grad_()
+    out = ad.rollout(x, g, sg, 0.005, 5, checkpoint=True, **kw)
+    ad.ring_loss(*out[:3], kernel=2, precision=FP64, vctx=ctx).backward()
+    assert float(out[3][:, 0].detach().abs().max()) > 0          # the dynamic coefficient is active
+
+    def loss(dx, dg, ds):
+        with torch.no_grad():
+            o = ad.rollout(x0 + dx, g0 + dg, s0 + ds, 0.005, 5, checkpoint=False, **kw)
+            return float(ad.ring_loss(*o[:3], kernel=2, precision=FP64, vctx=ctx))
+    rng = np.random.default_rng(3200)
+    h = 1e-6
+    rels = []
+    for _ in range(32):
+        d = rng.normal(size=x0.numel() + g0.numel() + s0.numel())
+        d /= np.linalg.norm(d)
+        dx = _dev(d[:x0.numel()].reshape(x0.shape))
+        dg = _dev(d[x0.numel():x0.numel() + g0.numel()].reshape(g0.shape))
+        ds = _dev(d[x0.numel() + g0.numel():])
+        fd = (loss(h * dx, h * dg, h * ds) - loss(-h * dx, -h * dg, -h * ds)) / (2 * h)
+        an = float((x.grad * dx).sum() + (g.grad * dg).sum() + (sg.grad * ds).sum())
+        rels.append(abs(fd - an) / max(abs(an), 1e-300))
+    assert max(rels) <= 1e-5, max(rels)
+
+
+def test_dynamic_sfs_recompute_checkpointing_gives_the_same_gradient(ctx):
+    from vpm_gb300 import autodiff as ad
+    X, G, s = _two_rings()
+    kw = dict(kernel=2, precision=FP64, vctx=ctx, sfs=ad.DynamicSFS(alpha=0.667, rlxf=0.005))
+    grads = []
+    for mode in (True, "recompute", False):
+        x, g, sg = (_dev(a).requires_grad_() for a in (X, G, s))
+        out = ad.rollout(x, g, sg, 0.005, 3, checkpoint=mode, **kw)
+        ad.ring_loss(*out[:3], kernel=2, precision=FP64, vctx=ctx).backward()
+        grads.append([t.grad.cpu().numpy() for t in (x, g, sg)])
+    for other in grads[1:]:
+        for a, b in zip(other, grads[0]):
+            assert normwise(a, b)[0] <= 1e-12
