@@ -36,7 +36,7 @@ static_assert(UJ_BLOCK % ESTR_SUB == 0, "whole sub-blocks");
 size_t estr_src_pack_bytes(int64_t ns, int precision)
 {
     const int64_t n = round_up(ns, UJ_TILE);
-    return (size_t)n * (precision ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64));
+    return (size_t)n * (precision ? sizeof(SrcEstrDF) : sizeof(SrcEstrF64));
 }
 
 // v = J^T Gamma (transposed) or J Gamma (classic); J column-major 3x3.
@@ -59,19 +59,20 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
                                 const double* __restrict__ gs, const double* __restrict__ sgs,
                                 const double* __restrict__ Js, int64_t ldJs,
                                 const uint8_t* __restrict__ static_s, bool transposed,
-                                const TgtPos* __restrict__ order, SrcEstrMixed* __restrict__ out)
+                                const TgtPos* __restrict__ order, SrcEstrDF* __restrict__ out)
 {
     // with `order` (sources = targets) the pack follows the targets' Morton order
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= ns_pad) return;
-    SrcEstrMixed p;
-    p.pad = 0.f;
+    SrcEstrDF p;
     if (o < ns) {
         const int64_t i = order ? (int64_t)order[o].idx : o;
         const double isig = 1.0 / sgs[i];
         const double isig2 = isig * isig;
-        p.x = xs[3 * i]; p.y = xs[3 * i + 1]; p.z = xs[3 * i + 2];
-        p.isig2 = (float)isig2;
+        const double x = xs[3 * i], y = xs[3 * i + 1], z = xs[3 * i + 2];
+        const float xh = (float)x, yh = (float)y, zh = (float)z;
+        p.a = make_float4(xh, yh, zh, (float)isig2);
+        p.b = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
         const bool off = static_s && static_s[i];
         const double k = off ? 0.0 : zeta_norm(K) * isig2 * isig;
         const double gx = gs[3 * i], gy = gs[3 * i + 1], gz = gs[3 * i + 2];
@@ -79,9 +80,9 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
         if (Js) stretch_vec(Js + i * ldJs, gx, gy, gz, transposed, vx, vy, vz);
         p.g = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), 0.f);
         p.v = make_float4((float)(k * vx), (float)(k * vy), (float)(k * vz), 0.f);
-    } else {
-        p.x = p.y = p.z = 0.0;
-        p.isig2 = 1.f;
+    } else {   // padding: far away, no strength
+        p.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+        p.b = make_float4(0.f, 0.f, 0.f, 0.f);
         p.g = p.v = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     out[o] = p;
@@ -198,6 +199,32 @@ estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __rest
     write_estr(t, idx, o, SFS, ldS, partial, nt_pad);
 }
 
+// 16-byte asynchronous global->shared copy (LDGSTS), L2-cached.
+__device__ __forceinline__ void ecp_async16(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void ecp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void ecp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int EWT = 32;                  // sources per warp tile
+constexpr int ESTR_FLUSH_TILES = 8;      // warp tiles between FP64 adds (256 sources)
+
+// The mixed Estr.  Each warp streams the sources on its own, 32 per tile,
+// double-buffered with cp.async (no block-wide barrier); the loading lane
+// converts its source to an FP32 offset from the warp's first target with
+// FP32 double-float arithmetic (df_offset: rounded once), and each target's
+// own offset is formed by the same operations, so that the self pair and
+// coincident particles have
+// r^2 == 0 exactly (they are skipped: their terms would only cancel to FP32
+// rounding, at the largest weight).  For the Gaussian kernels a whole tile is
+// skipped when every one of its sources is past zeta_skip_s from the warp's
+// target box (zeta/zeta(0) < 1e-13 for every pair: their terms are below the
+// FP32 resolution of the sums), and then an 8-source sub-block when every pair
+// of the warp is.  Sums: 8-source FP32 partials added with compensation
+// (comp_add), FP64 every ESTR_FLUSH_TILES tiles.
 // With DZ (the weight difference of the dynamic procedure's test filter,
 // dynamic.cu) each weight zeta~(r, sigma_s) is replaced by
 // zeta~(r, alpha sigma_s) - zeta~(r, sigma_s) = zeta~(r, sigma_s) (ratio - 1),
@@ -205,12 +232,12 @@ estr_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __rest
 template <int K, bool ZETA, bool DZ = false>
 __global__ void __launch_bounds__(UJ_THREADS)
 estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
-                  const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrMixed* __restrict__ src,
+                  const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrDF* __restrict__ src,
                   int64_t per_split, bool self, bool transposed, double* SFS, int64_t ldS, double* partial,
                   int64_t nt_pad, float3 fd = make_float3(0.f, 0.f, 0.f))
 {
-    __shared__ SrcEstrMixed tile[UJ_TILE];
-    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    __shared__ SrcEstrDF stage[UJ_WARPS][2][EWT];
+    __shared__ float4 offs[UJ_WARPS][2][EWT];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     double tx = 0.0, ty = 0.0, tz = 0.0;
@@ -220,57 +247,95 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
         tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
     }
     const bool valid = t < nt && (ZETA || !(static_t && static_t[idx]));
-    const double ox = __shfl_sync(0xffffffffu, tx, 0);
-    const double oy = __shfl_sync(0xffffffffu, ty, 0);
-    const double oz = __shfl_sync(0xffffffffu, tz, 0);
-    const float3 to = t < nt ? make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz))
-                             : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
+    // warp origin: lane 0's target as a double-float
+    const double ox = __shfl_sync(0xffffffffu, tx, 0), oy = __shfl_sync(0xffffffffu, ty, 0),
+                 oz = __shfl_sync(0xffffffffu, tz, 0);
+    const float3 oh = make_float3((float)ox, (float)oy, (float)oz);
+    const float3 ol = make_float3((float)(ox - (double)oh.x), (float)(oy - (double)oh.y), (float)(oz - (double)oh.z));
+    // the target's offset by the same FP32 double-float operations as the sources' (below);
+    // padding lanes sit at the origin
+    float3 to = make_float3(0.f, 0.f, 0.f);
+    if (t < nt) {
+        const float3 th = make_float3((float)tx, (float)ty, (float)tz);
+        const float3 tl = make_float3((float)(tx - (double)th.x), (float)(ty - (double)th.y),
+                                      (float)(tz - (double)th.z));
+        to = make_float3(df_offset(th.x, tl.x, oh.x, ol.x), df_offset(th.y, tl.y, oh.y, ol.y),
+                         df_offset(th.z, tl.z, oh.z, ol.z));
+    }
+    // the warp's target box (offsets), for the tile skip
+    float bmin[3] = {to.x, to.y, to.z}, bmax[3] = {to.x, to.y, to.z};
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            bmin[k] = fminf(bmin[k], __shfl_xor_sync(0xffffffffu, bmin[k], m));
+            bmax[k] = fmaxf(bmax[k], __shfl_xor_sync(0xffffffffu, bmax[k], m));
+        }
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
+    float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
-    for (int64_t base = s0; base < s1; base += UJ_TILE) {
-        __syncthreads();
-        tile[threadIdx.x] = src[base + threadIdx.x];
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < UJ_TILE / 32; q++) {
-            const int j = lane + 32 * q;
-            off[warp][j] = make_float4((float)(tile[j].x - ox), (float)(tile[j].y - oy),
-                                       (float)(tile[j].z - oz), tile[j].isig2);
+    const int ntiles = (int)((s1 - s0) / EWT);
+    const SrcEstrDF* wsrc = src + s0 + lane;
+    if (ntiles > 0) {
+        SrcEstrDF* d = &stage[warp][0][lane];
+        ecp_async16(&d->a, &wsrc->a); ecp_async16(&d->b, &wsrc->b);
+        ecp_async16(&d->g, &wsrc->g); ecp_async16(&d->v, &wsrc->v);
+        ecp_commit();
+    }
+    int in_flush = 0;
+    for (int it = 0; it < ntiles; it++) {
+        const int buf = it & 1;
+        if (it + 1 < ntiles) {
+            const SrcEstrDF* gp = wsrc + (int64_t)(it + 1) * EWT;
+            SrcEstrDF* d = &stage[warp][buf ^ 1][lane];
+            ecp_async16(&d->a, &gp->a); ecp_async16(&d->b, &gp->b);
+            ecp_async16(&d->g, &gp->g); ecp_async16(&d->v, &gp->v);
+            ecp_commit();
+            ecp_wait<1>();
+        } else {
+            ecp_wait<0>();
         }
         __syncwarp();
+        bool beyond;
+        {   // this lane's source: FP32 offset, and whether it is out of reach of the whole target box
+            const float4 a = stage[warp][buf][lane].a, b = stage[warp][buf][lane].b;
+            const float px = df_offset(a.x, b.x, oh.x, ol.x), py = df_offset(a.y, b.y, oh.y, ol.y),
+                        pz = df_offset(a.z, b.z, oh.z, ol.z);
+            offs[warp][buf][lane] = make_float4(px, py, pz, a.w);
+            const float ex = fmaxf(fmaxf(bmin[0] - px, px - bmax[0]), 0.0f);
+            const float ey = fmaxf(fmaxf(bmin[1] - py, py - bmax[1]), 0.0f);
+            const float ez = fmaxf(fmaxf(bmin[2] - pz, pz - bmax[2]), 0.0f);
+            beyond = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) * a.w > zeta_skip_s<K>();
+        }
+        __syncwarp();
+        if (!(zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, beyond))) {
 #pragma unroll 1
-        for (int sb = 0; sb < UJ_TILE; sb += UJ_BLOCK) {
-            // compensated FP32 sums over the block (see comp_add), FP64 across blocks
-            float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
-            for (int sub = 0; sub < UJ_BLOCK; sub += ESTR_SUB) {
-                // s of the sub-block's sources; the sub-block is skipped when every pair of the warp
-                // is past zeta_skip_s (zeta/zeta(0) < 1e-13 there)
+            for (int sub = 0; sub < EWT; sub += ESTR_SUB) {
                 float sv8[ESTR_SUB], r28[ESTR_SUB];
                 bool far = true;
 #pragma unroll
                 for (int jj = 0; jj < ESTR_SUB; jj++) {
-                    const float4 a = off[warp][sb + sub + jj];
-                    const float dx = to.x - a.x, dy = to.y - a.y, dz = to.z - a.z;
+                    const float4 h = offs[warp][buf][sub + jj];
+                    const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
                     r28[jj] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    sv8[jj] = r28[jj] * a.w;
+                    sv8[jj] = r28[jj] * h.w;
                     far = far && sv8[jj] > zeta_skip_s<K>();
                 }
                 if (zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, far)) continue;
                 float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
 #pragma unroll
                 for (int jj = 0; jj < ESTR_SUB; jj++) {
-                    const int j = sb + sub + jj;
+                    const int j = sub + jj;
                     float z = zhat_f32<K>(sv8[jj]);
                     if constexpr (DZ) z *= zeta_ratio_m1<K>(sv8[jj], fd);
                     if constexpr (!ZETA) z = (r28[jj] == 0.0f) ? 0.0f : z;
-                    const float4 g = tile[j].g;
+                    const float4 g = stage[warp][buf][j].g;
                     fg[0] = fmaf(z, g.x, fg[0]);
                     fg[1] = fmaf(z, g.y, fg[1]);
                     fg[2] = fmaf(z, g.z, fg[2]);
                     if constexpr (!ZETA) {
-                        const float4 v = tile[j].v;
+                        const float4 v = stage[warp][buf][j].v;
                         fv[0] = fmaf(z, v.x, fv[0]);
                         fv[1] = fmaf(z, v.y, fv[1]);
                         fv[2] = fmaf(z, v.z, fv[2]);
@@ -282,13 +347,25 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
                     if constexpr (!ZETA) comp_add(sv[k], cv[k], fv[k]);
                 }
             }
+        }
+        if (++in_flush == ESTR_FLUSH_TILES) {
+            in_flush = 0;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 zg[k] += (double)sg[k] + (double)cg[k];
-                if constexpr (!ZETA) zv[k] += (double)sv[k] + (double)cv[k];
+                sg[k] = cg[k] = 0.f;
+                if constexpr (!ZETA) {
+                    zv[k] += (double)sv[k] + (double)cv[k];
+                    sv[k] = cv[k] = 0.f;
+                }
             }
         }
-        __syncwarp();
+        __syncwarp();   // every lane is done with `buf` before it is refilled
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        zg[k] += (double)sg[k] + (double)cg[k];
+        if constexpr (!ZETA) zv[k] += (double)sv[k] + (double)cv[k];
     }
     if (!valid) return;
     double o[3];
@@ -329,7 +406,7 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
                                                                    per_split, a.self, a.transposed, a.SFS, a.ldS,
                                                                    partial, nt_pad);
     } else {
-        SrcEstrMixed* src = (SrcEstrMixed*)w.src_pack;
+        SrcEstrDF* src = (SrcEstrDF*)w.src_pack;
         pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.zeta ? nullptr : a.Js, a.ldJs,
                                                   static_s, a.transposed, a.self ? tgt : nullptr, src);
         if (a.zeta)

@@ -29,9 +29,10 @@
 // and an epilogue kernel per pass adds the splits in order and forms the
 // outputs.  FP64 follows the formulas above pair by pair, coincident pairs
 // (r = 0, s != t) included as in the forward; FP32-comp takes the forward mixed
-// Estr's arithmetic (FP32 offsets from a per-warp FP64 origin, compensated
-// 8-pair sub-sums, FP64 across blocks) and skips pairs at r = 0, as that
-// forward does.
+// Estr's arithmetic (per-warp streaming, FP32 offsets from a per-warp
+// double-float origin, tile and sub-block skips past the kernel's reach,
+// compensated 8-pair sub-sums, FP64 across tiles) and skips pairs at r = 0, as
+// that forward does.
 #include "internal.h"
 #include "vpm_math.cuh"
 
@@ -48,10 +49,10 @@ constexpr int NACC2 = 10;           // pass 2 sums: A[3], B[3], X[3], Sg
 // Pass-1 payload (a source): FP64 position, 1/sigma (FP64) or 1/sigma^2
 // (mixed), Gamma and v; in the mixed pack Gamma and v carry ZNORM/sigma^3.
 struct __align__(16) EA1F64 { double x, y, z, isig, gx, gy, gz, vx, vy, vz; };
-struct __align__(16) EA1Mx { double x, y, z; float isig2, pad; float4 g, v; };
+struct __align__(16) EA1Mx { float4 a, b, g, v; };        // a = (x_hi, isig2), b = (x_lo, 0)
 // Pass-2 payload (a target): FP64 position, a_t and Sbar_t.
 struct __align__(16) EA2F64 { double x, y, z, pad, ax, ay, az, sx, sy, sz; };
-struct __align__(16) EA2Mx { double x, y, z; float pad0, pad1; float4 a, sb; };
+struct __align__(16) EA2Mx { float4 h, l, a, sb; };       // h = (x_hi, 0), l = (x_lo, 0)
 
 // M v (ab = false) or M^T v (ab = true) for J column-major 3x3 (M[a][b] = J[a + 3b]).
 __device__ __forceinline__ void mat_vec(const double* J, double x0, double x1, double x2, bool transpose, double (&o)[3])
@@ -117,12 +118,16 @@ __global__ void ea_pack(int64_t n, int64_t n_pad, const TgtPos* __restrict__ ord
         ((EA2F64*)p2)[o] = s2;
     } else {
         const double k = zeta_norm(K) * isig * isig * isig;
+        const float xh = (float)px, yh = (float)py, zh = (float)pz;
+        const float4 lo = make_float4((float)(px - (double)xh), (float)(py - (double)yh), (float)(pz - (double)zh), 0.f);
         EA1Mx s1;
-        s1.x = px; s1.y = py; s1.z = pz; s1.isig2 = (float)(isig * isig); s1.pad = 0.f;
+        s1.a = make_float4(xh, yh, zh, (float)(isig * isig));
+        s1.b = lo;
         s1.g = make_float4((float)(k * G[0]), (float)(k * G[1]), (float)(k * G[2]), 0.f);
         s1.v = make_float4((float)(k * v[0]), (float)(k * v[1]), (float)(k * v[2]), 0.f);
         EA2Mx s2;
-        s2.x = px; s2.y = py; s2.z = pz; s2.pad0 = s2.pad1 = 0.f;
+        s2.h = make_float4(xh, yh, zh, 0.f);
+        s2.l = lo;
         s2.a = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
         s2.sb = make_float4((float)sb[0], (float)sb[1], (float)sb[2], 0.f);
         ((EA1Mx*)p1)[o] = s1;
@@ -208,89 +213,170 @@ ea2_f64(int64_t n, const EA1F64* __restrict__ self, int64_t n_pad, const EA2F64*
 }
 
 // -------------------------------------------------------------- FP32-comp passes
-// Both passes: per-warp FP32 offsets from the warp's first particle, the
-// forward mixed Estr's sub-block skip where every pair of the warp is past
-// zeta_skip_s, compensated FP32 sums over 8-pair sub-blocks, FP64 across blocks.
+// Both passes stream the other role's records per warp, 32 per tile,
+// double-buffered with cp.async (no block-wide barrier), as the forward mixed
+// Estr does; offsets from the warp's first particle are formed by df_offset
+// for both roles (the self pair has r^2 == 0 exactly and is skipped).  A tile
+// is skipped when every pair of it is past zeta_skip_s from the warp's box
+// (pass 1 with each source's own sigma; pass 2 with the warp's smallest lane
+// sigma), then an 8-pair sub-block when every pair of the warp is.  Sums:
+// 8-pair FP32 partials added with compensation, FP64 every 8 tiles.
+__device__ __forceinline__ void ea_cp16(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void ea_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void ea_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int EA_WT = 32;
+constexpr int EA_FLUSH = 8;
+
+// Stage one 64-byte record per lane (four 16-byte copies).
+template <class R>
+__device__ __forceinline__ void ea_stage(R* d, const R* g)
+{
+    const float4* gs = reinterpret_cast<const float4*>(g);
+    float4* ds = reinterpret_cast<float4*>(d);
+    ea_cp16(ds, gs); ea_cp16(ds + 1, gs + 1); ea_cp16(ds + 2, gs + 2); ea_cp16(ds + 3, gs + 3);
+    ea_commit();
+}
+
+// The warp's origin (lane 0's particle, double-float), this lane's offset and the
+// bounding box of the warp's offsets.
+struct EaFrame {
+    float3 oh, ol, me;
+    float bmin[3], bmax[3];
+    __device__ __forceinline__ void init(const float4& h, const float4& l, bool valid)
+    {
+        oh = make_float3(__shfl_sync(0xffffffffu, h.x, 0), __shfl_sync(0xffffffffu, h.y, 0),
+                         __shfl_sync(0xffffffffu, h.z, 0));
+        ol = make_float3(__shfl_sync(0xffffffffu, l.x, 0), __shfl_sync(0xffffffffu, l.y, 0),
+                         __shfl_sync(0xffffffffu, l.z, 0));
+        me = valid ? make_float3(df_offset(h.x, l.x, oh.x, ol.x), df_offset(h.y, l.y, oh.y, ol.y),
+                                 df_offset(h.z, l.z, oh.z, ol.z))
+                   : make_float3(0.f, 0.f, 0.f);
+        bmin[0] = bmax[0] = me.x; bmin[1] = bmax[1] = me.y; bmin[2] = bmax[2] = me.z;
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                bmin[k] = fminf(bmin[k], __shfl_xor_sync(0xffffffffu, bmin[k], m));
+                bmax[k] = fmaxf(bmax[k], __shfl_xor_sync(0xffffffffu, bmax[k], m));
+            }
+    }
+    __device__ __forceinline__ float3 offset(const float4& h, const float4& l) const
+    {
+        return make_float3(df_offset(h.x, l.x, oh.x, ol.x), df_offset(h.y, l.y, oh.y, ol.y),
+                           df_offset(h.z, l.z, oh.z, ol.z));
+    }
+    __device__ __forceinline__ float box_dist2(const float3& p) const
+    {
+        const float ex = fmaxf(fmaxf(bmin[0] - p.x, p.x - bmax[0]), 0.0f);
+        const float ey = fmaxf(fmaxf(bmin[1] - p.y, p.y - bmax[1]), 0.0f);
+        const float ez = fmaxf(fmaxf(bmin[2] - p.z, p.z - bmax[2]), 0.0f);
+        return fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    }
+};
+
+// Pass 1: lanes are targets t (Morton position), the tiles hold sources.
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
 ea1_mx(int64_t n, const TgtPos* __restrict__ tgt, const EA2Mx* __restrict__ self, int64_t n_pad,
        const EA1Mx* __restrict__ src, int64_t per_split, double* __restrict__ partial)
 {
-    __shared__ EA1Mx tile[UJ_TILE];
-    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    __shared__ EA1Mx stage[UJ_WARPS][2][EA_WT];
+    __shared__ float4 offs[UJ_WARPS][2][EA_WT];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const EA2Mx me = self[t < n ? t : n_pad - 1];
-    const double ox = __shfl_sync(0xffffffffu, me.x, 0), oy = __shfl_sync(0xffffffffu, me.y, 0),
-                 oz = __shfl_sync(0xffffffffu, me.z, 0);
-    const float3 to = t < n ? make_float3((float)(me.x - ox), (float)(me.y - oy), (float)(me.z - oz))
-                            : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
+    EaFrame fr;
+    fr.init(me.h, me.l, t < n);
     double acc[NACC1] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    float sm[NACC1], cm[NACC1];
+#pragma unroll
+    for (int k = 0; k < NACC1; k++) { sm[k] = 0.f; cm[k] = 0.f; }
     const int64_t s0 = (int64_t)blockIdx.y * per_split, s1 = min(s0 + per_split, n_pad);
-    for (int64_t base = s0; base < s1; base += UJ_TILE) {
-        __syncthreads();
-        tile[threadIdx.x] = src[base + threadIdx.x];
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < UJ_TILE / 32; q++) {
-            const int j = lane + 32 * q;
-            off[warp][j] = make_float4((float)(tile[j].x - ox), (float)(tile[j].y - oy), (float)(tile[j].z - oz),
-                                       tile[j].isig2);
+    const int ntiles = (int)((s1 - s0) / EA_WT);
+    const EA1Mx* wsrc = src + s0 + lane;
+    if (ntiles > 0) ea_stage(&stage[warp][0][lane], wsrc);
+    int in_flush = 0;
+    for (int it = 0; it < ntiles; it++) {
+        const int buf = it & 1;
+        if (it + 1 < ntiles) {
+            ea_stage(&stage[warp][buf ^ 1][lane], wsrc + (int64_t)(it + 1) * EA_WT);
+            ea_wait<1>();
+        } else {
+            ea_wait<0>();
         }
         __syncwarp();
-        float sm[NACC1], cm[NACC1];
-#pragma unroll
-        for (int k = 0; k < NACC1; k++) { sm[k] = 0.f; cm[k] = 0.f; }
+        bool beyond;
+        {
+            const EA1Mx& r = stage[warp][buf][lane];
+            const float3 p = fr.offset(r.a, r.b);
+            offs[warp][buf][lane] = make_float4(p.x, p.y, p.z, r.a.w);
+            beyond = fr.box_dist2(p) * r.a.w > zeta_skip_s<K>();
+        }
+        __syncwarp();
+        if (!(zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, beyond))) {
 #pragma unroll 1
-        for (int sub = 0; sub < UJ_TILE; sub += EA_SUB) {
-            float sv[EA_SUB], r2v[EA_SUB];
-            bool far = true;
+            for (int sub = 0; sub < EA_WT; sub += EA_SUB) {
+                float sv[EA_SUB], r2v[EA_SUB];
+                bool far = true;
 #pragma unroll
-            for (int jj = 0; jj < EA_SUB; jj++) {
-                const float4 h = off[warp][sub + jj];
-                const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
-                r2v[jj] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                sv[jj] = r2v[jj] * h.w;
-                far = far && sv[jj] > zeta_skip_s<K>();
+                for (int jj = 0; jj < EA_SUB; jj++) {
+                    const float4 h = offs[warp][buf][sub + jj];
+                    const float dx = fr.me.x - h.x, dy = fr.me.y - h.y, dz = fr.me.z - h.z;
+                    r2v[jj] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    sv[jj] = r2v[jj] * h.w;
+                    far = far && sv[jj] > zeta_skip_s<K>();
+                }
+                if (zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, far)) continue;
+                float f[NACC1] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int jj = 0; jj < EA_SUB; jj++) {
+                    const int j = sub + jj;
+                    const float4 h = offs[warp][buf][j];
+                    const float dx = fr.me.x - h.x, dy = fr.me.y - h.y, dz = fr.me.z - h.z;
+                    float zh = zhat_f32<K>(sv[jj]);
+                    zh = r2v[jj] == 0.0f ? 0.0f : zh;     // the self pair and coincident pairs
+                    const float4 g = stage[warp][buf][j].g, v = stage[warp][buf][j].v;
+                    const float wh = fmaf(g.x, me.a.x, fmaf(g.y, me.a.y, g.z * me.a.z)) -
+                                     fmaf(v.x, me.sb.x, fmaf(v.y, me.sb.y, v.z * me.sb.z));
+                    f[0] = fmaf(zh, g.x, f[0]); f[1] = fmaf(zh, g.y, f[1]); f[2] = fmaf(zh, g.z, f[2]);
+                    const float c = zh * wh * kappa_f32<K>(sv[jj]) * h.w;
+                    f[3] = fmaf(c, dx, f[3]); f[4] = fmaf(c, dy, f[4]); f[5] = fmaf(c, dz, f[5]);
+                }
+#pragma unroll
+                for (int k = 0; k < NACC1; k++) comp_add(sm[k], cm[k], f[k]);
             }
-            if (zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, far)) continue;
-            float f[NACC1] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int jj = 0; jj < EA_SUB; jj++) {
-                const int j = sub + jj;
-                const float4 h = off[warp][j];
-                const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
-                float zh = zhat_f32<K>(sv[jj]);
-                zh = r2v[jj] == 0.0f ? 0.0f : zh;     // the self pair and coincident pairs
-                const float4 g = tile[j].g, v = tile[j].v;
-                const float wh = fmaf(g.x, me.a.x, fmaf(g.y, me.a.y, g.z * me.a.z)) -
-                                 fmaf(v.x, me.sb.x, fmaf(v.y, me.sb.y, v.z * me.sb.z));
-                f[0] = fmaf(zh, g.x, f[0]); f[1] = fmaf(zh, g.y, f[1]); f[2] = fmaf(zh, g.z, f[2]);
-                const float c = zh * wh * kappa_f32<K>(sv[jj]) * h.w;
-                f[3] = fmaf(c, dx, f[3]); f[4] = fmaf(c, dy, f[4]); f[5] = fmaf(c, dz, f[5]);
-            }
-#pragma unroll
-            for (int k = 0; k < NACC1; k++) comp_add(sm[k], cm[k], f[k]);
         }
+        if (++in_flush == EA_FLUSH) {
+            in_flush = 0;
 #pragma unroll
-        for (int k = 0; k < NACC1; k++) acc[k] += (double)sm[k] + (double)cm[k];
-        __syncwarp();
+            for (int k = 0; k < NACC1; k++) { acc[k] += (double)sm[k] + (double)cm[k]; sm[k] = cm[k] = 0.f; }
+        }
+        __syncwarp();   // every lane is done with `buf` before it is refilled
     }
+#pragma unroll
+    for (int k = 0; k < NACC1; k++) acc[k] += (double)sm[k] + (double)cm[k];
     if (t < n) write_partial(partial, NACC1, n_pad, t, acc);
 }
 
+// Pass 2: lanes are sources s (Morton position), the tiles hold targets.
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
 ea2_mx(int64_t n, const EA1Mx* __restrict__ self, const double* __restrict__ gam, const TgtPos* __restrict__ tgt,
        const double* __restrict__ J, const uint8_t* __restrict__ st, bool transposed, int64_t n_pad,
        const EA2Mx* __restrict__ src, int64_t per_split, double* __restrict__ partial)
 {
-    __shared__ EA2Mx tile[UJ_TILE];
-    __shared__ float4 off[UJ_WARPS][UJ_TILE];
+    __shared__ EA2Mx stage[UJ_WARPS][2][EA_WT];
+    __shared__ float4 offs[UJ_WARPS][2][EA_WT];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t s = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const EA1Mx me = self[s < n ? s : n_pad - 1];
-    // this lane's Gamma_s and v_s unscaled (the mixed pass-1 payload carries ZNORM/sigma^3)
+    // this lane's Gamma_s and v_s unscaled (the pass-1 record carries ZNORM/sigma^3)
     float3 G = make_float3(0.f, 0.f, 0.f), V = make_float3(0.f, 0.f, 0.f);
     if (s < n) {
         const int64_t i = tgt[s].idx;
@@ -302,68 +388,85 @@ ea2_mx(int64_t n, const EA1Mx* __restrict__ self, const double* __restrict__ gam
             V = make_float3((float)v[0], (float)v[1], (float)v[2]);
         }
     }
-    const double ox = __shfl_sync(0xffffffffu, me.x, 0), oy = __shfl_sync(0xffffffffu, me.y, 0),
-                 oz = __shfl_sync(0xffffffffu, me.z, 0);
-    const float3 so = s < n ? make_float3((float)(me.x - ox), (float)(me.y - oy), (float)(me.z - oz))
-                            : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
-    const float isig2 = me.isig2;
+    EaFrame fr;
+    fr.init(me.a, me.b, s < n);
+    const float isig2 = me.a.w;
+    float i2min = s < n ? isig2 : 3.0e38f;
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) i2min = fminf(i2min, __shfl_xor_sync(0xffffffffu, i2min, m));
     double acc[NACC2];
+    float sm[NACC2], cm[NACC2];
 #pragma unroll
-    for (int k = 0; k < NACC2; k++) acc[k] = 0.0;
+    for (int k = 0; k < NACC2; k++) { acc[k] = 0.0; sm[k] = 0.f; cm[k] = 0.f; }
     const int64_t s0 = (int64_t)blockIdx.y * per_split, s1 = min(s0 + per_split, n_pad);
-    for (int64_t base = s0; base < s1; base += UJ_TILE) {
-        __syncthreads();
-        tile[threadIdx.x] = src[base + threadIdx.x];
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < UJ_TILE / 32; q++) {
-            const int j = lane + 32 * q;
-            off[warp][j] = make_float4((float)(tile[j].x - ox), (float)(tile[j].y - oy), (float)(tile[j].z - oz), 0.f);
+    const int ntiles = (int)((s1 - s0) / EA_WT);
+    const EA2Mx* wsrc = src + s0 + lane;
+    if (ntiles > 0) ea_stage(&stage[warp][0][lane], wsrc);
+    int in_flush = 0;
+    for (int it = 0; it < ntiles; it++) {
+        const int buf = it & 1;
+        if (it + 1 < ntiles) {
+            ea_stage(&stage[warp][buf ^ 1][lane], wsrc + (int64_t)(it + 1) * EA_WT);
+            ea_wait<1>();
+        } else {
+            ea_wait<0>();
         }
         __syncwarp();
-        float sm[NACC2], cm[NACC2];
-#pragma unroll
-        for (int k = 0; k < NACC2; k++) { sm[k] = 0.f; cm[k] = 0.f; }
-#pragma unroll 1
-        for (int sub = 0; sub < UJ_TILE; sub += EA_SUB) {
-            float sv[EA_SUB], r2v[EA_SUB];
-            bool far = true;
-#pragma unroll
-            for (int jj = 0; jj < EA_SUB; jj++) {
-                const float4 h = off[warp][sub + jj];
-                const float dx = so.x - h.x, dy = so.y - h.y, dz = so.z - h.z;
-                r2v[jj] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                sv[jj] = r2v[jj] * isig2;
-                far = far && sv[jj] > zeta_skip_s<K>();
-            }
-            if (zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, far)) continue;
-            float f[NACC2];
-#pragma unroll
-            for (int k = 0; k < NACC2; k++) f[k] = 0.f;
-#pragma unroll
-            for (int jj = 0; jj < EA_SUB; jj++) {
-                const int j = sub + jj;
-                const float4 h = off[warp][j];
-                const float dx = so.x - h.x, dy = so.y - h.y, dz = so.z - h.z;
-                float zh = zhat_f32<K>(sv[jj]);
-                zh = r2v[jj] == 0.0f ? 0.0f : zh;
-                const float4 a = tile[j].a, sb = tile[j].sb;
-                const float w = fmaf(G.x, a.x, fmaf(G.y, a.y, G.z * a.z)) - fmaf(V.x, sb.x, fmaf(V.y, sb.y, V.z * sb.z));
-                const float kp = kappa_f32<K>(sv[jj]);
-                f[0] = fmaf(zh, a.x, f[0]); f[1] = fmaf(zh, a.y, f[1]); f[2] = fmaf(zh, a.z, f[2]);
-                f[3] = fmaf(zh, sb.x, f[3]); f[4] = fmaf(zh, sb.y, f[4]); f[5] = fmaf(zh, sb.z, f[5]);
-                const float zw = zh * w;
-                const float c = zw * kp;
-                f[6] = fmaf(c, dx, f[6]); f[7] = fmaf(c, dy, f[7]); f[8] = fmaf(c, dz, f[8]);
-                f[9] = fmaf(zw, fmaf(sv[jj], kp, 3.0f), f[9]);
-            }
-#pragma unroll
-            for (int k = 0; k < NACC2; k++) comp_add(sm[k], cm[k], f[k]);
+        bool beyond;
+        {
+            const EA2Mx& r = stage[warp][buf][lane];
+            const float3 p = fr.offset(r.h, r.l);
+            offs[warp][buf][lane] = make_float4(p.x, p.y, p.z, 0.f);
+            beyond = fr.box_dist2(p) * i2min > zeta_skip_s<K>();
         }
+        __syncwarp();
+        if (!(zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, beyond))) {
+#pragma unroll 1
+            for (int sub = 0; sub < EA_WT; sub += EA_SUB) {
+                float sv[EA_SUB], r2v[EA_SUB];
+                bool far = true;
 #pragma unroll
-        for (int k = 0; k < NACC2; k++) acc[k] += (double)sm[k] + (double)cm[k];
+                for (int jj = 0; jj < EA_SUB; jj++) {
+                    const float4 h = offs[warp][buf][sub + jj];
+                    const float dx = fr.me.x - h.x, dy = fr.me.y - h.y, dz = fr.me.z - h.z;
+                    r2v[jj] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    sv[jj] = r2v[jj] * isig2;
+                    far = far && sv[jj] > zeta_skip_s<K>();
+                }
+                if (zeta_skip_s<K>() > 0.0f && __all_sync(0xffffffffu, far)) continue;
+                float f[NACC2];
+#pragma unroll
+                for (int k = 0; k < NACC2; k++) f[k] = 0.f;
+#pragma unroll
+                for (int jj = 0; jj < EA_SUB; jj++) {
+                    const int j = sub + jj;
+                    const float4 h = offs[warp][buf][j];
+                    const float dx = fr.me.x - h.x, dy = fr.me.y - h.y, dz = fr.me.z - h.z;
+                    float zh = zhat_f32<K>(sv[jj]);
+                    zh = r2v[jj] == 0.0f ? 0.0f : zh;
+                    const float4 a = stage[warp][buf][j].a, sb = stage[warp][buf][j].sb;
+                    const float w = fmaf(G.x, a.x, fmaf(G.y, a.y, G.z * a.z)) - fmaf(V.x, sb.x, fmaf(V.y, sb.y, V.z * sb.z));
+                    const float kp = kappa_f32<K>(sv[jj]);
+                    f[0] = fmaf(zh, a.x, f[0]); f[1] = fmaf(zh, a.y, f[1]); f[2] = fmaf(zh, a.z, f[2]);
+                    f[3] = fmaf(zh, sb.x, f[3]); f[4] = fmaf(zh, sb.y, f[4]); f[5] = fmaf(zh, sb.z, f[5]);
+                    const float zw = zh * w;
+                    const float c = zw * kp;
+                    f[6] = fmaf(c, dx, f[6]); f[7] = fmaf(c, dy, f[7]); f[8] = fmaf(c, dz, f[8]);
+                    f[9] = fmaf(zw, fmaf(sv[jj], kp, 3.0f), f[9]);
+                }
+#pragma unroll
+                for (int k = 0; k < NACC2; k++) comp_add(sm[k], cm[k], f[k]);
+            }
+        }
+        if (++in_flush == EA_FLUSH) {
+            in_flush = 0;
+#pragma unroll
+            for (int k = 0; k < NACC2; k++) { acc[k] += (double)sm[k] + (double)cm[k]; sm[k] = cm[k] = 0.f; }
+        }
         __syncwarp();
     }
+#pragma unroll
+    for (int k = 0; k < NACC2; k++) acc[k] += (double)sm[k] + (double)cm[k];
     if (s < n) write_partial(partial, NACC2, n_pad, s, acc);
 }
 

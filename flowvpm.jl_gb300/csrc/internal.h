@@ -36,6 +36,12 @@ struct __align__(16) SrcF64 { double2 xy, z_isig, gxy, gz_sig; };
 // FP32; g = v = 0 for static sources.
 struct __align__(16) SrcEstrMixed { double x, y, z; float isig2, pad; float4 g; float4 v; };
 
+// Packed source of the all-pairs and near-field mixed Estr kernels, 64 B:
+// position as a double-float (a.xyz + b.xyz), a.w = 1/sigma^2,
+// g = ZNORM Gamma / sigma^3 and v = ZNORM (J^T Gamma) / sigma^3 (or J Gamma), in
+// FP32; g = v = 0 for static sources.
+struct __align__(16) SrcEstrDF { float4 a, b, g, v; };
+
 // Packed source of the FP64 Estr kernel, 80 B:
 //   (x, y), (z, 1/sigma), (Gamma_x, Gamma_y), (Gamma_z, v_x), (v_y, v_z)
 // with Gamma and v = J^T Gamma zero for static sources.

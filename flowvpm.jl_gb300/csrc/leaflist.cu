@@ -29,6 +29,12 @@ constexpr int NF_MID_BLKS = 4;               // blocks summed in FP32 before the
 #ifndef VPM_NF_MIN_BLOCKS
 #define VPM_NF_MIN_BLOCKS 4                  // resident blocks per SM the UJ kernel is compiled for
 #endif
+#ifndef VPM_NF_LEAF
+#define VPM_NF_LEAF 0                        // 1: near-field UJ and Estr per target leaf; 0: warp groups
+#endif
+#ifndef VPM_NF_DF
+#define VPM_NF_DF 1                          // nf_uj_leaf: 1 = double-float displacement on every group
+#endif
 
 __global__ void tgt_from_perm(int64_t n, const double* __restrict__ x, const int32_t* __restrict__ perm,
                               TgtPos* __restrict__ out)
@@ -54,6 +60,26 @@ __global__ void leaf_pack_mixed(int64_t n, const double* __restrict__ x, const d
     const float xh = (float)px, yh = (float)py, zh = (float)pz;
     const double sig = (K == K_SING) ? 1.0 : sgs[i];
     const double k = singular_tail<K>() ? -C4 : -C4 / (sig * sig * sig);
+    SrcMixed p;
+    p.a = make_float4(xh, yh, zh, (float)(sig * sig));
+    p.b = make_float4((float)(px - (double)xh), (float)(py - (double)yh), (float)(pz - (double)zh), (float)(1.0 / sig));
+    p.gam = make_float4((float)(k * gs[3 * i]), (float)(k * gs[3 * i + 1]), (float)(k * gs[3 * i + 2]), 0.f);
+    out[o] = p;
+}
+
+// As leaf_pack_mixed, with gam = -Gamma/(4 pi sigma^3) for every kernel (nf_uj_leaf).
+template <int K>
+__global__ void leaf_pack_scaled(int64_t n, const double* __restrict__ x, const double* __restrict__ gs,
+                                 const double* __restrict__ sgs, const int32_t* __restrict__ perm,
+                                 SrcMixed* __restrict__ out)
+{
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int64_t i = perm[o];
+    const double px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+    const float xh = (float)px, yh = (float)py, zh = (float)pz;
+    const double sig = (K == K_SING) ? 1.0 : sgs[i];
+    const double k = -C4 / (sig * sig * sig);
     SrcMixed p;
     p.a = make_float4(xh, yh, zh, (float)(sig * sig));
     p.b = make_float4((float)(px - (double)xh), (float)(py - (double)yh), (float)(pz - (double)zh), (float)(1.0 / sig));
@@ -283,6 +309,425 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
     for (int k = 0; k < 3; k++) U[3 * (int64_t)me.idx + k] += dU[k];
 #pragma unroll
     for (int k = 0; k < 9; k++) J[9 * (int64_t)me.idx + k] += j9[k];
+}
+
+// ------------------------------------------------- UJ, FP32-comp, per leaf
+// One warp per target leaf, taken in chunks of at most 32 targets.  A chunk of
+// a targets runs in Ks = min(8, 32/a) stripes: lane (i, k) = (lane % a,
+// lane / a) holds target i and evaluates stripe k's share of every tile of
+// sources, so a chunk uses a Ks of the 32 lanes and all of them need every
+// source (no target masks: the leaf's own source list is walked, straight from
+// its CSR row).  A tile holds T = 4 Ks g <= 32 sources, stripe k taking the
+// g groups of four at [k T/Ks, (k + 1) T/Ks).  At the end of a chunk the
+// stripes' FP64 sums are added in stripe order.
+//
+// Displacements: FP32 offsets from the chunk's first target (the warp origin),
+// dx = t_off - s_off, whose error is at most ~1.5 ulp of |dx| when
+// |dx| > 2b (b: the chunk's extent around the origin).  A group of four in
+// which any lane has a pair closer than 2b takes the double-float difference
+// (x_t,hi - x_s,hi) + (x_t,lo - x_s,lo) instead (one vote).  Target and source
+// offsets are formed by the same FP32 double-float operations, so the self
+// pair has r^2 == 0 exactly on either path.  Sources carry
+// gam = -Gamma/(4 pi sigma^3), so the pair form needs no sigma^3 factor.
+
+// Source ranges of one target leaf, walked T at a time across leaf boundaries.
+// Lane i keeps source leaf wbase + i of a 32-leaf window of the CSR row.
+struct LeafWalk {
+    const int32_t* col;
+    const int32_t* lb;
+    const int32_t* le;
+    int e, e1, off, wbase;
+    int2 win;
+
+    __device__ __forceinline__ void load(int lane)
+    {
+        win = make_int2(0, 0);
+        if (wbase + lane < e1) {
+            const int c = col[wbase + lane];
+            win = make_int2(lb[c], le[c]);
+        }
+    }
+    __device__ __forceinline__ void init(const int32_t* c, const int32_t* b, const int32_t* en, int e0, int e_end,
+                                         int lane)
+    {
+        col = c; lb = b; le = en; e = e0; e1 = e_end; off = 0; wbase = e0;
+        load(lane);
+    }
+    // Next tile of at most T sources: this lane's source position (-1 for none) if lane < T;
+    // returns the tile's size.
+    __device__ __forceinline__ int next(int lane, int T, int& my_p)
+    {
+        int filled = 0;
+        my_p = -1;
+        while (filled < T && e < e1) {
+            if (e - wbase >= 32) {
+                wbase = e;
+                load(lane);
+            }
+            const int k = e - wbase;
+            const int p0 = __shfl_sync(0xffffffffu, win.x, k);
+            const int p1 = __shfl_sync(0xffffffffu, win.y, k);
+            const int take = min(p1 - p0 - off, T - filled);
+            if (lane >= filled && lane < filled + take) my_p = p0 + off + (lane - filled);
+            filled += take;
+            off += take;
+            if (off == p1 - p0) { e++; off = 0; }
+        }
+        return filled;
+    }
+};
+
+// Four sources j0..j0+3 of the tile against this lane's target (see above); idle lanes
+// take part in the votes only.
+template <int K>
+__device__ __forceinline__ void pair4_leaf(const float3& to, const float3& th, const float3& tl, float r2n,
+                                           const float4* __restrict__ off, const SrcMixed* __restrict__ tile, int j0,
+                                           bool idle, float (&u)[3], float (&jq)[8], float (&w)[3])
+{
+    float dx[4], dy[4], dz[4], r2[4], i2[4];
+    bool far = !VPM_NF_DF;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float4 h = off[j0 + q];
+        i2[q] = h.w;
+        if (!VPM_NF_DF) {
+            dx[q] = to.x - h.x;
+            dy[q] = to.y - h.y;
+            dz[q] = to.z - h.z;
+            r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
+            far = far && r2[q] > r2n;
+        }
+    }
+    if (VPM_NF_DF || !__all_sync(0xffffffffu, far || idle)) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float4 a = tile[j0 + q].a, b = tile[j0 + q].b;
+            dx[q] = (th.x - a.x) + (tl.x - b.x);
+            dy[q] = (th.y - a.y) + (tl.y - b.y);
+            dz[q] = (th.z - a.z) + (tl.z - b.z);
+            r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
+        }
+    }
+    float s4[4], G[4], Q[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) s4[q] = idle ? 1.0e4f : r2[q] * i2[q];
+    near_GQ4<K, true>(s4, i2, G, Q);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const bool on = !idle && r2[q] > 0.0f;
+        accum_pair(dx[q], dy[q], dz[q], on ? G[q] : 0.0f, on ? Q[q] : 0.0f, tile[j0 + q].gam, u, jq, w);
+    }
+}
+
+constexpr int NF_BLK_PAIRS = 64;    // pairs per lane summed in FP32 before the mid-level sum
+constexpr int NF_MID_PAIRS = 256;   // pairs per lane summed in the mid-level FP32 sum before FP64
+
+template <int K>
+__global__ void __launch_bounds__(NF_THREADS, VPM_NF_MIN_BLOCKS)
+nf_uj_leaf(int64_t nleaves, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb,
+           const int32_t* __restrict__ le, const int32_t* __restrict__ row, const int32_t* __restrict__ col,
+           const SrcMixed* __restrict__ src, double* U, double* J)
+{
+    __shared__ SrcMixed tile[NF_WARPS][32];
+    __shared__ float4 off[NF_WARPS][32];
+    __shared__ double acc64[14][NF_THREADS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t leaf = (int64_t)blockIdx.x * NF_WARPS + warp;
+    if (leaf >= nleaves) return;
+    const int p_begin = lb[leaf], p_end = le[leaf];
+    for (int c0 = p_begin; c0 < p_end; c0 += 32) {
+        const int na = min(32, p_end - c0);
+        const int ks = min(8, 32 / na);
+        const int T = 4 * ks * max(1, 32 / (4 * ks));
+        const int m = T / ks;                               // sources per stripe and tile
+        const int ti = lane % na, stripe = lane / na;
+        const bool idle = stripe >= ks;
+        const TgtPos me = tgt[c0 + ti];
+        const TgtPos o = tgt[c0];
+        const float3 th = make_float3((float)me.x, (float)me.y, (float)me.z);
+        const float3 tl = make_float3((float)(me.x - (double)th.x), (float)(me.y - (double)th.y),
+                                      (float)(me.z - (double)th.z));
+        const float3 oh = make_float3((float)o.x, (float)o.y, (float)o.z);
+        const float3 ol = make_float3((float)(o.x - (double)oh.x), (float)(o.y - (double)oh.y),
+                                      (float)(o.z - (double)oh.z));
+        // the same FP32 double-float operations as the sources' offsets: the self pair has r^2 == 0
+        const float3 to = make_float3(df_offset(th.x, tl.x, oh.x, ol.x), df_offset(th.y, tl.y, oh.y, ol.y),
+                                      df_offset(th.z, tl.z, oh.z, ol.z));
+        float b2 = fmaf(to.x, to.x, fmaf(to.y, to.y, to.z * to.z));
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, sh));
+        const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
+#pragma unroll
+        for (int k = 0; k < 14; k++) acc64[k][threadIdx.x] = 0.0;
+        float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
+        float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) { mj[k] = 0.f; jq[k] = 0.f; }
+        int blk = 0, mid = 0;
+        LeafWalk walk;
+        walk.init(col, lb, le, row[leaf], row[leaf + 1], lane);
+        for (;;) {
+            int sp;
+            const int cnt = walk.next(lane, T, sp);
+            if (cnt == 0) break;
+            __syncwarp();
+            if (lane < T) {
+                SrcMixed sj;
+                if (sp >= 0) {
+                    sj = src[sp];
+                } else {   // padding: far away, no strength
+                    sj.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+                    sj.b = make_float4(0.f, 0.f, 0.f, 1.f);
+                    sj.gam = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                tile[warp][lane] = sj;
+                off[warp][lane] = make_float4(df_offset(sj.a.x, sj.b.x, oh.x, ol.x),
+                                              df_offset(sj.a.y, sj.b.y, oh.y, ol.y),
+                                              df_offset(sj.a.z, sj.b.z, oh.z, ol.z), sj.b.w * sj.b.w);
+            }
+            __syncwarp();
+            // stripe k's groups; every lane runs the same trip count (warp-wide votes)
+            const int j1 = (idle ? 0 : stripe) * m;
+            for (int q = 0; q < m; q += 4)
+                pair4_leaf<K>(to, th, tl, r2n, off[warp], tile[warp], j1 + q, idle, u, jq, w);
+            blk += m;
+            if (blk >= NF_BLK_PAIRS) {
+                blk = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }
+#pragma unroll
+                for (int k = 0; k < 8; k++) { mj[k] += jq[k]; jq[k] = 0.f; }
+                mid += NF_BLK_PAIRS;
+                if (mid >= NF_MID_PAIRS) {
+                    mid = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        acc64[k][threadIdx.x] += (double)mu[k];
+                        acc64[3 + k][threadIdx.x] += (double)mw[k];
+                        mu[k] = 0.f; mw[k] = 0.f;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; k++) { acc64[6 + k][threadIdx.x] += (double)mj[k]; mj[k] = 0.f; }
+                }
+            }
+        }
+        // this lane's totals, then the stripes of each target added in order
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            acc64[k][threadIdx.x] += (double)mu[k] + (double)u[k];
+            acc64[3 + k][threadIdx.x] += (double)mw[k] + (double)w[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc64[6 + k][threadIdx.x] += (double)mj[k] + (double)jq[k];
+        __syncwarp();
+        if (lane < na) {
+            double dU[3], dW[3], dJ[8];
+            const int base = threadIdx.x - lane;
+#pragma unroll
+            for (int k = 0; k < 3; k++) { dU[k] = 0.0; dW[k] = 0.0; }
+#pragma unroll
+            for (int k = 0; k < 8; k++) dJ[k] = 0.0;
+            for (int st = 0; st < ks; st++) {
+                const int l2 = base + lane + st * na;
+#pragma unroll
+                for (int k = 0; k < 3; k++) { dU[k] += acc64[k][l2]; dW[k] += acc64[3 + k][l2]; }
+#pragma unroll
+                for (int k = 0; k < 8; k++) dJ[k] += acc64[6 + k][l2];
+            }
+            double j9[9];
+#pragma unroll
+            for (int k = 0; k < 8; k++) j9[k] = -3.0 * dJ[k];
+            j9[8] = 3.0 * (dJ[0] + dJ[4]);
+            j9[1] -= dW[2]; j9[2] += dW[1]; j9[3] += dW[2]; j9[5] -= dW[0]; j9[6] -= dW[1]; j9[7] += dW[0];
+            const int64_t idx = me.idx;
+#pragma unroll
+            for (int k = 0; k < 3; k++) U[3 * idx + k] += dU[k];
+#pragma unroll
+            for (int k = 0; k < 9; k++) J[9 * idx + k] += j9[k];
+        }
+        __syncwarp();   // acc64 is reset by the next chunk
+    }
+}
+
+// ----------------------------------------------- Estr, FP32-comp, per leaf
+// The layout of nf_uj_leaf (one warp per target leaf, chunks of <= 32 targets
+// in Ks stripes, the leaf's own CSR row walked T sources at a time) for the
+// Estr sums Zg = sum z g, Zv = sum z v of the factored form (estr.cu).  Target
+// and source offsets from the chunk's first target are formed by the same
+// FP32 double-float operations, so coincident particles (the self pair
+// included) have r^2 == 0 exactly and are skipped (ZETA: kept).  Per lane the
+// pairs of a tile are summed in FP32 and added with compensation (comp_add)
+// once at least 8 have gathered, and to FP64 every 256.
+template <int K>
+__global__ void leaf_pack_estr_df(int64_t n, const double* __restrict__ x, const double* __restrict__ gs,
+                                  const double* __restrict__ sgs, const double* __restrict__ Js,
+                                  const uint8_t* __restrict__ static_s, bool transposed,
+                                  const int32_t* __restrict__ perm, SrcEstrDF* __restrict__ out)
+{
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int64_t i = perm[o];
+    const bool st = static_s && static_s[i];
+    const double gx = gs[3 * i], gy = gs[3 * i + 1], gz = gs[3 * i + 2];
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    if (Js) {
+        const double* J = Js + 9 * i;
+        if (transposed) {
+            vx = J[0] * gx + J[1] * gy + J[2] * gz; vy = J[3] * gx + J[4] * gy + J[5] * gz; vz = J[6] * gx + J[7] * gy + J[8] * gz;
+        } else {
+            vx = J[0] * gx + J[3] * gy + J[6] * gz; vy = J[1] * gx + J[4] * gy + J[7] * gz; vz = J[2] * gx + J[5] * gy + J[8] * gz;
+        }
+    }
+    const double isig = 1.0 / sgs[i];
+    const double k = st ? 0.0 : zeta_norm(K) * isig * isig * isig;
+    const double px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+    const float xh = (float)px, yh = (float)py, zh = (float)pz;
+    SrcEstrDF p;
+    p.a = make_float4(xh, yh, zh, (float)(isig * isig));
+    p.b = make_float4((float)(px - (double)xh), (float)(py - (double)yh), (float)(pz - (double)zh), 0.f);
+    p.g = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), 0.f);
+    p.v = make_float4((float)(k * vx), (float)(k * vy), (float)(k * vz), 0.f);
+    out[o] = p;
+}
+
+template <int K, bool DZ = false, bool ZETA = false>
+__global__ void __launch_bounds__(NF_THREADS)
+nf_estr_leaf(int64_t nleaves, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb,
+             const int32_t* __restrict__ le, const int32_t* __restrict__ row, const int32_t* __restrict__ col,
+             const SrcEstrDF* __restrict__ src, const double* __restrict__ Jt, const uint8_t* __restrict__ static_t,
+             bool transposed, double* SFS, float3 fd = make_float3(0.f, 0.f, 0.f))
+{
+    static_assert(!(DZ && ZETA), "one mode at a time");
+    __shared__ SrcEstrDF tile[NF_WARPS][32];
+    __shared__ float4 off[NF_WARPS][32];
+    __shared__ double acc64[6][NF_THREADS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t leaf = (int64_t)blockIdx.x * NF_WARPS + warp;
+    if (leaf >= nleaves) return;
+    const int p_begin = lb[leaf], p_end = le[leaf];
+    for (int c0 = p_begin; c0 < p_end; c0 += 32) {
+        const int na = min(32, p_end - c0);
+        const int ks = min(8, 32 / na);
+        const int T = 4 * ks * max(1, 32 / (4 * ks));
+        const int m = T / ks;
+        const int ti = lane % na, stripe = lane / na;
+        const bool idle = stripe >= ks;
+        const TgtPos me = tgt[c0 + ti];
+        const TgtPos o = tgt[c0];
+        const float3 oh = make_float3((float)o.x, (float)o.y, (float)o.z);
+        const float3 ol = make_float3((float)(o.x - (double)oh.x), (float)(o.y - (double)oh.y),
+                                      (float)(o.z - (double)oh.z));
+        float3 to;
+        {
+            const float3 th = make_float3((float)me.x, (float)me.y, (float)me.z);
+            const float3 tl = make_float3((float)(me.x - (double)th.x), (float)(me.y - (double)th.y),
+                                          (float)(me.z - (double)th.z));
+            to = make_float3(df_offset(th.x, tl.x, oh.x, ol.x), df_offset(th.y, tl.y, oh.y, ol.y),
+                             df_offset(th.z, tl.z, oh.z, ol.z));
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc64[k][threadIdx.x] = 0.0;
+        float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
+        float fg[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f};
+        int part = 0, flush = 0;
+        LeafWalk walk;
+        walk.init(col, lb, le, row[leaf], row[leaf + 1], lane);
+        for (;;) {
+            int sp;
+            const int cnt = walk.next(lane, T, sp);
+            if (cnt == 0) break;
+            __syncwarp();
+            if (lane < T) {
+                SrcEstrDF sj;
+                if (sp >= 0) {
+                    sj = src[sp];
+                } else {   // padding: far away, no payload
+                    sj.a = make_float4(1.0e6f, 1.0e6f, 1.0e6f, 1.f);
+                    sj.b = sj.g = sj.v = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                tile[warp][lane] = sj;
+                off[warp][lane] = make_float4(df_offset(sj.a.x, sj.b.x, oh.x, ol.x),
+                                              df_offset(sj.a.y, sj.b.y, oh.y, ol.y),
+                                              df_offset(sj.a.z, sj.b.z, oh.z, ol.z), sj.a.w);
+            }
+            __syncwarp();
+            if (!idle) {
+                const int j1 = stripe * m;
+                for (int q = 0; q < m; q++) {
+                    const float4 h = off[warp][j1 + q];
+                    const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float s2 = r2 * h.w;
+                    float z = zhat_f32<K>(s2);
+                    if constexpr (DZ) z *= zeta_ratio_m1<K>(s2, fd);
+                    if constexpr (!ZETA) z = r2 == 0.0f ? 0.0f : z;
+                    const float4 g = tile[warp][j1 + q].g;
+                    fg[0] = fmaf(z, g.x, fg[0]); fg[1] = fmaf(z, g.y, fg[1]); fg[2] = fmaf(z, g.z, fg[2]);
+                    if constexpr (!ZETA) {
+                        const float4 v = tile[warp][j1 + q].v;
+                        fv[0] = fmaf(z, v.x, fv[0]); fv[1] = fmaf(z, v.y, fv[1]); fv[2] = fmaf(z, v.z, fv[2]);
+                    }
+                }
+                part += m;
+                if (part >= 8) {
+                    part = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        comp_add(sg[k], cg[k], fg[k]); fg[k] = 0.f;
+                        if constexpr (!ZETA) { comp_add(sv[k], cv[k], fv[k]); fv[k] = 0.f; }
+                    }
+                }
+                flush += m;
+                if (flush >= 256) {
+                    flush = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        acc64[k][threadIdx.x] += (double)sg[k] + (double)cg[k];
+                        acc64[3 + k][threadIdx.x] += (double)sv[k] + (double)cv[k];
+                        sg[k] = cg[k] = sv[k] = cv[k] = 0.f;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            acc64[k][threadIdx.x] += ((double)sg[k] + (double)cg[k]) + (double)fg[k];
+            acc64[3 + k][threadIdx.x] += ((double)sv[k] + (double)cv[k]) + (double)fv[k];
+        }
+        __syncwarp();
+        if (lane < na) {
+            const int64_t idx = me.idx;
+            const bool live = ZETA || !(static_t && static_t[idx]);
+            if (live) {
+                double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
+                const int base = threadIdx.x - lane;
+                for (int st = 0; st < ks; st++) {
+                    const int l2 = base + lane + st * na;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) { zg[k] += acc64[k][l2]; zv[k] += acc64[3 + k][l2]; }
+                }
+                if constexpr (ZETA) {
+#pragma unroll
+                    for (int k = 0; k < 3; k++) SFS[3 * idx + k] += zg[k];
+                } else {
+                    const double* Jp = Jt + 9 * idx;
+                    double o3[3];
+                    if (transposed) {
+                        o3[0] = Jp[0] * zg[0] + Jp[1] * zg[1] + Jp[2] * zg[2] - zv[0];
+                        o3[1] = Jp[3] * zg[0] + Jp[4] * zg[1] + Jp[5] * zg[2] - zv[1];
+                        o3[2] = Jp[6] * zg[0] + Jp[7] * zg[1] + Jp[8] * zg[2] - zv[2];
+                    } else {
+                        o3[0] = Jp[0] * zg[0] + Jp[3] * zg[1] + Jp[6] * zg[2] - zv[0];
+                        o3[1] = Jp[1] * zg[0] + Jp[4] * zg[1] + Jp[7] * zg[2] - zv[1];
+                        o3[2] = Jp[2] * zg[0] + Jp[5] * zg[1] + Jp[8] * zg[2] - zv[2];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 3; k++) SFS[3 * idx + k] += o3[k];
+                }
+            }
+        }
+        __syncwarp();   // acc64 is reset by the next chunk
+    }
 }
 
 // ------------------------------------------- dynamic procedure, FP32-comp
@@ -577,12 +1022,19 @@ static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* wo
     void* src = p;
     const unsigned g = (unsigned)((n + 255) / 256);
     const unsigned gb = (unsigned)((L.ngroups + NF_WARPS - 1) / NF_WARPS);
+    const unsigned gl = (unsigned)((L.nleaves + NF_WARPS - 1) / NF_WARPS);
     tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
     *launches += 1;
     if (a.uj && a.precision) {
+#if VPM_NF_LEAF
+        leaf_pack_scaled<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
+        nf_uj_leaf<K><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row, L.col,
+                                                 (const SrcMixed*)src, a.U, a.J);
+#else
         leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
         nf_uj_mixed<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
                                                   (const SrcMixed*)src, a.U, a.J);
+#endif
         *launches += 2;
     } else if (a.uj) {
         leaf_pack_f64<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcF64*)src);
@@ -591,14 +1043,22 @@ static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* wo
         *launches += 2;
     }
     if (a.sfs) {
-        leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm,
-                                              a.precision, src);
-        if (a.precision)
-            nf_estr<K, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
-                                                        a.static_flags, a.transposed, a.SFS);
-        else
-            nf_estr<K, false><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
-                                                         a.static_flags, a.transposed, a.SFS);
+        if (VPM_NF_LEAF && a.precision) {
+            leaf_pack_estr_df<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm,
+                                                     (SrcEstrDF*)src);
+            nf_estr_leaf<K><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row, L.col,
+                                                       (const SrcEstrDF*)src, a.J, a.static_flags, a.transposed,
+                                                       a.SFS);
+        } else {
+            leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm,
+                                                  a.precision, src);
+            if (a.precision)
+                nf_estr<K, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
+                                                            a.static_flags, a.transposed, a.SFS);
+            else
+                nf_estr<K, false><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src,
+                                                             a.J, a.static_flags, a.transposed, a.SFS);
+        }
         *launches += 2;
     }
     return cudaGetLastError();
@@ -634,12 +1094,25 @@ static cudaError_t launch_leaf_dyn_k(const LeafArgs& a, const NearLists& L, doub
     }
     const float3 fd = make_float3((float)(1.0 / (alpha * alpha * alpha) - 1.0), (float)(1.0 / (alpha * alpha * alpha)),
                                   (float)(1.0 / (alpha * alpha) - 1.0));
+#if VPM_NF_LEAF
+    const unsigned gl = (unsigned)((L.nleaves + NF_WARPS - 1) / NF_WARPS);
+    leaf_pack_estr_df<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm,
+                                             (SrcEstrDF*)src);
+    nf_estr_leaf<K, true><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row, L.col,
+                                                     (const SrcEstrDF*)src, a.J, a.static_flags, a.transposed, dSFS,
+                                                     fd);
+    leaf_pack_estr_df<K><<<g, 256, 0, st>>>(n, a.x, a.gam, sig_a, dJ, a.static_flags, a.transposed, L.perm,
+                                             (SrcEstrDF*)src);
+    nf_estr_leaf<K><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row, L.col,
+                                               (const SrcEstrDF*)src, dJ, a.static_flags, a.transposed, dSFS);
+#else
     leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, a.J, a.static_flags, a.transposed, L.perm, 1, src);
     nf_estr<K, true, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, a.J,
                                                       a.static_flags, a.transposed, dSFS, fd);
     leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, sig_a, dJ, a.static_flags, a.transposed, L.perm, 1, src);
     nf_estr<K, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src, dJ,
                                                 a.static_flags, a.transposed, dSFS);
+#endif
     *launches += 4;
     return cudaGetLastError();
 }
@@ -671,14 +1144,22 @@ static cudaError_t launch_leaf_zeta_k(const LeafArgs& a, const NearLists& L, dou
     void* src = p;
     const unsigned g = (unsigned)((n + 255) / 256);
     const unsigned gb = (unsigned)((L.ngroups + NF_WARPS - 1) / NF_WARPS);
+    const unsigned gl = (unsigned)((L.nleaves + NF_WARPS - 1) / NF_WARPS);
     tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
-    leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, nullptr, nullptr, true, L.perm, a.precision, src);
-    if (a.precision)
-        nf_estr<K, true, false, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src,
-                                                                 nullptr, nullptr, true, W);
-    else
-        nf_estr<K, false, false, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs, src,
-                                                                  nullptr, nullptr, true, W);
+    if (VPM_NF_LEAF && a.precision) {
+        leaf_pack_estr_df<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, nullptr, nullptr, true, L.perm, (SrcEstrDF*)src);
+        nf_estr_leaf<K, false, true><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row,
+                                                                L.col, (const SrcEstrDF*)src, nullptr, nullptr, true,
+                                                                W);
+    } else {
+        leaf_pack_estr<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, nullptr, nullptr, true, L.perm, a.precision, src);
+        if (a.precision)
+            nf_estr<K, true, false, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                                     src, nullptr, nullptr, true, W);
+        else
+            nf_estr<K, false, false, true><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
+                                                                      src, nullptr, nullptr, true, W);
+    }
     *launches += 3;
     return cudaGetLastError();
 }

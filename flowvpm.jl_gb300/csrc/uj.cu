@@ -242,6 +242,9 @@ constexpr int MID_BLOCKS = 16;
 #define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
 #endif
 constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
+#ifndef VPM_UJ_F32X2
+#define VPM_UJ_F32X2 0                      // 1: the packed-FP32 mixed kernel (uj_mixed_x2_kernel)
+#endif
 #ifndef VPM_UJ_SMEM_ACC
 // 1: the FP64 sums (touched once per 1,024 sources) live in shared memory, which frees the
 // registers for 7 resident blocks per SM instead of 5 -- measured 3.6 % faster at N = 2^20
@@ -390,6 +393,311 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     double acc[12] = {fU[0], fU[1], fU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
     write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
+// ------------------------------------------------- packed-FP32 mixed kernel
+// The mixed kernel with the pair math in Blackwell's packed FP32 instructions
+// (fma / mul / sub .rn.f32x2: two FP32 operations per lane and instruction),
+// each instruction taking one pair of sources.  The per-warp tile is staged as
+// before; the loading lanes then write it to a packed structure-of-arrays
+// layout per source pair (2p, 2p+1): offsets (x, y), (z, far threshold) and
+// strengths (gx, gy), (gz, -gx), (-gy, -gz), so that one 16-byte shared load
+// gives two packed operands.  Far groups (one vote per four sources, as
+// before) run entirely packed; near groups compute their displacements and
+// kernel forms per source and pack them for the same accumulation.  Sums are
+// kept per pair half (even / odd source) in FP32 blocks, then added in the
+// mid-level FP32 sums and in FP64 as in uj_mixed_kernel.
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 pk2(float lo, float hi)
+{
+    u64 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(u64 r, float& lo, float& hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+}
+__device__ __forceinline__ u64 ffma2(u64 a, u64 b, u64 c)
+{
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ u64 fmul2(u64 a, u64 b)
+{
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 fsub2(u64 a, u64 b)
+{
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// Packed source pair: px = (x0, x1, y0, y1), pz = (z0, z1, thr0, thr1),
+// ga = (gx0, gx1, gy0, gy1), gb = (gz0, gz1, -gx0, -gx1), gc = (-gy0, -gy1, -gz0, -gz1).
+struct __align__(16) PairX2 { float4 px, pz, ga, gb, gc; };
+
+// Accumulate two pairs (packed halves) of one lane: U += G c, W += G gam, J' += Q c_i dx_j.
+__device__ __forceinline__ void accum_x2(u64 dX, u64 dY, u64 dZ, u64 G, u64 Q, const PairX2& s, u64 (&u)[3],
+                                         u64 (&w)[3], u64 (&jq)[8])
+{
+    const u64 GX = pk2(s.ga.x, s.ga.y), GY = pk2(s.ga.z, s.ga.w), GZ = pk2(s.gb.x, s.gb.y);
+    const u64 NGX = pk2(s.gb.z, s.gb.w), NGY = pk2(s.gc.x, s.gc.y), NGZ = pk2(s.gc.z, s.gc.w);
+    const u64 CX = ffma2(dY, GZ, fmul2(dZ, NGY));
+    const u64 CY = ffma2(dZ, GX, fmul2(dX, NGZ));
+    const u64 CZ = ffma2(dX, GY, fmul2(dY, NGX));
+    u[0] = ffma2(G, CX, u[0]);
+    u[1] = ffma2(G, CY, u[1]);
+    u[2] = ffma2(G, CZ, u[2]);
+    w[0] = ffma2(G, GX, w[0]);
+    w[1] = ffma2(G, GY, w[1]);
+    w[2] = ffma2(G, GZ, w[2]);
+    const u64 BX = fmul2(Q, CX), BY = fmul2(Q, CY), BZ = fmul2(Q, CZ);
+    jq[0] = ffma2(BX, dX, jq[0]);
+    jq[1] = ffma2(BY, dX, jq[1]);
+    jq[2] = ffma2(BZ, dX, jq[2]);
+    jq[3] = ffma2(BX, dY, jq[3]);
+    jq[4] = ffma2(BY, dY, jq[4]);
+    jq[5] = ffma2(BZ, dY, jq[5]);
+    jq[6] = ffma2(BX, dZ, jq[6]);
+    jq[7] = ffma2(BY, dZ, jq[7]);
+}
+
+// Four sources (two packed pairs p0, p0 + 1) against this lane's target.
+template <int K>
+__device__ __forceinline__ void pair4_x2(u64 TX, u64 TY, u64 TZ, const float3& th, const float3& tl,
+                                         const PairX2* __restrict__ pr, const SrcMixed* __restrict__ tile, int p0,
+                                         u64 (&u)[3], u64 (&w)[3], u64 (&jq)[8])
+{
+    u64 dX[2], dY[2], dZ[2], R2[2];
+    bool far = true;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const float4 px = pr[p0 + h].px, pz = pr[p0 + h].pz;
+        dX[h] = fsub2(TX, pk2(px.x, px.y));
+        dY[h] = fsub2(TY, pk2(px.z, px.w));
+        dZ[h] = fsub2(TZ, pk2(pz.x, pz.y));
+        R2[h] = ffma2(dX[h], dX[h], ffma2(dY[h], dY[h], fmul2(dZ[h], dZ[h])));
+        float r0, r1;
+        upk2(R2[h], r0, r1);
+        far = far && r0 > pz.z && r1 > pz.w;
+    }
+    if (__all_sync(0xffffffffu, far)) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float r0, r1;
+            upk2(R2[h], r0, r1);
+            u64 G, Q;
+            if constexpr (singular_tail<K>()) {
+                const u64 RS = pk2(frsqrt(r0), frsqrt(r1));
+                const u64 RSS = fmul2(RS, RS);
+                G = fmul2(RS, RSS);
+                Q = fmul2(G, RSS);
+            } else {   // Winckelmans: the regular form at every distance
+                const float4 pz = pr[p0 + h].pz;
+                float g0, q0, g1, q1;
+                near_GQ<K>(r0 * pz.z, pz.z, g0, q0);
+                near_GQ<K>(r1 * pz.w, pz.w, g1, q1);
+                G = pk2(g0, g1);
+                Q = pk2(q0, q1);
+            }
+            accum_x2(dX[h], dY[h], dZ[h], G, Q, pr[p0 + h], u, w, jq);
+        }
+    } else {
+        // near group: double-float displacement and the full form, per source
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float ex[2], ey[2], ez[2], gg[2], qq[2];
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int j = 2 * (p0 + h) + e;
+                const float4 a = tile[j].a, b = tile[j].b;
+                ex[e] = (th.x - a.x) + (tl.x - b.x);
+                ey[e] = (th.y - a.y) + (tl.y - b.y);
+                ez[e] = (th.z - a.z) + (tl.z - b.z);
+                const float e2 = fmaf(ex[e], ex[e], fmaf(ey[e], ey[e], ez[e] * ez[e]));
+                float G, Q;
+                if constexpr (singular_tail<K>()) {
+                    const float isig2 = b.w * b.w;
+                    near_GQ<K>(e2 * isig2, isig2, G, Q);
+                    const float isig3 = isig2 * b.w;
+                    G *= isig3;
+                    Q *= isig3;
+                } else {
+                    const float i2 = e ? pr[p0 + h].pz.w : pr[p0 + h].pz.z;
+                    near_GQ<K>(e2 * i2, i2, G, Q);
+                }
+                const bool nz = e2 > 0.0f;
+                gg[e] = nz ? G : 0.0f;
+                qq[e] = nz ? Q : 0.0f;
+            }
+            accum_x2(pk2(ex[0], ex[1]), pk2(ey[0], ey[1]), pk2(ez[0], ez[1]), pk2(gg[0], gg[1]), pk2(qq[0], qq[1]),
+                     pr[p0 + h], u, w, jq);
+        }
+    }
+}
+
+#ifndef VPM_UJ_X2_MIN_BLOCKS
+#define VPM_UJ_X2_MIN_BLOCKS 5
+#endif
+
+template <int K>
+__global__ void __launch_bounds__(UJ_THREADS, VPM_UJ_X2_MIN_BLOCKS)
+uj_mixed_x2_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
+                   const SrcMixed* __restrict__ src, int64_t per_split, double* U, int64_t ldU,
+                   double* J, int64_t ldJ, double* partial, int64_t nt_pad)
+{
+    __shared__ SrcMixed stage[UJ_WARPS][2][WT];
+    __shared__ PairX2 prs[UJ_WARPS][2][WT / 2];
+    __shared__ double acc64[14][UJ_THREADS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
+    const bool valid = t < nt;
+    double tx = 3.0e4, ty = 3.0e4, tz = 3.0e4;
+    int32_t idx = 0;
+    if (valid) {
+        const TgtPos p = tgt[t];
+        tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
+    }
+    const float3 th = make_float3((float)tx, (float)ty, (float)tz);
+    const float3 tl = make_float3((float)(tx - (double)th.x), (float)(ty - (double)th.y), (float)(tz - (double)th.z));
+    const double ox = __shfl_sync(0xffffffffu, tx, 0);
+    const double oy = __shfl_sync(0xffffffffu, ty, 0);
+    const double oz = __shfl_sync(0xffffffffu, tz, 0);
+    const float3 oh = make_float3(__shfl_sync(0xffffffffu, th.x, 0), __shfl_sync(0xffffffffu, th.y, 0),
+                                  __shfl_sync(0xffffffffu, th.z, 0));
+    const float3 ol = make_float3(__shfl_sync(0xffffffffu, tl.x, 0), __shfl_sync(0xffffffffu, tl.y, 0),
+                                  __shfl_sync(0xffffffffu, tl.z, 0));
+    const float3 to = valid ? make_float3((float)(tx - ox), (float)(ty - oy), (float)(tz - oz))
+                            : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
+    float b2 = valid ? fmaf(to.x, to.x, fmaf(to.y, to.y, to.z * to.z)) : 0.0f;
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
+    const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
+    const float sfar = s_far<K>();
+    const u64 TX = pk2(to.x, to.x), TY = pk2(to.y, to.y), TZ = pk2(to.z, to.z);
+
+#pragma unroll
+    for (int k = 0; k < 14; k++) acc64[k][threadIdx.x] = 0.0;
+    float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) mj[k] = 0.f;
+    u64 u[3], w[3], jq[8];
+    const u64 Z0 = pk2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 3; k++) { u[k] = Z0; w[k] = Z0; }
+#pragma unroll
+    for (int k = 0; k < 8; k++) jq[k] = Z0;
+
+    const int64_t s0 = (int64_t)blockIdx.y * per_split;
+    const int64_t s1 = min(s0 + per_split, ns_pad);
+    const int ntiles = (int)((s1 - s0) / WT);
+    const SrcMixed* wsrc = src + s0 + lane;
+    if (ntiles > 0) {
+        SrcMixed* d = &stage[warp][0][lane];
+        cp_async16(&d->a, &wsrc->a);
+        cp_async16(&d->b, &wsrc->b);
+        cp_async16(&d->gam, &wsrc->gam);
+        cp_async_commit();
+    }
+    int in_block = 0, in_mid = 0;
+    for (int it = 0; it < ntiles; it++) {
+        const int buf = it & 1;
+        if (it + 1 < ntiles) {
+            const SrcMixed* g = wsrc + (int64_t)(it + 1) * WT;
+            SrcMixed* d = &stage[warp][buf ^ 1][lane];
+            cp_async16(&d->a, &g->a);
+            cp_async16(&d->b, &g->b);
+            cp_async16(&d->gam, &g->gam);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        {   // this lane's source into its half of the packed pair record
+            const float4 a = stage[warp][buf][lane].a, b = stage[warp][buf][lane].b, g = stage[warp][buf][lane].gam;
+            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : b.w * b.w;
+            const float px = (a.x - oh.x) + (b.x - ol.x), py = (a.y - oh.y) + (b.y - ol.y),
+                        pz = (a.z - oh.z) + (b.z - ol.z);
+            float* r = reinterpret_cast<float*>(&prs[warp][buf][lane >> 1]);
+            const int e = lane & 1;
+            r[0 + e] = px;  r[2 + e] = py;       // px
+            r[4 + e] = pz;  r[6 + e] = thr;      // pz
+            r[8 + e] = g.x; r[10 + e] = g.y;     // ga
+            r[12 + e] = g.z; r[14 + e] = -g.x;   // gb
+            r[16 + e] = -g.y; r[18 + e] = -g.z;  // gc
+        }
+        __syncwarp();
+#pragma unroll (UJ_UNROLL)
+        for (int p = 0; p < WT / 2; p += 2)
+            pair4_x2<K>(TX, TY, TZ, th, tl, prs[warp][buf], stage[warp][buf], p, u, w, jq);
+        if (++in_block == BLOCK_TILES) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                float a0, a1, b0, b1;
+                upk2(u[k], a0, a1);
+                upk2(w[k], b0, b1);
+                mu[k] += a0 + a1;
+                mw[k] += b0 + b1;
+                u[k] = Z0;
+                w[k] = Z0;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                float a0, a1;
+                upk2(jq[k], a0, a1);
+                mj[k] += a0 + a1;
+                jq[k] = Z0;
+            }
+            in_block = 0;
+            if (++in_mid == MID_BLOCKS) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    acc64[k][threadIdx.x] += (double)mu[k];
+                    acc64[3 + k][threadIdx.x] += (double)mw[k];
+                    mu[k] = 0.f;
+                    mw[k] = 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) { acc64[6 + k][threadIdx.x] += (double)mj[k]; mj[k] = 0.f; }
+                in_mid = 0;
+            }
+        }
+        __syncwarp();   // every lane is done with `buf` before it is refilled
+    }
+    double fU[3], fW[3], fJ[8];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float a0, a1, b0, b1;
+        upk2(u[k], a0, a1);
+        upk2(w[k], b0, b1);
+        fU[k] = acc64[k][threadIdx.x] + ((double)mu[k] + ((double)a0 + (double)a1));
+        fW[k] = acc64[3 + k][threadIdx.x] + ((double)mw[k] + ((double)b0 + (double)b1));
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        float a0, a1;
+        upk2(jq[k], a0, a1);
+        fJ[k] = acc64[6 + k][threadIdx.x] + ((double)mj[k] + ((double)a0 + (double)a1));
+    }
+    if (!valid) return;
+    double j9[9];
+#pragma unroll
+    for (int k = 0; k < 8; k++) j9[k] = -3.0 * fJ[k];
+    j9[8] = 3.0 * (fJ[0] + fJ[4]);
+    j9[1] -= fW[2];
+    j9[2] += fW[1];
+    j9[3] += fW[2];
+    j9[5] -= fW[0];
+    j9[6] -= fW[1];
+    j9[7] += fW[0];
+    double acc[12] = {fU[0], fU[1], fU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
+    write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
+}
+
 // --------------------------------------------------------------- launcher
 template <int K>
 static cudaError_t launch_uj_k(const UJArgs& a, const Workspace& w, int num_sms, cudaStream_t st,
@@ -415,8 +723,13 @@ static cudaError_t launch_uj_k(const UJArgs& a, const Workspace& w, int num_sms,
         SrcMixed* src = (SrcMixed*)w.src_pack;
         pack_src_mixed<K><<<(unsigned)((ns_pad + pb - 1) / pb), pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs,
                                                                              a.self ? tgt : nullptr, src);
+#if VPM_UJ_F32X2
+        uj_mixed_x2_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
+                                                            a.J, a.ldJ, partial, nt_pad);
+#else
         uj_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
                                                          a.J, a.ldJ, partial, nt_pad);
+#endif
     }
     *launches += 2;
     if (partial) {

@@ -339,6 +339,19 @@ __device__ __forceinline__ void near_GQ4(const float (&s)[4], const float (&isig
     }
 }
 
+// (a + b) - (oh + ol) for two double-floats (hi a / oh, lo b / ol) in FP32: the
+// difference of the high parts is made exact by TwoSum (s + e), the rest added
+// after, so the result is rounded once, nearly correctly.  The same operations
+// on the same inputs give the same bits: a point's offset from an origin
+// equals itself wherever it is formed (the self pair has r^2 == 0 exactly).
+__device__ __forceinline__ float df_offset(float a, float b, float oh, float ol)
+{
+    const float s = a - oh;
+    const float v = s - a;
+    const float e = (a - (s - v)) - (oh + v);
+    return s + (e + (b - ol));
+}
+
 // s += y, with the rounding error of the addition accumulated in c (Fast2Sum;
 // exact when |s| >= |y|, which a running sum of like terms keeps after its
 // first additions).  s + c is the compensated sum.
