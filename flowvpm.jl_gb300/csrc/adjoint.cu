@@ -16,7 +16,8 @@
 //
 // Layout: one target per thread (Morton order, as in uj.cu), sources staged in
 // shared memory.  Target-side sums stay in registers; each source's 7 sums
-// (x, Gamma, sigma) are reduced across the warp with shuffles, across the
+// (x, Gamma, sigma) are reduce-scattered across the warp with shuffles, four
+// sources at a time (adj_reduce4), summed across the
 // block's 4 warps in shared memory, then added to the outputs with one FP64
 // atomic per source and block (so the summation order of those sums is not
 // fixed).  Arithmetic is FP64 throughout.
@@ -58,8 +59,19 @@ __device__ __forceinline__ void g_d1_d2_f64(double rho, double& g, double& d1, d
     }
 }
 
+// r^2 past which kernel K has g = 1, g' = g'' = 0 to FP64 (g_d1_d2_f64's cuts), as a
+// multiple of sigma^2; 0 = never (the singular kernel takes that form at every r).
+template <int K>
+__host__ __device__ constexpr double adj_far_s()
+{
+    return K == K_GAUSERF ? 81.0 : K == K_GAUS ? 12.25 : 0.0;
+}
+
 // The 7 derivatives of phi for one pair: o[0..2] = dphi/d(dx), o[3..5] = dphi/dGamma,
-// o[6] = dphi/dsigma.  Pairs with r^2 == 0 give zeros.
+// o[6] = dphi/dsigma.  Pairs with r^2 == 0 give zeros.  Pairs past the kernel's cut
+// (s.gz_sig.y = adj_far_s sigma^2, from pack_src_adj) and every pair of the singular
+// kernel take A = -C4/r^3, B = 3 C4/r^5, B'/r = -15 C4/r^7, dA = dB = 0: the general
+// coefficients at g = 1, g' = g'' = 0.
 template <int K>
 __device__ __forceinline__ void adj_pair_f64(double dx, double dy, double dz, const SrcF64& s,
                                              const double (&Ub)[3], const double (&Jb)[9], const double (&wb)[3],
@@ -71,20 +83,27 @@ __device__ __forceinline__ void adj_pair_f64(double dx, double dy, double dz, co
         for (int k = 0; k < 7; k++) o[k] = 0.0;
         return;
     }
-    const double isig = s.z_isig.y, sig = s.gz_sig.y;
     const double rinv = rsqrt(r2);
-    const double r = r2 * rinv;
-    const double rho = r * isig;
-    double g, g1, g2;
-    g_d1_d2_f64<K>(rho, g, g1, g2);
-    const double ri2 = rinv * rinv, ri3 = ri2 * rinv, ri4 = ri2 * ri2, ri5 = ri4 * rinv;
-    const double A = -C4 * g * ri3;
-    const double B = -C4 * (g1 * isig * ri4 - 3.0 * g * ri5);
-    const double qpp = -C4 * (g2 * isig * isig * ri3 - 6.0 * g1 * isig * ri4 + 12.0 * g * ri5);
-    const double Bpr = (qpp - B) * ri2;
-    const double dA = C4 * g1 * rho * isig * ri3;
-    const double dB = -C4 * (2.0 * g1 - rho * g2) * isig * isig * ri4;
-    (void)sig;
+    const double ri2 = rinv * rinv, ri3 = ri2 * rinv;
+    double A, B, Bpr, dA = 0.0, dB = 0.0;
+    if (K == K_SING || (adj_far_s<K>() > 0.0 && r2 > s.gz_sig.y)) {
+        const double ri5 = ri3 * ri2;
+        A = -C4 * ri3;
+        B = (3.0 * C4) * ri5;
+        Bpr = (-15.0 * C4) * ri5 * ri2;
+    } else {
+        const double isig = s.z_isig.y;
+        const double rho = r2 * rinv * isig;
+        double g, g1, g2;
+        g_d1_d2_f64<K>(rho, g, g1, g2);
+        const double ri4 = ri2 * ri2, ri5 = ri4 * rinv;
+        A = -C4 * g * ri3;
+        B = -C4 * (g1 * isig * ri4 - 3.0 * g * ri5);
+        const double qpp = -C4 * (g2 * isig * isig * ri3 - 6.0 * g1 * isig * ri4 + 12.0 * g * ri5);
+        Bpr = (qpp - B) * ri2;
+        dA = C4 * g1 * rho * isig * ri3;
+        dB = -C4 * (2.0 * g1 - rho * g2) * isig * isig * ri4;
+    }
     const double Gx = s.gxy.x, Gy = s.gxy.y, Gz = s.gz_sig.x;
     const double cx = dy * Gz - dz * Gy, cy = dz * Gx - dx * Gz, cz = dx * Gy - dy * Gx;
     const double JDx = Jb[0] * dx + Jb[3] * dy + Jb[6] * dz;
@@ -103,6 +122,31 @@ __device__ __forceinline__ void adj_pair_f64(double dx, double dy, double dz, co
     o[4] = A * (Ub[2] * dx - Ub[0] * dz + wb[1]) + B * (JDz * dx - JDx * dz);
     o[5] = A * (Ub[0] * dy - Ub[1] * dx + wb[2]) + B * (JDx * dy - JDy * dx);
     o[6] = (K == K_SING) ? 0.0 : dA * P + dB * Q;
+}
+
+// Source-side sums of four pairs, reduce-scattered over the warp: v0..v3 are this lane's
+// 7 terms of sources 0..3.  Lanes exchange half of the sources 16 apart, then half of the rest
+// 8 apart, then add the remaining source's 7 terms across the 8 lanes left (42 FP64 adds
+// a lane for the four sources, against 140 for a full reduction of each).  On return
+// every lane of the 8-lane group of source q = 2 (lane/16 % 2) + (lane/8 % 2) holds its
+// 7 sums in w; q is returned.
+__device__ __forceinline__ int adj_reduce4(const double (&v0)[7], const double (&v1)[7], const double (&v2)[7],
+                                           const double (&v3)[7], int lane, double (&w)[7])
+{
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    double a[7], b[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) {   // sources {0, 2} -> lanes without / with bit 16; {1, 3} likewise
+        a[k] = (h16 ? v2[k] : v0[k]) + __shfl_xor_sync(0xffffffffu, h16 ? v0[k] : v2[k], 16);
+        b[k] = (h16 ? v3[k] : v1[k]) + __shfl_xor_sync(0xffffffffu, h16 ? v1[k] : v3[k], 16);
+    }
+#pragma unroll
+    for (int k = 0; k < 7; k++) w[k] = (h8 ? b[k] : a[k]) + __shfl_xor_sync(0xffffffffu, h8 ? a[k] : b[k], 8);
+#pragma unroll
+    for (int m = 4; m > 0; m >>= 1)
+#pragma unroll
+        for (int k = 0; k < 7; k++) w[k] += __shfl_xor_sync(0xffffffffu, w[k], m);
+    return (h16 ? 2 : 0) + (h8 ? 1 : 0);
 }
 
 template <int K>
@@ -139,22 +183,31 @@ uj_adjoint_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* 
         __syncthreads();
         tile[threadIdx.x] = src[base + threadIdx.x];
         __syncthreads();
-        for (int j = 0; j < UJ_TILE; j++) {
-            const SrcF64& s = tile[j];
-            double o[7];
-            adj_pair_f64<K>(tx - s.xy.x, ty - s.xy.y, tz - s.z_isig.x, s, Ub, Jb, wb, o);
-            acc[0] += o[0]; acc[1] += o[1]; acc[2] += o[2];
-            o[0] = -o[0]; o[1] = -o[1]; o[2] = -o[2];
-#pragma unroll
-            for (int k = 0; k < 7; k++) {
-                double v = o[k];
-#pragma unroll
-                for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-                o[k] = v;
+        for (int j = 0; j < UJ_TILE; j += 4) {
+            double o0[7], o1[7], o2[7], o3[7];
+            {
+                const SrcF64& s = tile[j];
+                adj_pair_f64<K>(tx - s.xy.x, ty - s.xy.y, tz - s.z_isig.x, s, Ub, Jb, wb, o0);
             }
-            if (lane == 0) {
+            {
+                const SrcF64& s = tile[j + 1];
+                adj_pair_f64<K>(tx - s.xy.x, ty - s.xy.y, tz - s.z_isig.x, s, Ub, Jb, wb, o1);
+            }
+            {
+                const SrcF64& s = tile[j + 2];
+                adj_pair_f64<K>(tx - s.xy.x, ty - s.xy.y, tz - s.z_isig.x, s, Ub, Jb, wb, o2);
+            }
+            {
+                const SrcF64& s = tile[j + 3];
+                adj_pair_f64<K>(tx - s.xy.x, ty - s.xy.y, tz - s.z_isig.x, s, Ub, Jb, wb, o3);
+            }
 #pragma unroll
-                for (int k = 0; k < 7; k++) red[warp][j][k] = o[k];
+            for (int k = 0; k < 3; k++) acc[k] += (o0[k] + o1[k]) + (o2[k] + o3[k]);
+            double w[7];
+            const int q = adj_reduce4(o0, o1, o2, o3, lane, w);
+            if ((lane & 7) == 0) {   // x_s gets -dphi/d(dx)
+#pragma unroll
+                for (int k = 0; k < 7; k++) red[warp][j + q][k] = k < 3 ? -w[k] : w[k];
             }
         }
         __syncthreads();
@@ -191,12 +244,13 @@ __global__ void pack_src_adj(int64_t ns, int64_t ns_pad, const double* __restric
         p.xy = make_double2(xs[3 * i], xs[3 * i + 1]);
         p.z_isig = make_double2(xs[3 * i + 2], 1.0 / sig);
         p.gxy = make_double2(gs[3 * i], gs[3 * i + 1]);
-        p.gz_sig = make_double2(gs[3 * i + 2], sig);
+        // .y: the r^2 of adj_pair_f64's cut
+        p.gz_sig = make_double2(gs[3 * i + 2], adj_far_s<K>() * sig * sig);
     } else {  // padding: far away, no strength
         p.xy = make_double2(1.0e6, 1.0e6);
         p.z_isig = make_double2(1.0e6, 1.0);
         p.gxy = make_double2(0.0, 0.0);
-        p.gz_sig = make_double2(0.0, 1.0);
+        p.gz_sig = make_double2(0.0, adj_far_s<K>());
     }
     out[i] = p;
 }

@@ -17,6 +17,7 @@
 // their reference term is zero; in the factored form their two terms would
 // only cancel to FP32 rounding, at the largest weight zeta(0)).
 #include "dyn_math.cuh"
+#include "estr_tiles.cuh"
 #include "internal.h"
 #include "vpm_math.cuh"
 
@@ -33,10 +34,14 @@ constexpr int ESTR_SUB = 8;
 
 static_assert(UJ_BLOCK % ESTR_SUB == 0, "whole sub-blocks");
 
+constexpr int EWT = EST_TILE;   // sources per tile of the mixed kernel's streams (one per lane)
+
 size_t estr_src_pack_bytes(int64_t ns, int precision)
 {
     const int64_t n = round_up(ns, UJ_TILE);
-    return (size_t)n * (precision ? sizeof(SrcEstrDF) : sizeof(SrcEstrF64));
+    // FP32-comp: the records, then two float4 per 32-source tile (estr_tile_boxes)
+    return precision ? (size_t)n * sizeof(SrcEstrDF) + (size_t)(n / EWT) * 2 * sizeof(float4)
+                     : (size_t)n * sizeof(SrcEstrF64);
 }
 
 // v = J^T Gamma (transposed) or J Gamma (classic); J column-major 3x3.
@@ -59,11 +64,12 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
                                 const double* __restrict__ gs, const double* __restrict__ sgs,
                                 const double* __restrict__ Js, int64_t ldJs,
                                 const uint8_t* __restrict__ static_s, bool transposed,
-                                const TgtPos* __restrict__ order, SrcEstrDF* __restrict__ out)
+                                const TgtPos* __restrict__ order, SrcEstrDF* __restrict__ out,
+                                float4* __restrict__ box)
 {
     // with `order` (sources = targets) the pack follows the targets' Morton order
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (o >= ns_pad) return;
+    if (o >= ns_pad) return;   // whole warps: ns_pad is a multiple of 32
     SrcEstrDF p;
     if (o < ns) {
         const int64_t i = order ? (int64_t)order[o].idx : o;
@@ -86,6 +92,7 @@ __global__ void pack_estr_mixed(int64_t ns, int64_t ns_pad, const double* __rest
         p.g = p.v = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     out[o] = p;
+    estr_tile_box(o, ns, p.a.x, p.a.y, p.a.z, p.a.w, box);
 }
 
 template <int K>
@@ -209,8 +216,7 @@ __device__ __forceinline__ void ecp_commit() { asm volatile("cp.async.commit_gro
 template <int N>
 __device__ __forceinline__ void ecp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-constexpr int EWT = 32;                  // sources per warp tile
-constexpr int ESTR_FLUSH_TILES = 8;      // warp tiles between FP64 adds (256 sources)
+constexpr int ESTR_FLUSH_TILES = 8;      // evaluated warp tiles between FP64 adds (256 sources)
 
 // The mixed Estr.  Each warp streams the sources on its own, 32 per tile,
 // double-buffered with cp.async (no block-wide barrier); the loading lane
@@ -219,12 +225,13 @@ constexpr int ESTR_FLUSH_TILES = 8;      // warp tiles between FP64 adds (256 so
 // own offset is formed by the same operations, so that the self pair and
 // coincident particles have
 // r^2 == 0 exactly (they are skipped: their terms would only cancel to FP32
-// rounding, at the largest weight).  For the Gaussian kernels a whole tile is
-// skipped when every one of its sources is past zeta_skip_s from the warp's
-// target box (zeta/zeta(0) < 1e-13 for every pair: their terms are below the
-// FP32 resolution of the sums), and then an 8-source sub-block when every pair
-// of the warp is.  Sums: 8-source FP32 partials added with compensation
-// (comp_add), FP64 every ESTR_FLUSH_TILES tiles.
+// rounding, at the largest weight).  For the Gaussian kernels the terms past
+// zeta_skip_s (zeta/zeta(0) < 1e-13: below the FP32 resolution of the sums) are
+// skipped at three levels: a tile whose pack box is out of reach of the warp's
+// targets is not loaded (TileWalk); a loaded tile is skipped when every one of its
+// sources is out of reach of the warp's target box; an 8-source sub-block when
+// every pair of the warp is.  Sums: 8-source FP32 partials added with
+// compensation (comp_add), FP64 every ESTR_FLUSH_TILES evaluated tiles.
 // With DZ (the weight difference of the dynamic procedure's test filter,
 // dynamic.cu) each weight zeta~(r, sigma_s) is replaced by
 // zeta~(r, alpha sigma_s) - zeta~(r, sigma_s) = zeta~(r, sigma_s) (ratio - 1),
@@ -233,8 +240,8 @@ template <int K, bool ZETA, bool DZ = false>
 __global__ void __launch_bounds__(UJ_THREADS)
 estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __restrict__ Jt, int64_t ldJt,
                   const uint8_t* __restrict__ static_t, int64_t ns_pad, const SrcEstrDF* __restrict__ src,
-                  int64_t per_split, bool self, bool transposed, double* SFS, int64_t ldS, double* partial,
-                  int64_t nt_pad, float3 fd = make_float3(0.f, 0.f, 0.f))
+                  const float4* __restrict__ box, int64_t per_split, bool self, bool transposed, double* SFS,
+                  int64_t ldS, double* partial, int64_t nt_pad, float3 fd = make_float3(0.f, 0.f, 0.f))
 {
     __shared__ SrcEstrDF stage[UJ_WARPS][2][EWT];
     __shared__ float4 offs[UJ_WARPS][2][EWT];
@@ -262,32 +269,53 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
         to = make_float3(df_offset(th.x, tl.x, oh.x, ol.x), df_offset(th.y, tl.y, oh.y, ol.y),
                          df_offset(th.z, tl.z, oh.z, ol.z));
     }
-    // the warp's target box (offsets), for the tile skip
-    float bmin[3] = {to.x, to.y, to.z}, bmax[3] = {to.x, to.y, to.z};
-#pragma unroll
-    for (int m = 16; m > 0; m >>= 1)
+    // the warp's target boxes: offsets (for the per-source test of a tile) and FP32
+    // positions of its targets (for the tile boxes of the pack); [0], [1] = offsets low,
+    // high; [2], [3] = positions low, high (empty without a target)
+    __shared__ float4 wbox[UJ_WARPS][4];
+    {
+        float v[12] = {to.x, to.y, to.z, -to.x, -to.y, -to.z};
+        const bool real = t < nt;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            bmin[k] = fminf(bmin[k], __shfl_xor_sync(0xffffffffu, bmin[k], m));
-            bmax[k] = fmaxf(bmax[k], __shfl_xor_sync(0xffffffffu, bmax[k], m));
+            const float h = (float)(k == 0 ? tx : k == 1 ? ty : tz);
+            v[6 + k] = real ? h : 3.0e38f;
+            v[9 + k] = real ? -h : 3.0e38f;
         }
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1)
+#pragma unroll
+            for (int k = 0; k < 12; k++) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], m));
+        if (lane == 0) {
+            wbox[warp][0] = make_float4(v[0], v[1], v[2], 0.f);
+            wbox[warp][1] = make_float4(-v[3], -v[4], -v[5], 0.f);
+            wbox[warp][2] = make_float4(v[6], v[7], v[8], 0.f);
+            wbox[warp][3] = make_float4(-v[9], -v[10], -v[11], 0.f);
+        }
+        __syncwarp();
+    }
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
     float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
     const int ntiles = (int)((s1 - s0) / EWT);
     const SrcEstrDF* wsrc = src + s0 + lane;
-    if (ntiles > 0) {
+    // the split's tiles within reach of the warp's targets, 32 tiles per ballot
+    TileWalk walk;
+    walk.init(ntiles);
+    int cur = walk.next<K>(box + 2 * (s0 / EWT), wbox[warp][2], wbox[warp][3], lane);
+    if (cur >= 0) {
         SrcEstrDF* d = &stage[warp][0][lane];
-        ecp_async16(&d->a, &wsrc->a); ecp_async16(&d->b, &wsrc->b);
-        ecp_async16(&d->g, &wsrc->g); ecp_async16(&d->v, &wsrc->v);
+        const SrcEstrDF* gp = wsrc + (int64_t)cur * EWT;
+        ecp_async16(&d->a, &gp->a); ecp_async16(&d->b, &gp->b);
+        ecp_async16(&d->g, &gp->g); ecp_async16(&d->v, &gp->v);
         ecp_commit();
     }
-    int in_flush = 0;
-    for (int it = 0; it < ntiles; it++) {
-        const int buf = it & 1;
-        if (it + 1 < ntiles) {
-            const SrcEstrDF* gp = wsrc + (int64_t)(it + 1) * EWT;
+    int in_flush = 0, buf = 0;
+    while (cur >= 0) {
+        const int nxt = walk.next<K>(box + 2 * (s0 / EWT), wbox[warp][2], wbox[warp][3], lane);
+        if (nxt >= 0) {
+            const SrcEstrDF* gp = wsrc + (int64_t)nxt * EWT;
             SrcEstrDF* d = &stage[warp][buf ^ 1][lane];
             ecp_async16(&d->a, &gp->a); ecp_async16(&d->b, &gp->b);
             ecp_async16(&d->g, &gp->g); ecp_async16(&d->v, &gp->v);
@@ -303,9 +331,10 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
             const float px = df_offset(a.x, b.x, oh.x, ol.x), py = df_offset(a.y, b.y, oh.y, ol.y),
                         pz = df_offset(a.z, b.z, oh.z, ol.z);
             offs[warp][buf][lane] = make_float4(px, py, pz, a.w);
-            const float ex = fmaxf(fmaxf(bmin[0] - px, px - bmax[0]), 0.0f);
-            const float ey = fmaxf(fmaxf(bmin[1] - py, py - bmax[1]), 0.0f);
-            const float ez = fmaxf(fmaxf(bmin[2] - pz, pz - bmax[2]), 0.0f);
+            const float4 lo = wbox[warp][0], hi = wbox[warp][1];
+            const float ex = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.0f);
+            const float ey = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.0f);
+            const float ez = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.0f);
             beyond = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) * a.w > zeta_skip_s<K>();
         }
         __syncwarp();
@@ -347,20 +376,23 @@ estr_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double* __re
                     if constexpr (!ZETA) comp_add(sv[k], cv[k], fv[k]);
                 }
             }
-        }
-        if (++in_flush == ESTR_FLUSH_TILES) {
-            in_flush = 0;
+            // skipped tiles add nothing, so only the tiles taken count towards a flush
+            if (++in_flush == ESTR_FLUSH_TILES) {
+                in_flush = 0;
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                zg[k] += (double)sg[k] + (double)cg[k];
-                sg[k] = cg[k] = 0.f;
-                if constexpr (!ZETA) {
-                    zv[k] += (double)sv[k] + (double)cv[k];
-                    sv[k] = cv[k] = 0.f;
+                for (int k = 0; k < 3; k++) {
+                    zg[k] += (double)sg[k] + (double)cg[k];
+                    sg[k] = cg[k] = 0.f;
+                    if constexpr (!ZETA) {
+                        zv[k] += (double)sv[k] + (double)cv[k];
+                        sv[k] = cv[k] = 0.f;
+                    }
                 }
             }
         }
         __syncwarp();   // every lane is done with `buf` before it is refilled
+        cur = nxt;
+        buf ^= 1;
     }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -407,23 +439,24 @@ static cudaError_t launch_estr_k(const EstrArgs& a, const Workspace& w, int num_
                                                                    partial, nt_pad);
     } else {
         SrcEstrDF* src = (SrcEstrDF*)w.src_pack;
+        float4* box = (float4*)(src + ns_pad);   // the tile boxes follow the records
         pack_estr_mixed<K><<<pgrid, pb, 0, st>>>(a.ns, ns_pad, a.xs, a.gs, a.sgs, a.zeta ? nullptr : a.Js, a.ldJs,
-                                                  static_s, a.transposed, a.self ? tgt : nullptr, src);
+                                                  static_s, a.transposed, a.self ? tgt : nullptr, src, box);
         if (a.zeta)
             estr_mixed_kernel<K, true><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
-                                                                    per_split, a.self, a.transposed, a.SFS, a.ldS,
-                                                                    partial, nt_pad);
+                                                                    box, per_split, a.self, a.transposed, a.SFS,
+                                                                    a.ldS, partial, nt_pad);
         else if (a.dz_alpha > 0.0) {
             const double al = a.dz_alpha;
             const float3 fd = make_float3((float)(1.0 / (al * al * al) - 1.0), (float)(1.0 / (al * al * al)),
                                           (float)(1.0 / (al * al) - 1.0));
             estr_mixed_kernel<K, false, true><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad,
-                                                                           src, per_split, a.self, a.transposed,
+                                                                           src, box, per_split, a.self, a.transposed,
                                                                            a.SFS, a.ldS, partial, nt_pad, fd);
         } else
             estr_mixed_kernel<K, false><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, a.Jt, a.ldJt, static_t, ns_pad, src,
-                                                                     per_split, a.self, a.transposed, a.SFS, a.ldS,
-                                                                     partial, nt_pad);
+                                                                     box, per_split, a.self, a.transposed, a.SFS,
+                                                                     a.ldS, partial, nt_pad);
     }
     *launches += 2;
     if (partial) {

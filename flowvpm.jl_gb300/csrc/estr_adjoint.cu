@@ -33,6 +33,7 @@
 // double-float origin, tile and sub-block skips past the kernel's reach,
 // compensated 8-pair sub-sums, FP64 across tiles) and skips pairs at r = 0, as
 // that forward does.
+#include "estr_tiles.cuh"
 #include "internal.h"
 #include "vpm_math.cuh"
 
@@ -93,7 +94,7 @@ template <int K>
 __global__ void ea_pack(int64_t n, int64_t n_pad, const TgtPos* __restrict__ order, const double* __restrict__ x,
                         const double* __restrict__ gam, const double* __restrict__ sig, const double* __restrict__ J,
                         const uint8_t* __restrict__ st, const double* __restrict__ Sbar, bool transposed, bool mixed,
-                        void* __restrict__ p1, void* __restrict__ p2)
+                        void* __restrict__ p1, void* __restrict__ p2, float4* __restrict__ box)
 {
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= n_pad) return;
@@ -132,6 +133,7 @@ __global__ void ea_pack(int64_t n, int64_t n_pad, const TgtPos* __restrict__ ord
         s2.sb = make_float4((float)sb[0], (float)sb[1], (float)sb[2], 0.f);
         ((EA1Mx*)p1)[o] = s1;
         ((EA2Mx*)p2)[o] = s2;
+        estr_tile_box(o, n, xh, yh, zh, s1.a.w, box);   // whole warps (n_pad is a multiple of 32)
     }
 }
 
@@ -220,7 +222,7 @@ ea2_f64(int64_t n, const EA1F64* __restrict__ self, int64_t n_pad, const EA2F64*
 // is skipped when every pair of it is past zeta_skip_s from the warp's box
 // (pass 1 with each source's own sigma; pass 2 with the warp's smallest lane
 // sigma), then an 8-pair sub-block when every pair of the warp is.  Sums:
-// 8-pair FP32 partials added with compensation, FP64 every 8 tiles.
+// 8-pair FP32 partials added with compensation, FP64 every 8 evaluated tiles.
 __device__ __forceinline__ void ea_cp16(void* smem, const void* gmem)
 {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -266,6 +268,21 @@ struct EaFrame {
                 bmax[k] = fmaxf(bmax[k], __shfl_xor_sync(0xffffffffu, bmax[k], m));
             }
     }
+    // the FP32 box of the warp's valid particles (high parts) to wb[0] (low), wb[1] (high)
+    __device__ __forceinline__ static void abs_box(const float4& h, bool valid, float4* wb)
+    {
+        float v[6] = {valid ? h.x : 3.0e38f, valid ? h.y : 3.0e38f, valid ? h.z : 3.0e38f,
+                      valid ? -h.x : 3.0e38f, valid ? -h.y : 3.0e38f, valid ? -h.z : 3.0e38f};
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1)
+#pragma unroll
+            for (int k = 0; k < 6; k++) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], m));
+        if ((threadIdx.x & 31) == 0) {
+            wb[0] = make_float4(v[0], v[1], v[2], 0.f);
+            wb[1] = make_float4(-v[3], -v[4], -v[5], 0.f);
+        }
+        __syncwarp();
+    }
     __device__ __forceinline__ float3 offset(const float4& h, const float4& l) const
     {
         return make_float3(df_offset(h.x, l.x, oh.x, ol.x), df_offset(h.y, l.y, oh.y, ol.y),
@@ -284,15 +301,17 @@ struct EaFrame {
 template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
 ea1_mx(int64_t n, const TgtPos* __restrict__ tgt, const EA2Mx* __restrict__ self, int64_t n_pad,
-       const EA1Mx* __restrict__ src, int64_t per_split, double* __restrict__ partial)
+       const EA1Mx* __restrict__ src, const float4* __restrict__ box, int64_t per_split, double* __restrict__ partial)
 {
     __shared__ EA1Mx stage[UJ_WARPS][2][EA_WT];
     __shared__ float4 offs[UJ_WARPS][2][EA_WT];
+    __shared__ float4 wbox[UJ_WARPS][2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const EA2Mx me = self[t < n ? t : n_pad - 1];
     EaFrame fr;
     fr.init(me.h, me.l, t < n);
+    EaFrame::abs_box(me.h, t < n, wbox[warp]);
     double acc[NACC1] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     float sm[NACC1], cm[NACC1];
 #pragma unroll
@@ -300,12 +319,16 @@ ea1_mx(int64_t n, const TgtPos* __restrict__ tgt, const EA2Mx* __restrict__ self
     const int64_t s0 = (int64_t)blockIdx.y * per_split, s1 = min(s0 + per_split, n_pad);
     const int ntiles = (int)((s1 - s0) / EA_WT);
     const EA1Mx* wsrc = src + s0 + lane;
-    if (ntiles > 0) ea_stage(&stage[warp][0][lane], wsrc);
-    int in_flush = 0;
-    for (int it = 0; it < ntiles; it++) {
-        const int buf = it & 1;
-        if (it + 1 < ntiles) {
-            ea_stage(&stage[warp][buf ^ 1][lane], wsrc + (int64_t)(it + 1) * EA_WT);
+    const float4* tbox = box + 2 * (s0 / EA_WT);
+    TileWalk walk;
+    walk.init(ntiles);
+    int cur = walk.next<K>(tbox, wbox[warp][0], wbox[warp][1], lane);
+    if (cur >= 0) ea_stage(&stage[warp][0][lane], wsrc + (int64_t)cur * EA_WT);
+    int in_flush = 0, buf = 0;
+    while (cur >= 0) {
+        const int nxt = walk.next<K>(tbox, wbox[warp][0], wbox[warp][1], lane);
+        if (nxt >= 0) {
+            ea_stage(&stage[warp][buf ^ 1][lane], wsrc + (int64_t)nxt * EA_WT);
             ea_wait<1>();
         } else {
             ea_wait<0>();
@@ -351,13 +374,15 @@ ea1_mx(int64_t n, const TgtPos* __restrict__ tgt, const EA2Mx* __restrict__ self
 #pragma unroll
                 for (int k = 0; k < NACC1; k++) comp_add(sm[k], cm[k], f[k]);
             }
-        }
-        if (++in_flush == EA_FLUSH) {
-            in_flush = 0;
+            if (++in_flush == EA_FLUSH) {     // evaluated tiles only
+                in_flush = 0;
 #pragma unroll
-            for (int k = 0; k < NACC1; k++) { acc[k] += (double)sm[k] + (double)cm[k]; sm[k] = cm[k] = 0.f; }
+                for (int k = 0; k < NACC1; k++) { acc[k] += (double)sm[k] + (double)cm[k]; sm[k] = cm[k] = 0.f; }
+            }
         }
         __syncwarp();   // every lane is done with `buf` before it is refilled
+        cur = nxt;
+        buf ^= 1;
     }
 #pragma unroll
     for (int k = 0; k < NACC1; k++) acc[k] += (double)sm[k] + (double)cm[k];
@@ -369,10 +394,11 @@ template <int K>
 __global__ void __launch_bounds__(UJ_THREADS)
 ea2_mx(int64_t n, const EA1Mx* __restrict__ self, const double* __restrict__ gam, const TgtPos* __restrict__ tgt,
        const double* __restrict__ J, const uint8_t* __restrict__ st, bool transposed, int64_t n_pad,
-       const EA2Mx* __restrict__ src, int64_t per_split, double* __restrict__ partial)
+       const EA2Mx* __restrict__ src, const float4* __restrict__ box, int64_t per_split, double* __restrict__ partial)
 {
     __shared__ EA2Mx stage[UJ_WARPS][2][EA_WT];
     __shared__ float4 offs[UJ_WARPS][2][EA_WT];
+    __shared__ float4 wbox[UJ_WARPS][2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t s = (int64_t)blockIdx.x * UJ_THREADS + threadIdx.x;
     const EA1Mx me = self[s < n ? s : n_pad - 1];
@@ -390,6 +416,7 @@ ea2_mx(int64_t n, const EA1Mx* __restrict__ self, const double* __restrict__ gam
     }
     EaFrame fr;
     fr.init(me.a, me.b, s < n);
+    EaFrame::abs_box(me.a, s < n, wbox[warp]);
     const float isig2 = me.a.w;
     float i2min = s < n ? isig2 : 3.0e38f;
 #pragma unroll
@@ -401,12 +428,16 @@ ea2_mx(int64_t n, const EA1Mx* __restrict__ self, const double* __restrict__ gam
     const int64_t s0 = (int64_t)blockIdx.y * per_split, s1 = min(s0 + per_split, n_pad);
     const int ntiles = (int)((s1 - s0) / EA_WT);
     const EA2Mx* wsrc = src + s0 + lane;
-    if (ntiles > 0) ea_stage(&stage[warp][0][lane], wsrc);
-    int in_flush = 0;
-    for (int it = 0; it < ntiles; it++) {
-        const int buf = it & 1;
-        if (it + 1 < ntiles) {
-            ea_stage(&stage[warp][buf ^ 1][lane], wsrc + (int64_t)(it + 1) * EA_WT);
+    const float4* tbox = box + 2 * (s0 / EA_WT);
+    TileWalk walk;   // target tiles, tested at the lanes' largest sigma
+    walk.init(ntiles);
+    int cur = walk.next<K>(tbox, wbox[warp][0], wbox[warp][1], lane, i2min);
+    if (cur >= 0) ea_stage(&stage[warp][0][lane], wsrc + (int64_t)cur * EA_WT);
+    int in_flush = 0, buf = 0;
+    while (cur >= 0) {
+        const int nxt = walk.next<K>(tbox, wbox[warp][0], wbox[warp][1], lane, i2min);
+        if (nxt >= 0) {
+            ea_stage(&stage[warp][buf ^ 1][lane], wsrc + (int64_t)nxt * EA_WT);
             ea_wait<1>();
         } else {
             ea_wait<0>();
@@ -457,13 +488,15 @@ ea2_mx(int64_t n, const EA1Mx* __restrict__ self, const double* __restrict__ gam
 #pragma unroll
                 for (int k = 0; k < NACC2; k++) comp_add(sm[k], cm[k], f[k]);
             }
-        }
-        if (++in_flush == EA_FLUSH) {
-            in_flush = 0;
+            if (++in_flush == EA_FLUSH) {     // evaluated tiles only
+                in_flush = 0;
 #pragma unroll
-            for (int k = 0; k < NACC2; k++) { acc[k] += (double)sm[k] + (double)cm[k]; sm[k] = cm[k] = 0.f; }
+                for (int k = 0; k < NACC2; k++) { acc[k] += (double)sm[k] + (double)cm[k]; sm[k] = cm[k] = 0.f; }
+            }
         }
         __syncwarp();
+        cur = nxt;
+        buf ^= 1;
     }
 #pragma unroll
     for (int k = 0; k < NACC2; k++) acc[k] += (double)sm[k] + (double)cm[k];
@@ -544,8 +577,10 @@ cudaError_t launch_k(const EstrAdjArgs& a, const EstrAdjWork& w, int num_sms, cu
     cudaError_t e = order_targets(n, a.x, w.order, w.order_bytes, st, launches, &tgt);
     if (e != cudaSuccess) return e;
     const bool mixed = a.precision != 0;
+    // FP32-comp: the tile boxes follow pack 1's 64-byte records (within its 80-byte slots)
+    float4* box = (float4*)((EA1Mx*)w.pack1 + n_pad);
     ea_pack<K><<<pg, pb, 0, st>>>(n, n_pad, tgt, a.x, a.gam, a.sig, a.J, a.static_flags, a.Sbar, a.transposed, mixed,
-                                  w.pack1, w.pack2);
+                                  w.pack1, w.pack2, box);
     if (!mixed) {
         ea1_f64<K><<<grid, UJ_THREADS, 0, st>>>(n, tgt, (const EA2F64*)w.pack2, n_pad, (const EA1F64*)w.pack1,
                                                 per_split, w.partial);
@@ -554,12 +589,13 @@ cudaError_t launch_k(const EstrAdjArgs& a, const EstrAdjWork& w, int num_sms, cu
         ea2_f64<K><<<grid, UJ_THREADS, 0, st>>>(n, (const EA1F64*)w.pack1, n_pad, (const EA2F64*)w.pack2, per_split,
                                                 w.partial);
     } else {
-        ea1_mx<K><<<grid, UJ_THREADS, 0, st>>>(n, tgt, (const EA2Mx*)w.pack2, n_pad, (const EA1Mx*)w.pack1,
+        ea1_mx<K><<<grid, UJ_THREADS, 0, st>>>(n, tgt, (const EA2Mx*)w.pack2, n_pad, (const EA1Mx*)w.pack1, box,
                                                per_split, w.partial);
         ea1_epilogue<<<eg, pb, 0, st>>>(n, nsplit, w.partial, n_pad, tgt, a.static_flags, a.Sbar, a.transposed,
                                         a.xbar, a.Jbar);
         ea2_mx<K><<<grid, UJ_THREADS, 0, st>>>(n, (const EA1Mx*)w.pack1, a.gam, tgt, a.J, a.static_flags,
-                                               a.transposed, n_pad, (const EA2Mx*)w.pack2, per_split, w.partial);
+                                               a.transposed, n_pad, (const EA2Mx*)w.pack2, box, per_split,
+                                               w.partial);
     }
     ea2_epilogue<K><<<eg, pb, 0, st>>>(n, nsplit, w.partial, n_pad, tgt, a.static_flags, a.gam, a.sig, a.J,
                                        a.transposed, mixed, a.xbar, a.gbar, a.sbar, a.Jbar);
@@ -573,7 +609,9 @@ EstrAdjSizes estr_adjoint_sizes(int64_t n, int num_sms)
 {
     const int64_t n_pad = round_up(n, UJ_TILE);
     EstrAdjSizes z;
-    z.pack = (size_t)n_pad * 80;   // the larger of the FP64 (80 B) and mixed (64 B) records
+    // the larger of the FP64 (80 B) and mixed (64 B) records; pack 1's mixed tile boxes
+    // (1 B a particle) fit in the difference
+    z.pack = (size_t)n_pad * 80;
     z.partial = (size_t)uj_num_splits(n, n, num_sms) * NACC2 * (size_t)n_pad * sizeof(double);
     return z;
 }

@@ -100,7 +100,8 @@ __global__ void leaf_pack_f64(int64_t n, const double* __restrict__ x, const dou
     p.xy = make_double2(x[3 * i], x[3 * i + 1]);
     p.z_isig = make_double2(x[3 * i + 2], 1.0 / sig);
     p.gxy = make_double2(gs[3 * i], gs[3 * i + 1]);
-    p.gz_sig = make_double2(gs[3 * i + 2], sig);
+    // .y: for Gaussian-erf the r^2 past which g = 1, g' = 0 (pair_f64_acc), else sigma
+    p.gz_sig = make_double2(gs[3 * i + 2], K == K_GAUSERF ? 81.0 * sig * sig : sig);
     out[o] = p;
 }
 
@@ -805,30 +806,7 @@ nf_filter_diff(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const
 }
 
 // --------------------------------------------------------------------- UJ, FP64
-template <int K>
-__device__ __forceinline__ void leaf_pair_f64(double tx, double ty, double tz, const SrcF64& s, double (&acc)[12])
-{
-    const double dx = tx - s.xy.x, dy = ty - s.xy.y, dz = tz - s.z_isig.x;
-    const double r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 != 0.0) {
-        const double rinv = rsqrt(r2);
-        const double isig = s.z_isig.y;
-        double g, dg;
-        g_dgdr_f64<K>(r2 * rinv * isig, g, dg);
-        const double r3inv = rinv * rinv * rinv;
-        const double gx = s.gxy.x, gy = s.gxy.y, gz = s.gz_sig.x;
-        const double k = -C4 * r3inv;
-        const double c1 = k * (dy * gz - dz * gy), c2 = k * (dz * gx - dx * gz), c3 = k * (dx * gy - dy * gx);
-        acc[0] += g * c1; acc[1] += g * c2; acc[2] += g * c3;
-        const double aux = dg * isig * rinv - 3.0 * g * rinv * rinv;
-        const double aux2 = -C4 * g * r3inv;
-        const double a1 = aux * c1, a2 = aux * c2, a3 = aux * c3;
-        acc[3] += a1 * dx; acc[4] += a2 * dx - aux2 * gz; acc[5] += a3 * dx + aux2 * gy;
-        acc[6] += a1 * dy + aux2 * gz; acc[7] += a2 * dy; acc[8] += a3 * dy - aux2 * gx;
-        acc[9] += a1 * dz - aux2 * gy; acc[10] += a2 * dz + aux2 * gx; acc[11] += a3 * dz;
-    }
-}
-
+// pair_f64_acc (uj_pair.cuh) over the group's intervals, for the targets of each source's mask.
 template <int K>
 __global__ void __launch_bounds__(NF_THREADS)
 nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
@@ -841,9 +819,9 @@ nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int3
     const int64_t grp = (int64_t)blockIdx.x * NF_WARPS + warp;
     if (grp >= ngroups) return;
     const GroupTarget me = group_target(n, 32 * grp, lane, tgt, leaf_of);
-    double acc[12];
+    double u[3] = {0.0, 0.0, 0.0}, w[3] = {0.0, 0.0, 0.0}, jq[9];
 #pragma unroll
-    for (int k = 0; k < 12; k++) acc[k] = 0.0;
+    for (int k = 0; k < 9; k++) jq[k] = 0.0;
     IntervalWalk walk;
     walk.init(ivs, grp_row[grp], grp_row[grp + 1], lane);
     for (;;) {
@@ -856,9 +834,11 @@ nf_uj_f64(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int3
         tmask[warp][lane] = smask;
         __syncwarp();
         for (int j = 0; j < cnt; j++)
-            if (tmask[warp][j] & me.bit) leaf_pair_f64<K>(me.tx, me.ty, me.tz, tile[warp][j], acc);
+            if (tmask[warp][j] & me.bit) pair_f64_acc<K>(me.tx, me.ty, me.tz, tile[warp][j], u, w, jq);
     }
     if (!me.valid) return;
+    double acc[12];
+    uj_f64_finish(u, w, jq, acc);
 #pragma unroll
     for (int k = 0; k < 3; k++) U[3 * (int64_t)me.idx + k] += acc[k];
 #pragma unroll

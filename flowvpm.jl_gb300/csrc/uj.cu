@@ -109,7 +109,8 @@ __global__ void pack_src_f64(int64_t ns, int64_t ns_pad, const double* __restric
         p.xy = make_double2(xs[3 * i], xs[3 * i + 1]);
         p.z_isig = make_double2(xs[3 * i + 2], 1.0 / sig);
         p.gxy = make_double2(gs[3 * i], gs[3 * i + 1]);
-        p.gz_sig = make_double2(gs[3 * i + 2], sig);
+        // .y: for Gaussian-erf the r^2 past which g = 1, g' = 0 (rho > 9), else sigma
+        p.gz_sig = make_double2(gs[3 * i + 2], K == K_GAUSERF ? 81.0 * sig * sig : sig);
     } else {
         p.xy = make_double2(0.0, 0.0);
         p.z_isig = make_double2(0.0, 1.0);
@@ -157,6 +158,13 @@ __device__ __forceinline__ void pair_f64(double tx, double ty, double tz, const 
         acc[11] += a3 * dz;
     }
 }
+
+#ifndef VPM_UJ_F64_ACC
+// 1: the FP64 pair in the accumulated form (pair_f64_acc, uj_pair.cuh), measured 1.44x
+// faster than 0, the reference's per-pair form (pair_f64: 62 FP64 instructions a pair),
+// on 2^15 x 2^20 Gaussian-erf pairs
+#define VPM_UJ_F64_ACC 1
+#endif
 
 // --------------------------------------------------------------- epilogue
 __device__ __forceinline__ void write_uj(int64_t t, int32_t idx, const double (&acc)[12], double* U,
@@ -206,8 +214,14 @@ uj_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad, const 
         tx = p.x; ty = p.y; tz = p.z; idx = p.idx;
     }
     double acc[12];
+#if VPM_UJ_F64_ACC
+    double u[3] = {0.0, 0.0, 0.0}, w[3] = {0.0, 0.0, 0.0}, jq[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) jq[k] = 0.0;
+#else
 #pragma unroll
     for (int k = 0; k < 12; k++) acc[k] = 0.0;
+#endif
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
     for (int64_t base = s0; base < s1; base += UJ_TILE) {
@@ -215,8 +229,17 @@ uj_f64_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad, const 
         tile[threadIdx.x] = src[base + threadIdx.x];
         __syncthreads();
 #pragma unroll 2
-        for (int j = 0; j < UJ_TILE; j++) pair_f64<K>(tx, ty, tz, tile[j], acc);
+        for (int j = 0; j < UJ_TILE; j++) {
+#if VPM_UJ_F64_ACC
+            pair_f64_acc<K>(tx, ty, tz, tile[j], u, w, jq);
+#else
+            pair_f64<K>(tx, ty, tz, tile[j], acc);
+#endif
+        }
     }
+#if VPM_UJ_F64_ACC
+    uj_f64_finish(u, w, jq, acc);
+#endif
     if (valid) write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
 
@@ -236,7 +259,9 @@ constexpr int BLOCK_TILES = UJ_BLOCK / WT;  // warp tiles per FP32 block
 // slower -- the FP64 pipe runs at 1/64 rate -- with the same U, J error against the oracle)
 constexpr int MID_BLOCKS = 16;
 #ifndef VPM_UJ_MIN_BLOCKS
-#define VPM_UJ_MIN_BLOCKS 7                 // resident blocks per SM the register budget targets (72 registers)
+// resident blocks per SM the register budget targets: 6 (80 registers) measured 0.9 % faster
+// than 7 (72 registers, a few spills) at N = 2^20 with the per-tile far flags
+#define VPM_UJ_MIN_BLOCKS 6
 #endif
 #ifndef VPM_UJ_UNROLL
 #define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
@@ -249,6 +274,13 @@ constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
 // 1: the FP64 sums (touched once per 1,024 sources) live in shared memory, which frees the
 // registers for 7 resident blocks per SM instead of 5 -- measured 3.6 % faster at N = 2^20
 #define VPM_UJ_SMEM_ACC 1
+#endif
+#ifndef VPM_UJ_TILE_FLAGS
+// 1: far/near decided once per tile from the warp's target box: the loading lane flags its
+// source far when the box is out of the source's reach, one ballot gives the tile's flags,
+// a tile of far sources runs the far form with no test, other tiles choose per 4-source
+// group.  0: every pair tested, one vote per 4-source group (pair4_mixed).
+#define VPM_UJ_TILE_FLAGS 1
 #endif
 
 // Each warp streams the sources on its own: 32 per tile, double-buffered with
@@ -288,6 +320,27 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
     const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
     const float sfar = s_far<K>();
+#if VPM_UJ_TILE_FLAGS
+    // the box of the warp's valid targets (offsets; empty when it has none), read by the
+    // loading lanes
+    __shared__ float4 wbox[UJ_WARPS][2];
+    {
+        float lo[3] = {valid ? to.x : 3.0e38f, valid ? to.y : 3.0e38f, valid ? to.z : 3.0e38f};
+        float hi[3] = {valid ? to.x : -3.0e38f, valid ? to.y : -3.0e38f, valid ? to.z : -3.0e38f};
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], m));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], m));
+            }
+        if (lane == 0) {
+            wbox[warp][0] = make_float4(lo[0], lo[1], lo[2], 0.f);
+            wbox[warp][1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+        }
+        __syncwarp();
+    }
+#endif
 
 #if VPM_UJ_SMEM_ACC
     // FP64 sums of this thread: [0..2] U, [3..5] W, [6..13] J' (touched once per mid-level flush)
@@ -337,6 +390,36 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
             cp_async_wait<0>();
         }
         __syncwarp();
+#if VPM_UJ_TILE_FLAGS
+        bool far_src;
+        {   // this lane's source: FP32 offset from the warp origin, and whether every pair
+            // with the warp's targets is past max(reach, (2 b)^2)
+            const float4 a = stage[warp][buf][lane].a, b = stage[warp][buf][lane].b;
+            const float px = (a.x - oh.x) + (b.x - ol.x), py = (a.y - oh.y) + (b.y - ol.y),
+                        pz = (a.z - oh.z) + (b.z - ol.z);
+            offs[warp][buf][lane] = make_float4(px, py, pz, b.w * b.w);
+            const float4 lo = wbox[warp][0], hi = wbox[warp][1];
+            const float ex = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.0f);
+            const float ey = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.0f);
+            const float ez = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.0f);
+            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : r2n;
+            far_src = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > thr;
+        }
+        const unsigned farbits = __ballot_sync(0xffffffffu, far_src);
+        __syncwarp();
+        if (farbits == 0xffffffffu) {
+#pragma unroll (UJ_UNROLL)
+            for (int j = 0; j < WT; j += 4) pair4_far<K>(to, offs[warp][buf], stage[warp][buf], j, u, jq, w);
+        } else {
+#pragma unroll 1
+            for (int j = 0; j < WT; j += 4) {
+                if (((farbits >> j) & 0xFu) == 0xFu)
+                    pair4_far<K>(to, offs[warp][buf], stage[warp][buf], j, u, jq, w);
+                else
+                    pair4_near<K>(th, tl, offs[warp][buf], stage[warp][buf], j, u, jq, w);
+            }
+        }
+#else
         {   // this lane's source: FP32 offset from the warp origin and its far threshold
             const float4 a = stage[warp][buf][lane].a, b = stage[warp][buf][lane].b;
             const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : b.w * b.w;
@@ -347,6 +430,7 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
 #pragma unroll (UJ_UNROLL)
         for (int j = 0; j < WT; j += 4)
             pair4_mixed<K>(to, th, tl, r2n, offs[warp][buf], stage[warp][buf], j, u, jq, w);
+#endif
         if (++in_block == BLOCK_TILES) {
 #pragma unroll
             for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }

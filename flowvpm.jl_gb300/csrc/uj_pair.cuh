@@ -1,5 +1,5 @@
-// uj_pair.cuh -- the mixed (FP32-comp) UJ pair machinery shared by the all-pairs
-// kernel (uj.cu) and the near-field warp-group kernel (leaflist.cu).
+// uj_pair.cuh -- the UJ pair machinery (FP32-comp and FP64) shared by the all-pairs
+// kernels (uj.cu) and the near-field warp-group kernels (leaflist.cu).
 #pragma once
 #include "internal.h"
 #include "vpm_math.cuh"
@@ -35,6 +35,65 @@ __device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float G
     jq[5] = fmaf(bz, dy, jq[5]);
     jq[6] = fmaf(bx, dz, jq[6]);
     jq[7] = fmaf(by, dz, jq[7]);
+}
+
+// Far form of four sources j0..j0+3 whose pairs with every target of the warp are
+// known to be past the kernel's reach and past (2 b)^2: FP32 offsets, no test.
+// off[].w is 1/sigma^2 for the kernels without a singular tail (Winckelmans).
+template <int K>
+__device__ __forceinline__ void pair4_far(const float3& to, const float4* __restrict__ off,
+                                          const SrcMixed* __restrict__ tile, int j0, float (&u)[3],
+                                          float (&jq)[8], float (&w)[3])
+{
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float4 h = off[j0 + q];
+        const float dx = to.x - h.x, dy = to.y - h.y, dz = to.z - h.z;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        float G, Q;
+        if constexpr (singular_tail<K>()) {
+            const float rs = frsqrt(r2);
+            const float rs2 = rs * rs;
+            G = rs * rs2;
+            Q = G * rs2;
+        } else {
+            near_GQ<K>(r2 * h.w, h.w, G, Q);
+        }
+        accum_pair(dx, dy, dz, G, Q, tile[j0 + q].gam, u, jq, w);
+    }
+}
+
+// Full form of four sources j0..j0+3, per pair, with the displacement from the
+// double-float positions (th + tl) - (a + b); r == 0 contributes nothing.
+// off[].w as in pair4_far.
+template <int K>
+__device__ __forceinline__ void pair4_near(const float3& th, const float3& tl, const float4* __restrict__ off,
+                                           const SrcMixed* __restrict__ tile, int j0, float (&u)[3],
+                                           float (&jq)[8], float (&w)[3])
+{
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float4 a = tile[j0 + q].a, b = tile[j0 + q].b;
+        const float ex = (th.x - a.x) + (tl.x - b.x);
+        const float ey = (th.y - a.y) + (tl.y - b.y);
+        const float ez = (th.z - a.z) + (tl.z - b.z);
+        const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+        float G, Q;
+        if constexpr (singular_tail<K>()) {
+            const float isig2 = b.w * b.w;
+            near_GQ<K>(e2 * isig2, isig2, G, Q);
+            const float isig3 = isig2 * b.w;
+            G *= isig3;
+            Q *= isig3;
+        } else {
+            const float hw = off[j0 + q].w;
+            near_GQ<K>(e2 * hw, hw, G, Q);
+        }
+        const bool nz = e2 > 0.0f;
+        G = nz ? G : 0.0f;
+        Q = nz ? Q : 0.0f;
+        accum_pair(ex, ey, ez, G, Q, tile[j0 + q].gam, u, jq, w);
+    }
 }
 
 // Four sources j0..j0+3 of the tile against this lane's target.
@@ -152,6 +211,64 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             accum_pair(ex[q], ey[q], ez[q], g, qq, gq, u, jq, w);
         }
     }
+}
+
+// ----------------------------------------------------------- pair: FP64
+// The FP64 pair in the accumulated form of the mixed kernels: with c = dx x Gamma,
+//     u += G c,   w += G Gamma,   jq[3 i + j] += Q c_j dx_i,
+// G = g / r^3 and Q = -aux / (3 r^3) = (G - g' rho' r^-2 / 3) / r^2 (aux, g' = dg/drho and
+// rho' = 1/sigma as in src/FLOWVPM_fmm.jl:122-146); the target's U = -u/(4 pi), and
+// J = 3 jq/(4 pi) plus the Kronecker terms of src/FLOWVPM_fmm.jl:148-159 from -w/(4 pi)
+// (uj_f64_finish).  Algebraically the reference's terms, regrouped so that the strength
+// factor -1/(4 pi) and the products shared by the nine J entries are taken once.
+// Gaussian-erf pairs past rho = 9 take g = 1, g' = 0 (the reference's cut) from the
+// pack's threshold 81 sigma^2 without forming rho.  Pairs with r^2 == 0 are skipped.
+template <int K>
+__device__ __forceinline__ void pair_f64_acc(double tx, double ty, double tz, const SrcF64& s, double (&u)[3],
+                                             double (&w)[3], double (&jq)[9])
+{
+    const double dx = tx - s.xy.x, dy = ty - s.xy.y, dz = tz - s.z_isig.x;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 == 0.0) return;
+    const double rinv = rsqrt(r2);
+    const double rinv2 = rinv * rinv;
+    double G, Q;
+    if (K == K_SING || (K == K_GAUSERF && r2 > s.gz_sig.y)) {
+        G = rinv * rinv2;
+        Q = G * rinv2;
+    } else {
+        const double isig = s.z_isig.y;
+        double g, dg;
+        g_dgdr_f64<K>(r2 * rinv * isig, g, dg);
+        G = g * rinv * rinv2;
+        Q = (G - dg * isig * rinv2 * (1.0 / 3.0)) * rinv2;
+    }
+    const double gx = s.gxy.x, gy = s.gxy.y, gz = s.gz_sig.x;
+    const double cx = dy * gz - dz * gy, cy = dz * gx - dx * gz, cz = dx * gy - dy * gx;
+    u[0] += G * cx; u[1] += G * cy; u[2] += G * cz;
+    w[0] += G * gx; w[1] += G * gy; w[2] += G * gz;
+    const double bx = Q * cx, by = Q * cy, bz = Q * cz;
+    jq[0] += bx * dx; jq[1] += by * dx; jq[2] += bz * dx;
+    jq[3] += bx * dy; jq[4] += by * dy; jq[5] += bz * dy;
+    jq[6] += bx * dz; jq[7] += by * dz; jq[8] += bz * dz;
+}
+
+// U and J (the layout of pair_f64's acc) from the sums of pair_f64_acc.
+__device__ __forceinline__ void uj_f64_finish(const double (&u)[3], const double (&w)[3], const double (&jq)[9],
+                                              double (&acc)[12])
+{
+    constexpr double k = -C4;
+#pragma unroll
+    for (int m = 0; m < 3; m++) acc[m] = k * u[m];
+#pragma unroll
+    for (int m = 0; m < 9; m++) acc[3 + m] = (-3.0 * k) * jq[m];
+    const double wx = k * w[0], wy = k * w[1], wz = k * w[2];
+    acc[4] -= wz;
+    acc[5] += wy;
+    acc[6] += wz;
+    acc[8] -= wx;
+    acc[9] -= wy;
+    acc[10] += wx;
 }
 
 }  // namespace vpm
