@@ -41,10 +41,10 @@ FLOP_PER_PAIR = 74    # VPM_FLOP_PER_UJ_PAIR
 # DRAM bytes of one uj_mixed_kernel<gaussianerf> launch at N = 2^20, measured by ncu
 # (`ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
 #  --clock-control none -k regex:uj_mixed_kernel -c 1 python bench.py --kernel-only --n 1048576
-#  --warmup 0 --steps 1`): 394,715,392 read + 153,797,376 written.  The compulsory traffic is
+#  --warmup 0 --steps 1`): 405,746,944 read + 181,722,112 written.  The compulsory traffic is
 # ~0.16 GB (56 B in, 96 B out a particle); the rest is re-reads of the 50 MB source pack that
-# miss L2.  Either way it is ~0.35 GB/s over the 1.55 s launch: the kernel is FP32-bound.
-UJ_DRAM_BYTES_2P20 = 394_715_392 + 153_797_376
+# miss L2.  Either way it is ~0.42 GB/s over the 1.41 s launch: the kernel is FP32-bound.
+UJ_DRAM_BYTES_2P20 = 405_746_944 + 181_722_112
 # the headline metric as the reference's benchmark definition names it; `value` is the
 # FP32-comp rate, `fp64_gpu` / `mixed_over_fp64` and `adjoint` carry the other two parts
 METRIC = "UJ pair-interactions/s, FP32-comp vs FP64 GPU @≤1e-6 rel err; adjoint/fwd ratio"
@@ -317,7 +317,7 @@ def run_gpu(args, rank, world):
                          "traffic": UJ_DRAM_BYTES_2P20 if n == 1 << 20 else None,
                          "traffic_unit": "bytes per launch",
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one N=2^20 launch "
-                                           "(394.7 + 153.8 MB; 1 pass, --clock-control none)",
+                                           "(405.7 + 181.7 MB; 1 pass, --clock-control none)",
                          "kernel": "uj_mixed_kernel<gaussianerf>",
                          "flop_per_pair": FLOP_PER_PAIR,
                          "peak_source": "FFMA-loop kernel measured in this run (no FP32 figure in "
@@ -843,8 +843,8 @@ def run_rollout(args):
     estimate + strength-weighted axial centroid at the final step.  FP64
     forward and its gradient with per-step checkpointing (each step's UJ values
     kept, the adjoint kernel in the backward pass), checked against central
-    differences (h=1e-6) along --ro-dirs seeded random unit directions in
-    (X, Gamma, sigma); the FP32-comp forward is timed beside it."""
+    differences (h = each of --ro-h, 1e-6 by default) along --ro-dirs seeded random unit
+    directions in (X, Gamma, sigma); the FP32-comp forward is timed beside it."""
     import torch
     import vpm_gb300 as vpm
     import vpm_gb300.rings as rings
@@ -887,19 +887,24 @@ def run_rollout(args):
     ms_grad32, g32 = timed(grad32)
     g32_rel = max(float((a - b).abs().max() / b.abs().max()) for a, b in zip(g32, (gx, gg, gs)))
     rng = np.random.default_rng(3)
-    h = 1e-6
+    hs = [float(t) for t in args.ro_h.split(",")]
+    h = hs[0]
     worst = 0.0
+    worst_by_h = {f"{t:g}": 0.0 for t in hs}
     checks = []
     for _ in range(args.ro_dirs):
         v = [d(rng.normal(size=t.shape)) for t in (x0, g0, s0)]
         nrm = math.sqrt(sum(float((t * t).sum()) for t in v))
         v = [t / nrm for t in v]
-        fd = (loss_at(x0 + h * v[0], g0 + h * v[1], s0 + h * v[2]) -
-              loss_at(x0 - h * v[0], g0 - h * v[1], s0 - h * v[2])) / (2 * h)
         an = float((gx * v[0]).sum() + (gg * v[1]).sum() + (gs * v[2]).sum())
-        rel = abs(fd - an) / max(abs(an), 1e-300)
-        worst = max(worst, rel)
-        checks.append({"fd": fd, "adjoint": an, "rel": rel})
+        for t in hs:
+            fd = (loss_at(x0 + t * v[0], g0 + t * v[1], s0 + t * v[2]) -
+                  loss_at(x0 - t * v[0], g0 - t * v[1], s0 - t * v[2])) / (2 * t)
+            rel = abs(fd - an) / max(abs(an), 1e-300)
+            worst_by_h[f"{t:g}"] = max(worst_by_h[f"{t:g}"], rel)
+            if t == h:
+                worst = max(worst, rel)
+            checks.append({"h": t, "fd": fd, "adjoint": an, "rel": rel})
     print(json.dumps({"mode": "rollout", "n_particles": X.shape[0], "steps": steps, "dt": dt,
                       "sfs": None if sfs is None else f"ConstantSFS(Cs={sfs.Cs})",
                       "gradient_ms_fp32comp": ms_grad32, "fp32comp_gradient_vs_fp64_max_rel": g32_rel,
@@ -907,7 +912,8 @@ def run_rollout(args):
                       "forward_ms_fp32comp": ms_fwd32, "gradient_ms_fp64": ms_grad,
                       "gradient_over_forward": ms_grad / ms_fwd,
                       "backward_over_forward": (ms_grad - ms_fwd) / ms_fwd,
-                      "fd_directions": args.ro_dirs, "fd_h": h, "fd_max_rel_err": worst, "fd_checks": checks,
+                      "fd_directions": args.ro_dirs, "fd_h": h, "fd_max_rel_err": worst,
+                      "fd_max_rel_err_by_h": worst_by_h, "fd_checks": checks,
                       "note": "gradient = forward + backward with per-step checkpointing that keeps each step's "
                               "UJ values; central differences of the FP64 forward"}), flush=True)
 
@@ -978,6 +984,7 @@ def main():
     ap.add_argument("--ro-steps", type=int, default=50)
     ap.add_argument("--ro-dirs", type=int, default=4)
     ap.add_argument("--ro-sfs", type=float, default=0.0, help="Cs of a ConstantSFS term in the rollout (0: none)")
+    ap.add_argument("--ro-h", default="1e-6", help="central-difference steps of the rollout check, comma-separated")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))

@@ -531,48 +531,59 @@ uj_adjoint_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double
                 far = far && r2[q] > h.w;
             }
             const bool allfar = __all_sync(0xffffffffu, far);
-            float ex[4], ey[4], ez[4], i2[4], sq[4];
-            bool on[4];
+            float ex[4], ey[4], ez[4];
+            float A[4], B[4], Bpr[4], dA[4], dB[4];
+            if (allfar) {
+                // singular form, in r directly: A = -C4/r^3, B = 3 C4/r^5 = -3 A/r^2,
+                // B'/r = -15 C4/r^7 = -5 B/r^2, no sigma derivative.  Every pair is past
+                // (2 b)^2 > 0, and a lane without a target has zero Ubar, Jbar: all its terms
+                // vanish without the `on` weight.
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const SrcAdjMixed& sp = tile[j0 + q];
-                ex[q] = dx[q]; ey[q] = dy[q]; ez[q] = dz[q];
-                float e2 = r2[q];
-                if (!allfar) {   // double-float displacement
+                for (int q = 0; q < 4; q++) {
+                    ex[q] = dx[q]; ey[q] = dy[q]; ez[q] = dz[q];
+                    const float rs = frsqrt(r2[q]), rs2 = rs * rs;
+                    A[q] = -F_C4 * rs * rs2;
+                    B[q] = -3.0f * A[q] * rs2;
+                    Bpr[q] = -5.0f * B[q] * rs2;
+                    dA[q] = 0.0f;
+                    dB[q] = 0.0f;
+                }
+            } else {
+                float i2[4], sq[4];
+                bool on[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {   // double-float displacement
+                    const SrcAdjMixed& sp = tile[j0 + q];
                     ex[q] = (th.x - sp.a.x) + (tl.x - sp.b.x);
                     ey[q] = (th.y - sp.a.y) + (tl.y - sp.b.y);
                     ez[q] = (th.z - sp.a.z) + (tl.z - sp.b.z);
-                    e2 = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+                    const float e2 = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+                    on[q] = valid && e2 > 0.0f;
+                    i2[q] = sp.a.w * sp.a.w;
+                    sq[q] = on[q] ? e2 * i2[q] : 1.0f;
                 }
-                on[q] = valid && e2 > 0.0f;
-                i2[q] = sp.a.w * sp.a.w;
-                sq[q] = on[q] ? e2 * i2[q] : 1.0f;
-            }
-            float G[4], H[4], Kc[4], ca[4], cb[4];
-            if (allfar) {   // singular form (no sigma derivative)
+                float G[4], H[4], Kc[4], ca[4], cb[4];
+                adj_coeffs4_f32<K>(sq, G, H, Kc, ca, cb);
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const float rs = frsqrt(sq[q]), rs2 = rs * rs;
-                    G[q] = rs * rs2; H[q] = -3.0f * G[q] * rs2; Kc[q] = -5.0f * H[q] * rs2; ca[q] = 0.0f; cb[q] = 0.0f;
+                    const float isig = tile[j0 + q].a.w;
+                    const float w = on[q] ? 1.0f : 0.0f;
+                    const float i3 = i2[q] * isig;
+                    A[q] = -F_C4 * i3 * G[q] * w;
+                    B[q] = -F_C4 * i3 * i2[q] * H[q] * w;
+                    Bpr[q] = -F_C4 * i3 * i2[q] * i2[q] * Kc[q] * w;
+                    dA[q] = F_C4 * i2[q] * i2[q] * ca[q] * w;
+                    dB[q] = -F_C4 * i3 * i3 * cb[q] * w;
                 }
-            } else {
-                adj_coeffs4_f32<K>(sq, G, H, Kc, ca, cb);
             }
             float o[4][7];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const SrcAdjMixed& sp = tile[j0 + q];
-                const float isig = sp.a.w;
-                const float w = on[q] ? 1.0f : 0.0f;
-                const float i3 = i2[q] * isig;
-                const float A = -F_C4 * i3 * G[q] * w;
-                const float B = -F_C4 * i3 * i2[q] * H[q] * w;
-                const float Bpr = -F_C4 * i3 * i2[q] * i2[q] * Kc[q] * w;
-                const float dA = F_C4 * i2[q] * i2[q] * ca[q] * w;
-                const float dB = -F_C4 * i3 * i3 * cb[q] * w;
 #pragma unroll
                 for (int k = 0; k < 7; k++) o[q][k] = 0.f;
-                adj_pair_f32(ex[q], ey[q], ez[q], sp.g.x, sp.g.y, sp.g.z, A, B, Bpr, dA, dB, Ub, Jb, wb, o[q]);
+                adj_pair_f32(ex[q], ey[q], ez[q], sp.g.x, sp.g.y, sp.g.z, A[q], B[q], Bpr[q], dA[q], dB[q], Ub, Jb,
+                             wb, o[q]);
                 acc[0] += o[q][0]; acc[1] += o[q][1]; acc[2] += o[q][2];
                 o[q][0] = -o[q][0]; o[q][1] = -o[q][1]; o[q][2] = -o[q][2];
             }

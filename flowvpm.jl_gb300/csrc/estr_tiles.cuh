@@ -1,7 +1,8 @@
 // estr_tiles.cuh -- per-tile boxes of a source pack and the walk over the tiles within
-// reach of a warp's targets, shared by the mixed Estr (estr.cu) and its adjoint
-// (estr_adjoint.cu).  Their Gaussian weights fall below 1e-13 of zeta(0) past
-// zeta_skip_s, so whole 32-source tiles out of a warp's reach need not be loaded.
+// reach of a warp's targets, shared by the mixed Estr (estr.cu), its adjoint
+// (estr_adjoint.cu) and the filter differences (dynamic.cu).  Their Gaussian terms fall
+// below FP32 resolution past a reach (zeta_skip_s, dyn_skip_s), so whole 32-source tiles
+// out of a warp's reach need not be loaded.
 #pragma once
 #include "internal.h"
 #include "vpm_math.cuh"
@@ -41,8 +42,9 @@ __device__ __forceinline__ void estr_tile_box(int64_t o, int64_t ns, float xh, f
 // zeta/zeta(0) < 1e-13); the FP32 boxes shift that bound by a few ulp of the
 // coordinates, where the weights are already far below the FP32 resolution of the sums.
 // With wfix > 0 the test takes 1/sigma^2 = wfix instead of the tile's (the adjoint's second
-// pass, whose tiles hold targets and whose sigma is the lanes' sources').
-// Kernels that never skip take every tile.  All 32 lanes call it, with the same values.
+// pass, whose tiles hold targets and whose sigma is the lanes' sources').  next_s takes the
+// reach skip_s explicitly (the filter differences' dyn_skip_s); skip_s <= 0 or >= 1e37 (a
+// kernel without a reach) takes every tile.  All 32 lanes call it, with the same values.
 struct TileWalk {
     int n, c;
     unsigned mask;
@@ -51,17 +53,22 @@ struct TileWalk {
     __device__ __forceinline__ int next(const float4* __restrict__ box, const float4 lo, const float4 hi, int lane,
                                         float wfix = 0.0f)
     {
+        return next_s(box, lo, hi, lane, zeta_skip_s<K>(), wfix);
+    }
+    __device__ __forceinline__ int next_s(const float4* __restrict__ box, const float4 lo, const float4 hi, int lane,
+                                          float skip_s, float wfix = 0.0f)
+    {
         while (mask == 0u) {
             if ((c + 1) * 32 >= n) return -1;
             ++c;
             const int i = c * 32 + lane;
             bool in = i < n;
-            if (zeta_skip_s<K>() > 0.0f && in) {
+            if (skip_s > 0.0f && skip_s < 1.0e37f && in) {
                 const float4 bl = box[2 * i], bh = box[2 * i + 1];
                 const float ex = fmaxf(fmaxf(lo.x - bh.x, bl.x - hi.x), 0.0f);
                 const float ey = fmaxf(fmaxf(lo.y - bh.y, bl.y - hi.y), 0.0f);
                 const float ez = fmaxf(fmaxf(lo.z - bh.z, bl.z - hi.z), 0.0f);
-                in = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) * (wfix > 0.0f ? wfix : bl.w) > zeta_skip_s<K>());
+                in = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) * (wfix > 0.0f ? wfix : bl.w) > skip_s);
             }
             mask = __ballot_sync(0xffffffffu, in);
         }
