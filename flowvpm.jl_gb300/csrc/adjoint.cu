@@ -520,106 +520,110 @@ uj_adjoint_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, const double
         }
         __syncwarp();
 #pragma unroll 1
-        for (int j0 = 0; j0 < UJ_TILE; j0 += 4) {
-            float dx[4], dy[4], dz[4], r2[4];
-            bool far = true;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float4 h = off[warp][j0 + q];
-                dx[q] = to.x - h.x; dy[q] = to.y - h.y; dz[q] = to.z - h.z;
-                r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
-                far = far && r2[q] > h.w;
-            }
-            const bool allfar = __all_sync(0xffffffffu, far);
-            float ex[4], ey[4], ez[4];
-            float A[4], B[4], Bpr[4], dA[4], dB[4];
-            if (allfar) {
-                // singular form, in r directly: A = -C4/r^3, B = 3 C4/r^5 = -3 A/r^2,
-                // B'/r = -15 C4/r^7 = -5 B/r^2, no sigma derivative.  Every pair is past
-                // (2 b)^2 > 0, and a lane without a target has zero Ubar, Jbar: all its terms
-                // vanish without the `on` weight.
+        for (int sb = 0; sb < UJ_TILE; sb += 64) {
+#pragma unroll 1
+            for (int j0 = sb; j0 < sb + 64; j0 += 4) {
+                float dx[4], dy[4], dz[4], r2[4];
+                bool far = true;
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    ex[q] = dx[q]; ey[q] = dy[q]; ez[q] = dz[q];
-                    const float rs = frsqrt(r2[q]), rs2 = rs * rs;
-                    A[q] = -F_C4 * rs * rs2;
-                    B[q] = -3.0f * A[q] * rs2;
-                    Bpr[q] = -5.0f * B[q] * rs2;
-                    dA[q] = 0.0f;
-                    dB[q] = 0.0f;
+                    const float4 h = off[warp][j0 + q];
+                    dx[q] = to.x - h.x; dy[q] = to.y - h.y; dz[q] = to.z - h.z;
+                    r2[q] = fmaf(dx[q], dx[q], fmaf(dy[q], dy[q], dz[q] * dz[q]));
+                    far = far && r2[q] > h.w;
                 }
-            } else {
-                float i2[4], sq[4];
-                bool on[4];
+                const bool allfar = __all_sync(0xffffffffu, far);
+                float ex[4], ey[4], ez[4];
+                float A[4], B[4], Bpr[4], dA[4], dB[4];
+                if (allfar) {
+                    // singular form, in r directly: A = -C4/r^3, B = 3 C4/r^5 = -3 A/r^2,
+                    // B'/r = -15 C4/r^7 = -5 B/r^2, no sigma derivative.  Every pair is past
+                    // (2 b)^2 > 0, and a lane without a target has zero Ubar, Jbar: all its terms
+                    // vanish without the `on` weight.
 #pragma unroll
-                for (int q = 0; q < 4; q++) {   // double-float displacement
+                    for (int q = 0; q < 4; q++) {
+                        ex[q] = dx[q]; ey[q] = dy[q]; ez[q] = dz[q];
+                        const float rs = frsqrt(r2[q]), rs2 = rs * rs;
+                        A[q] = -F_C4 * rs * rs2;
+                        B[q] = -3.0f * A[q] * rs2;
+                        Bpr[q] = -5.0f * B[q] * rs2;
+                        dA[q] = 0.0f;
+                        dB[q] = 0.0f;
+                    }
+                } else {
+                    float i2[4], sq[4];
+                    bool on[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {   // double-float displacement
+                        const SrcAdjMixed& sp = tile[j0 + q];
+                        ex[q] = (th.x - sp.a.x) + (tl.x - sp.b.x);
+                        ey[q] = (th.y - sp.a.y) + (tl.y - sp.b.y);
+                        ez[q] = (th.z - sp.a.z) + (tl.z - sp.b.z);
+                        const float e2 = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+                        on[q] = valid && e2 > 0.0f;
+                        i2[q] = sp.a.w * sp.a.w;
+                        sq[q] = on[q] ? e2 * i2[q] : 1.0f;
+                    }
+                    float G[4], H[4], Kc[4], ca[4], cb[4];
+                    adj_coeffs4_f32<K>(sq, G, H, Kc, ca, cb);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const float isig = tile[j0 + q].a.w;
+                        const float w = on[q] ? 1.0f : 0.0f;
+                        const float i3 = i2[q] * isig;
+                        A[q] = -F_C4 * i3 * G[q] * w;
+                        B[q] = -F_C4 * i3 * i2[q] * H[q] * w;
+                        Bpr[q] = -F_C4 * i3 * i2[q] * i2[q] * Kc[q] * w;
+                        dA[q] = F_C4 * i2[q] * i2[q] * ca[q] * w;
+                        dB[q] = -F_C4 * i3 * i3 * cb[q] * w;
+                    }
+                }
+                float o[4][7];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
                     const SrcAdjMixed& sp = tile[j0 + q];
-                    ex[q] = (th.x - sp.a.x) + (tl.x - sp.b.x);
-                    ey[q] = (th.y - sp.a.y) + (tl.y - sp.b.y);
-                    ez[q] = (th.z - sp.a.z) + (tl.z - sp.b.z);
-                    const float e2 = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
-                    on[q] = valid && e2 > 0.0f;
-                    i2[q] = sp.a.w * sp.a.w;
-                    sq[q] = on[q] ? e2 * i2[q] : 1.0f;
+#pragma unroll
+                    for (int k = 0; k < 7; k++) o[q][k] = 0.f;
+                    adj_pair_f32(ex[q], ey[q], ez[q], sp.g.x, sp.g.y, sp.g.z, A[q], B[q], Bpr[q], dA[q], dB[q], Ub, Jb,
+                                 wb, o[q]);
+                    acc[0] += o[q][0]; acc[1] += o[q][1]; acc[2] += o[q][2];
+                    o[q][0] = -o[q][0]; o[q][1] = -o[q][1]; o[q][2] = -o[q][2];
                 }
-                float G[4], H[4], Kc[4], ca[4], cb[4];
-                adj_coeffs4_f32<K>(sq, G, H, Kc, ca, cb);
+                // source-side sums of the four sources over the warp's 32 targets, by reduce-scatter:
+                // lanes 16-31 / 0-15 keep sources {2,3} / {0,1}, then lanes with bit 3 set / clear
+                // keep the odd / even one, then a butterfly over the remaining 8 lanes; lane 8 g
+                // ends with source g's seven sums (21 + 21 shuffles per four sources, not 4 x 35)
+                const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+                float r[7];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float isig = tile[j0 + q].a.w;
-                    const float w = on[q] ? 1.0f : 0.0f;
-                    const float i3 = i2[q] * isig;
-                    A[q] = -F_C4 * i3 * G[q] * w;
-                    B[q] = -F_C4 * i3 * i2[q] * H[q] * w;
-                    Bpr[q] = -F_C4 * i3 * i2[q] * i2[q] * Kc[q] * w;
-                    dA[q] = F_C4 * i2[q] * i2[q] * ca[q] * w;
-                    dB[q] = -F_C4 * i3 * i3 * cb[q] * w;
+                for (int k = 0; k < 7; k++) {
+                    const float p0 = (b4 ? o[2][k] : o[0][k]) + __shfl_xor_sync(0xffffffffu, b4 ? o[0][k] : o[2][k], 16);
+                    const float p1 = (b4 ? o[3][k] : o[1][k]) + __shfl_xor_sync(0xffffffffu, b4 ? o[1][k] : o[3][k], 16);
+                    float v = (b3 ? p1 : p0) + __shfl_xor_sync(0xffffffffu, b3 ? p0 : p1, 8);
+#pragma unroll
+                    for (int m = 4; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+                    r[k] = v;
+                }
+                if ((lane & 7) == 0) {
+                    const int q = (b4 ? 2 : 0) + (b3 ? 1 : 0);
+#pragma unroll
+                    for (int k = 0; k < 7; k++) red[warp][j0 + q][k] = r[k];
                 }
             }
-            float o[4][7];
+            // FP64 after each 64 sources, outside the 4-source loop (as a branch in that loop it
+            // measured as issued on every iteration)
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const SrcAdjMixed& sp = tile[j0 + q];
-#pragma unroll
-                for (int k = 0; k < 7; k++) o[q][k] = 0.f;
-                adj_pair_f32(ex[q], ey[q], ez[q], sp.g.x, sp.g.y, sp.g.z, A[q], B[q], Bpr[q], dA[q], dB[q], Ub, Jb,
-                             wb, o[q]);
-                acc[0] += o[q][0]; acc[1] += o[q][1]; acc[2] += o[q][2];
-                o[q][0] = -o[q][0]; o[q][1] = -o[q][1]; o[q][2] = -o[q][2];
-            }
-            // source-side sums of the four sources over the warp's 32 targets, by reduce-scatter:
-            // lanes 16-31 / 0-15 keep sources {2,3} / {0,1}, then lanes with bit 3 set / clear
-            // keep the odd / even one, then a butterfly over the remaining 8 lanes; lane 8 g
-            // ends with source g's seven sums (21 + 21 shuffles per four sources, not 4 x 35)
-            const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
-            float r[7];
-#pragma unroll
-            for (int k = 0; k < 7; k++) {
-                const float p0 = (b4 ? o[2][k] : o[0][k]) + __shfl_xor_sync(0xffffffffu, b4 ? o[0][k] : o[2][k], 16);
-                const float p1 = (b4 ? o[3][k] : o[1][k]) + __shfl_xor_sync(0xffffffffu, b4 ? o[1][k] : o[3][k], 16);
-                float v = (b3 ? p1 : p0) + __shfl_xor_sync(0xffffffffu, b3 ? p0 : p1, 8);
-#pragma unroll
-                for (int m = 4; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-                r[k] = v;
-            }
-            if ((lane & 7) == 0) {
-                const int q = (b4 ? 2 : 0) + (b3 ? 1 : 0);
-#pragma unroll
-                for (int k = 0; k < 7; k++) red[warp][j0 + q][k] = r[k];
-            }
-            if ((j0 & 63) == 60) {
-#pragma unroll
-                for (int k = 0; k < 3; k++) { accd[k] += (double)acc[k]; acc[k] = 0.f; }
-            }
+            for (int k = 0; k < 3; k++) { accd[k] += (double)acc[k]; acc[k] = 0.f; }
         }
         __syncthreads();
         const int si = (int)__float_as_int(tile[threadIdx.x].g.w);
         if (si >= 0) {
+            // the 4 warps' FP32 sums of this source, added in FP32 (4 terms), then FP64
             double v[7];
 #pragma unroll
             for (int k = 0; k < 7; k++)
-                v[k] = (double)red[0][threadIdx.x][k] + (double)red[1][threadIdx.x][k] +
-                       (double)red[2][threadIdx.x][k] + (double)red[3][threadIdx.x][k];
+                v[k] = (double)((red[0][threadIdx.x][k] + red[1][threadIdx.x][k]) +
+                                (red[2][threadIdx.x][k] + red[3][threadIdx.x][k]));
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 atomicAdd(&xbar[3 * (int64_t)si + k], v[k]);

@@ -35,6 +35,9 @@ constexpr int NF_MID_BLKS = 4;               // blocks summed in FP32 before the
 #ifndef VPM_NF_DF
 #define VPM_NF_DF 1                          // nf_uj_leaf: 1 = double-float displacement on every group
 #endif
+#ifndef VPM_NF_LANE
+#define VPM_NF_LANE 0                        // 1: near-field FP32-comp UJ with a list walk per lane (nf_uj_lane)
+#endif
 
 __global__ void tgt_from_perm(int64_t n, const double* __restrict__ x, const int32_t* __restrict__ perm,
                               TgtPos* __restrict__ out)
@@ -301,6 +304,141 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
 #pragma unroll
     for (int k = 0; k < 8; k++) dJ[k] = acc64[6 + k][threadIdx.x] + ((double)mj[k] + (double)jq[k]);
     if (!me.valid) return;
+    double j9[9];
+#pragma unroll
+    for (int k = 0; k < 8; k++) j9[k] = -3.0 * dJ[k];
+    j9[8] = 3.0 * (dJ[0] + dJ[4]);
+    j9[1] -= dW[2]; j9[2] += dW[1]; j9[3] += dW[2]; j9[5] -= dW[0]; j9[6] -= dW[1]; j9[7] += dW[0];
+#pragma unroll
+    for (int k = 0; k < 3; k++) U[3 * (int64_t)me.idx + k] += dU[k];
+#pragma unroll
+    for (int k = 0; k < 9; k++) J[9 * (int64_t)me.idx + k] += j9[k];
+}
+
+// --------------------------------------------- UJ, FP32-comp, a walk per lane
+// Sources of nf_uj_lane: the double-float position with 1/sigma^2 in a.w, and
+// gam = -Gamma/(4 pi sigma^3) for every kernel (the near form's sigma^-3 taken once).
+template <int K>
+__global__ void leaf_pack_lane(int64_t n, const double* __restrict__ x, const double* __restrict__ gs,
+                               const double* __restrict__ sgs, const int32_t* __restrict__ perm,
+                               SrcMixed* __restrict__ out)
+{
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int64_t i = perm[o];
+    const double px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+    const float xh = (float)px, yh = (float)py, zh = (float)pz;
+    const double sig = (K == K_SING) ? 1.0 : sgs[i];
+    const double k = -C4 / (sig * sig * sig);
+    SrcMixed p;
+    p.a = make_float4(xh, yh, zh, (float)(1.0 / (sig * sig)));
+    p.b = make_float4((float)(px - (double)xh), (float)(py - (double)yh), (float)(pz - (double)zh), 0.f);
+    p.gam = make_float4((float)(k * gs[3 * i]), (float)(k * gs[3 * i + 1]), (float)(k * gs[3 * i + 2]), 0.f);
+    out[o] = p;
+}
+
+// Each lane walks the source list of its own target's leaf, straight from the CSR rows
+// (col[row[L] .. row[L+1]) source leaves, each the particle range [lb, le) of the pack),
+// four sources at a time, so that every pair a lane computes is one of its leaf's pairs:
+// no lane computes a pair of another leaf with zero weight, as the warp-group kernel's do
+// (a third of them on the jet cloud).  A warp runs until its longest list ends.  Lanes
+// read their sources themselves (read-only loads; the lanes of one leaf read the same
+// address together).  Pair math as the warp-group kernel's (double-float displacement,
+// the form of four pairs chosen warp-wide); FP32 sums over 64 sources, then FP32 mid-level
+// sums, then FP64 in shared memory.
+template <int K>
+__global__ void __launch_bounds__(NF_THREADS, VPM_NF_MIN_BLOCKS)
+nf_uj_lane(int64_t n, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
+           const int32_t* __restrict__ lb, const int32_t* __restrict__ le, const int32_t* __restrict__ row,
+           const int32_t* __restrict__ col, const SrcMixed* __restrict__ src, double* U, double* J)
+{
+    const int64_t t = (int64_t)blockIdx.x * NF_THREADS + threadIdx.x;
+    const bool valid = t < n;
+    const TgtPos me = tgt[valid ? t : n - 1];
+    const float3 th = make_float3((float)me.x, (float)me.y, (float)me.z);
+    const float3 tl = make_float3((float)(me.x - (double)th.x), (float)(me.y - (double)th.y),
+                                  (float)(me.z - (double)th.z));
+    // the walk: the current range [pc, pe), the next range [nb, ne) loaded ahead, col entry e of [.., e1)
+    int e = 0, e1 = 0, pc = 0, pe = 0, nb = 0, ne = 0;
+    if (valid) {
+        const int L = leaf_of[t];
+        e = row[L];
+        e1 = row[L + 1];
+        if (e < e1) { const int S = col[e]; nb = lb[S]; ne = le[S]; }
+    }
+    __shared__ double acc64[14][NF_THREADS];
+#pragma unroll
+    for (int k = 0; k < 14; k++) acc64[k][threadIdx.x] = 0.0;
+    float mu[3] = {0.f, 0.f, 0.f}, mw[3] = {0.f, 0.f, 0.f}, mj[8];
+    float u[3] = {0.f, 0.f, 0.f}, w[3] = {0.f, 0.f, 0.f}, jq[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { mj[k] = 0.f; jq[k] = 0.f; }
+    int its = 0, blks = 0;
+    for (;;) {
+        int sp[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (pc == pe && e < e1) {   // the next range of the list (leaves are never empty)
+                pc = nb; pe = ne; ++e;
+                if (e < e1) { const int S = col[e]; nb = lb[S]; ne = le[S]; }
+            }
+            const bool has = pc < pe;
+            sp[q] = has ? pc : -1;
+            pc += has ? 1 : 0;
+        }
+        if (!__any_sync(0xffffffffu, sp[0] >= 0)) break;   // every lane's list has ended
+        float ex[4], ey[4], ez[4], s4[4], i2[4], G[4], Q[4];
+        bool on[4];
+        float4 gq[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float4 a = make_float4(th.x, th.y, th.z, 1.f), b = make_float4(tl.x, tl.y, tl.z, 0.f);
+            gq[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (sp[q] >= 0) {
+                a = __ldg(&src[sp[q]].a);
+                b = __ldg(&src[sp[q]].b);
+                gq[q] = __ldg(&src[sp[q]].gam);
+            }
+            ex[q] = (th.x - a.x) + (tl.x - b.x);
+            ey[q] = (th.y - a.y) + (tl.y - b.y);
+            ez[q] = (th.z - a.z) + (tl.z - b.z);
+            const float e2 = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
+            on[q] = e2 > 0.0f;   // no source, the self pair and coincident particles: nothing
+            i2[q] = a.w;
+            s4[q] = on[q] ? e2 * a.w : 1.0f;
+        }
+        near_GQ4<K, false>(s4, i2, G, Q);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            accum_pair(ex[q], ey[q], ez[q], on[q] ? G[q] : 0.0f, on[q] ? Q[q] : 0.0f, gq[q], u, jq, w);
+        if (++its == 16) {   // 64 sources a lane
+            its = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) { mu[k] += u[k]; mw[k] += w[k]; u[k] = 0.f; w[k] = 0.f; }
+#pragma unroll
+            for (int k = 0; k < 8; k++) { mj[k] += jq[k]; jq[k] = 0.f; }
+            if (++blks == NF_MID_BLKS) {
+                blks = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    acc64[k][threadIdx.x] += (double)mu[k];
+                    acc64[3 + k][threadIdx.x] += (double)mw[k];
+                    mu[k] = 0.f; mw[k] = 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) { acc64[6 + k][threadIdx.x] += (double)mj[k]; mj[k] = 0.f; }
+            }
+        }
+    }
+    if (!valid) return;
+    double dU[3], dW[3], dJ[8];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        dU[k] = acc64[k][threadIdx.x] + ((double)mu[k] + (double)u[k]);
+        dW[k] = acc64[3 + k][threadIdx.x] + ((double)mw[k] + (double)w[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) dJ[k] = acc64[6 + k][threadIdx.x] + ((double)mj[k] + (double)jq[k]);
     double j9[9];
 #pragma unroll
     for (int k = 0; k < 8; k++) j9[k] = -3.0 * dJ[k];
@@ -1006,7 +1144,11 @@ static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* wo
     tgt_from_perm<<<g, 256, 0, st>>>(n, a.x, L.perm, tgt);
     *launches += 1;
     if (a.uj && a.precision) {
-#if VPM_NF_LEAF
+#if VPM_NF_LANE
+        leaf_pack_lane<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
+        nf_uj_lane<K><<<(unsigned)((n + NF_THREADS - 1) / NF_THREADS), NF_THREADS, 0, st>>>(
+            n, tgt, L.leaf_of, L.leaf_begin, L.leaf_end, L.row, L.col, (const SrcMixed*)src, a.U, a.J);
+#elif VPM_NF_LEAF
         leaf_pack_scaled<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
         nf_uj_leaf<K><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row, L.col,
                                                  (const SrcMixed*)src, a.U, a.J);

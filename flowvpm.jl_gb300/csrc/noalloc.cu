@@ -12,9 +12,8 @@
 //
 // Host code cannot use the array's name as a device address (on the host it is
 // only a stand-in), so the first call on each device, with that device
-// current, looks the address up with cudaGetSymbolAddress and caches it.  That
-// first call should therefore come before any stream capture.  Every call
-// shares the one array and overwrites what it needs (nothing has to start at
+// current, looks the address up with cudaGetSymbolAddress and caches it.  Every
+// call shares the one array and overwrites what it needs (nothing has to start at
 // zero), so calls whose device work overlaps -- on different streams or from
 // different threads -- race on it; serialise them.
 #include "../../include/vpm_gb300.h"

@@ -348,8 +348,7 @@ int vpm_leaflist_dev(vpm_ctx* ctx, int64_t n, const double* x, int leaf_size, do
  * held by every GPU that loads it until the process exits; problems needing
  * more scratch than that (roughly N > 2^19 particles) return VPM_ERR_CAPACITY.
  * The first call on each device looks up the array's device address (with
- * that device current), so make that first call before any stream capture.
- * All calls share the array: calls whose device work overlaps race on it.
+ * that device current) and caches it.  All calls share the array: calls whose device work overlaps race on it.
  * Errors are described by vpm_last_error(NULL). */
 int vpm_uj_dev_noalloc(int64_t nt, const double* xt,
                        int64_t ns, const double* xs, const double* gs, const double* sgs,
