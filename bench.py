@@ -38,6 +38,7 @@ for p in (ROOT, os.path.join(ROOT, "flowvpm.jl_gb300")):
 N_PARTICLES = 1 << 20
 KERNEL = 2            # gaussianerf
 FLOP_PER_PAIR = 74    # VPM_FLOP_PER_UJ_PAIR
+FLOP_PER_ADJ_PAIR = 186   # VPM_FLOP_PER_UJ_ADJ_PAIR
 # DRAM bytes of one uj_mixed_kernel<gaussianerf> launch at N = 2^20, measured by ncu
 # (`ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
 #  --clock-control none -k regex:uj_mixed_kernel -c 1 python bench.py --kernel-only --n 1048576
@@ -293,9 +294,10 @@ def run_gpu(args, rank, world):
                "U_rms_rel": float(np.linalg.norm(Uh - Ur) / np.linalg.norm(Ur)),
                "J_rms_rel": float(np.linalg.norm(Jh - Jr) / np.linalg.norm(Jr)),
                "targets_checked": 256}
-        fp64 = fp64_rate(ctx, vpm, torch, X, G, s, measure_dfma_peak(ffma))
+        dfma_peak = measure_dfma_peak(ffma)
+        fp64 = fp64_rate(ctx, vpm, torch, X, G, s, dfma_peak)
         wnk = winckelmans_rate(ctx, vpm, torch, X, G, s)
-        adjoint = adjoint_ratio(ctx, vpm, torch)
+        adjoint = adjoint_ratio(ctx, vpm, torch, peak_tflops, dfma_peak)
         estr_b, lf_b = rings_blocks(ctx, vpm, torch, peak_tflops)
         jet_b = jet_block(ctx, vpm, torch, peak_tflops)
         base = cpu_baseline(X, G, s)
@@ -493,7 +495,7 @@ def winckelmans_rate(ctx, vpm, torch, X, G, s):
                                 "targets_checked": 256}}
 
 
-def adjoint_ratio(ctx, vpm, torch, n=32000):
+def adjoint_ratio(ctx, vpm, torch, ffma_peak, dfma_peak, n=32000):
     """FP64 UJ adjoint (vpm_uj_adjoint_dev) vs FP64 UJ forward on an n-particle
     ring (1000 sections x 32 per section, the rollout workload's size), and a
     5-step rollout gradient (with per-step recompute) vs its forward."""
@@ -561,9 +563,15 @@ def adjoint_ratio(ctx, vpm, torch, n=32000):
     t_grad_sfs = timed(roll_grad_sfs)
     estr.update({"sfs_rollout_fwd_ms": t_roll_sfs, "sfs_rollout_grad_ms": t_grad_sfs,
                  "sfs_rollout_grad_over_fwd": t_grad_sfs / t_roll_sfs})
+    def roof(ms, peak, pipe):
+        ach = FLOP_PER_ADJ_PAIR * n * n / (ms / 1e3) / 1e12
+        return {"bound": pipe, "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "flop_per_pair": FLOP_PER_ADJ_PAIR}
     return {"n_particles": n, "uj_fwd_ms": fwd, "uj_adjoint_ms": adj, "uj_adjoint_over_fwd": adj / fwd,
             "uj_fwd_ms_fp32comp": fwd32, "uj_adjoint_ms_fp32comp": adj32,
-            "uj_adjoint_over_fwd_fp32comp": adj32 / fwd32, **estr,
+            "uj_adjoint_over_fwd_fp32comp": adj32 / fwd32,
+            "uj_adjoint_roofline_fp64": roof(adj, dfma_peak, "fp64"),
+            "uj_adjoint_roofline_fp32comp": roof(adj32, ffma_peak, "fp32"), **estr,
             "rollout_steps": steps, "rollout_fwd_ms": t_roll, "rollout_grad_ms": t_grad,
             "rollout_grad_over_fwd": t_grad / t_roll, "rollout_backward_over_fwd": (t_grad - t_roll) / t_roll,
             "rollout_grad_recompute_ms": t_grad_rc, "rollout_grad_recompute_over_fwd": t_grad_rc / t_roll,

@@ -215,6 +215,8 @@ struct IntervalWalk {
 };
 
 // ------------------------------------------------------------- UJ, FP32-comp
+// Sources from leaf_pack_lane: 1/sigma^2 in a.w and the near form's 1/sigma^3 in gam, so
+// that a pair takes neither (pair4_mixed with SCALED).
 template <int K>
 __global__ void __launch_bounds__(NF_THREADS, VPM_NF_MIN_BLOCKS)
 nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ leaf_of,
@@ -239,7 +241,6 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
     const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
-    const float sfar = s_far<K>();
 
     // FP64 sums of this lane in shared memory ([0..2] U, [3..5] W, [6..13] J'), touched once per
     // NF_MID_BLKS blocks: the registers go to occupancy instead
@@ -267,15 +268,14 @@ nf_uj_mixed(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const in
             sj.gam = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         sj.gam.w = __uint_as_float(smask);
-        const float thr = singular_tail<K>() ? fmaxf(sfar * sj.a.w, r2n) : sj.b.w * sj.b.w;
         __syncwarp();
         tile[warp][lane] = sj;
         off[warp][lane] = make_float4((sj.a.x - oh.x) + (sj.b.x - ol.x), (sj.a.y - oh.y) + (sj.b.y - ol.y),
-                                      (sj.a.z - oh.z) + (sj.b.z - ol.z), thr);
+                                      (sj.a.z - oh.z) + (sj.b.z - ol.z), sj.a.w);
         __syncwarp();
         const int ng = (cnt + 3) >> 2;
         for (int q = 0; q < ng; q++)
-            pair4_mixed<K, true, false>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, me.bit);
+            pair4_mixed<K, true, false, true>(to, th, tl, r2n, off[warp], tile[warp], 4 * q, u, jq, w, me.bit);
         if (++tiles == NF_BLK_TILES) {
             tiles = 0;
 #pragma unroll
@@ -1153,7 +1153,7 @@ static cudaError_t launch_leaf_k(const LeafArgs& a, const NearLists& L, void* wo
         nf_uj_leaf<K><<<gl, NF_THREADS, 0, st>>>(L.nleaves, tgt, L.leaf_begin, L.leaf_end, L.row, L.col,
                                                  (const SrcMixed*)src, a.U, a.J);
 #else
-        leaf_pack_mixed<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
+        leaf_pack_lane<K><<<g, 256, 0, st>>>(n, a.x, a.gam, a.sig, L.perm, (SrcMixed*)src);
         nf_uj_mixed<K><<<gb, NF_THREADS, 0, st>>>(n, L.ngroups, tgt, L.leaf_of, L.grp_row, L.ivs,
                                                   (const SrcMixed*)src, a.U, a.J);
 #endif

@@ -108,7 +108,9 @@ __device__ __forceinline__ void pair4_near(const float3& th, const float3& tl, c
 //             four pairs at a time with the form chosen warp-wide (near_GQ4)
 //             and no singular branch; off[].w (1/sigma^2 for Winckelmans) is
 //             still read
-template <int K, bool MASK = false, bool VOTE = true>
+//   SCALED  : (with VOTE = false) the tile holds 1/sigma^2 in a.w and gam carries
+//             the 1/sigma^3 of the near form (leaf_pack_lane), for every kernel
+template <int K, bool MASK = false, bool VOTE = true, bool SCALED = false>
 __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, const float3& tl, float r2n,
                                             const float4* __restrict__ off, const SrcMixed* __restrict__ tile,
                                             int j0, float (&u)[3], float (&jq)[8], float (&w)[3],
@@ -191,14 +193,14 @@ __device__ __forceinline__ void pair4_mixed(const float3& to, const float3& th, 
             ey[q] = (th.y - a.y) + (tl.y - b.y);
             ez[q] = (th.z - a.z) + (tl.z - b.z);
             e2[q] = fmaf(ex[q], ex[q], fmaf(ey[q], ey[q], ez[q] * ez[q]));
-            i2[q] = singular_tail<K>() ? b.w * b.w : hw[q];
+            i2[q] = SCALED ? a.w : singular_tail<K>() ? b.w * b.w : hw[q];
             s4[q] = e2[q] * i2[q];
         }
         near_GQ4<K, false>(s4, i2, G, Q);
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             float g = G[q], qq = Q[q];
-            if constexpr (singular_tail<K>()) {
+            if constexpr (singular_tail<K>() && !SCALED) {
                 const float isig3 = i2[q] * tile[j0 + q].b.w;
                 g *= isig3;
                 qq *= isig3;

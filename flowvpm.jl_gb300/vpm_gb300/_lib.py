@@ -25,6 +25,7 @@ CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy, the legacy default stream's handle
 NFIELDS = 46
 FLOP_PER_UJ_PAIR = 74
 FLOP_PER_ESTR_PAIR = 25
+FLOP_PER_UJ_ADJ_PAIR = 186
 
 _STATUS_NAMES = {ERR_ARG: "VPM_ERR_ARG", ERR_CAPACITY: "VPM_ERR_CAPACITY", ERR_CUDA: "VPM_ERR_CUDA",
                  ERR_NONFINITE: "VPM_ERR_NONFINITE", ERR_TIMEOUT: "VPM_ERR_TIMEOUT",

@@ -95,6 +95,9 @@ enum {
  * mul = 1, fma = 2; sqrt/exp/erf/reciprocals counted separately). */
 #define VPM_FLOP_PER_UJ_PAIR   74
 #define VPM_FLOP_PER_ESTR_PAIR 25
+/* the reverse mode of a UJ pair (vpm_uj_adjoint_dev): the 7 derivatives of
+ * Ubar.u + Jbar:j with respect to dx, Gamma and sigma, g, g' and g'' included */
+#define VPM_FLOP_PER_UJ_ADJ_PAIR 186
 
 /* ---------------------------------------------------------------- context */
 
