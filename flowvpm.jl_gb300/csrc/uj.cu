@@ -275,6 +275,10 @@ constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
 // registers for 7 resident blocks per SM instead of 5 -- measured 3.6 % faster at N = 2^20
 #define VPM_UJ_SMEM_ACC 1
 #endif
+#ifndef VPM_UJ_TPL
+// targets per lane of the mixed kernel: 1 (uj_mixed_kernel) or 2 (uj_mixed2_kernel)
+#define VPM_UJ_TPL 1
+#endif
 #ifndef VPM_UJ_TILE_FLAGS
 // 1: far/near decided once per tile from the warp's target box: the loading lane flags its
 // source far when the box is out of the source's reach, one ballot gives the tile's flags,
@@ -477,6 +481,200 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     double acc[12] = {fU[0], fU[1], fU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
     write_uj(t, idx, acc, U, ldU, J, ldJ, partial, nt_pad);
 }
+// --------------------------------------------- mixed kernel, two targets a lane
+// uj_mixed_kernel with two targets per lane: a warp takes 64 Morton-consecutive
+// targets (lane l: base + l and base + 32 + l), so that each source's shared-memory
+// reads, its tile's far flag and the tile's loads and conversions serve two pairs.
+// Blocks of 128 threads take 256 targets; the register budget is 3 resident blocks
+// per SM (every sum of both targets in registers, FP64 sums in shared memory).
+template <int K>
+__global__ void __launch_bounds__(UJ_THREADS, 3)
+uj_mixed2_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
+                 const SrcMixed* __restrict__ src, int64_t per_split, double* U, int64_t ldU,
+                 double* J, int64_t ldJ, double* partial, int64_t nt_pad)
+{
+    __shared__ SrcMixed stage[UJ_WARPS][2][WT];
+    __shared__ float4 offs[UJ_WARPS][2][WT];
+    __shared__ float4 wbox[UJ_WARPS][2];
+    __shared__ double acc64[14][2 * UJ_THREADS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * (2 * UJ_THREADS) + 64 * warp;
+    const int64_t tt[2] = {base + lane, base + 32 + lane};
+    bool valid[2];
+    double tx[2], ty[2], tz[2];
+    int32_t idx[2];
+    float3 th[2], tl[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        valid[k] = tt[k] < nt;
+        tx[k] = ty[k] = tz[k] = 3.0e4;
+        idx[k] = 0;
+        if (valid[k]) {
+            const TgtPos p = tgt[tt[k]];
+            tx[k] = p.x; ty[k] = p.y; tz[k] = p.z; idx[k] = p.idx;
+        }
+        th[k] = make_float3((float)tx[k], (float)ty[k], (float)tz[k]);
+        tl[k] = make_float3((float)(tx[k] - (double)th[k].x), (float)(ty[k] - (double)th[k].y),
+                            (float)(tz[k] - (double)th[k].z));
+    }
+    // warp origin: lane 0's first target (valid whenever any target of the warp is)
+    const double ox = __shfl_sync(0xffffffffu, tx[0], 0);
+    const double oy = __shfl_sync(0xffffffffu, ty[0], 0);
+    const double oz = __shfl_sync(0xffffffffu, tz[0], 0);
+    const float3 oh = make_float3(__shfl_sync(0xffffffffu, th[0].x, 0), __shfl_sync(0xffffffffu, th[0].y, 0),
+                                  __shfl_sync(0xffffffffu, th[0].z, 0));
+    const float3 ol = make_float3(__shfl_sync(0xffffffffu, tl[0].x, 0), __shfl_sync(0xffffffffu, tl[0].y, 0),
+                                  __shfl_sync(0xffffffffu, tl[0].z, 0));
+    float3 to[2];
+    float b2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        to[k] = valid[k] ? make_float3((float)(tx[k] - ox), (float)(ty[k] - oy), (float)(tz[k] - oz))
+                         : make_float3(3.0e4f, 3.0e4f, 3.0e4f);
+        if (valid[k]) b2 = fmaxf(b2, fmaf(to[k].x, to[k].x, fmaf(to[k].y, to[k].y, to[k].z * to[k].z)));
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) b2 = fmaxf(b2, __shfl_xor_sync(0xffffffffu, b2, m));
+    const float r2n = fmaxf(4.0f * b2, 1.0e-30f);
+    const float sfar = s_far<K>();
+    {   // the box of the warp's valid targets (offsets)
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+            if (valid[k]) {
+                lo[0] = fminf(lo[0], to[k].x); lo[1] = fminf(lo[1], to[k].y); lo[2] = fminf(lo[2], to[k].z);
+                hi[0] = fmaxf(hi[0], to[k].x); hi[1] = fmaxf(hi[1], to[k].y); hi[2] = fmaxf(hi[2], to[k].z);
+            }
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], m));
+                hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], m));
+            }
+        if (lane == 0) {
+            wbox[warp][0] = make_float4(lo[0], lo[1], lo[2], 0.f);
+            wbox[warp][1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 14; k++) { acc64[k][threadIdx.x] = 0.0; acc64[k][UJ_THREADS + threadIdx.x] = 0.0; }
+    __syncwarp();
+    float mu0[3] = {0.f, 0.f, 0.f}, mw0[3] = {0.f, 0.f, 0.f}, mj0[8];
+    float mu1[3] = {0.f, 0.f, 0.f}, mw1[3] = {0.f, 0.f, 0.f}, mj1[8];
+    float u0[3] = {0.f, 0.f, 0.f}, w0[3] = {0.f, 0.f, 0.f}, jq0[8];
+    float u1[3] = {0.f, 0.f, 0.f}, w1[3] = {0.f, 0.f, 0.f}, jq1[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { mj0[k] = 0.f; jq0[k] = 0.f; mj1[k] = 0.f; jq1[k] = 0.f; }
+
+    const int64_t s0 = (int64_t)blockIdx.y * per_split;
+    const int64_t s1 = min(s0 + per_split, ns_pad);
+    const int ntiles = (int)((s1 - s0) / WT);
+    const SrcMixed* wsrc = src + s0 + lane;
+    if (ntiles > 0) {
+        SrcMixed* d = &stage[warp][0][lane];
+        cp_async16(&d->a, &wsrc->a);
+        cp_async16(&d->b, &wsrc->b);
+        cp_async16(&d->gam, &wsrc->gam);
+        cp_async_commit();
+    }
+    int in_block = 0, in_mid = 0;
+    for (int it = 0; it < ntiles; it++) {
+        const int buf = it & 1;
+        if (it + 1 < ntiles) {
+            const SrcMixed* g = wsrc + (int64_t)(it + 1) * WT;
+            SrcMixed* d = &stage[warp][buf ^ 1][lane];
+            cp_async16(&d->a, &g->a);
+            cp_async16(&d->b, &g->b);
+            cp_async16(&d->gam, &g->gam);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        bool far_src;
+        {
+            const float4 a = stage[warp][buf][lane].a, b = stage[warp][buf][lane].b;
+            const float px = (a.x - oh.x) + (b.x - ol.x), py = (a.y - oh.y) + (b.y - ol.y),
+                        pz = (a.z - oh.z) + (b.z - ol.z);
+            offs[warp][buf][lane] = make_float4(px, py, pz, b.w * b.w);
+            const float4 lo = wbox[warp][0], hi = wbox[warp][1];
+            const float ex = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.0f);
+            const float ey = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.0f);
+            const float ez = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.0f);
+            const float thr = singular_tail<K>() ? fmaxf(sfar * a.w, r2n) : r2n;
+            far_src = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > thr;
+        }
+        const unsigned farbits = __ballot_sync(0xffffffffu, far_src);
+        __syncwarp();
+        if (farbits == 0xffffffffu) {
+#pragma unroll (UJ_UNROLL)
+            for (int j = 0; j < WT; j += 4)
+                pair4_far2<K>(to[0], to[1], offs[warp][buf], stage[warp][buf], j, u0, jq0, w0, u1, jq1, w1);
+        } else {
+#pragma unroll 1
+            for (int j = 0; j < WT; j += 4) {
+                if (((farbits >> j) & 0xFu) == 0xFu) {
+                    pair4_far2<K>(to[0], to[1], offs[warp][buf], stage[warp][buf], j, u0, jq0, w0, u1, jq1, w1);
+                } else {
+                    pair4_near<K>(th[0], tl[0], offs[warp][buf], stage[warp][buf], j, u0, jq0, w0);
+                    pair4_near<K>(th[1], tl[1], offs[warp][buf], stage[warp][buf], j, u1, jq1, w1);
+                }
+            }
+        }
+        if (++in_block == BLOCK_TILES) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                mu0[k] += u0[k]; mw0[k] += w0[k]; u0[k] = 0.f; w0[k] = 0.f;
+                mu1[k] += u1[k]; mw1[k] += w1[k]; u1[k] = 0.f; w1[k] = 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) { mj0[k] += jq0[k]; jq0[k] = 0.f; mj1[k] += jq1[k]; jq1[k] = 0.f; }
+            in_block = 0;
+            if (++in_mid == MID_BLOCKS) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    acc64[k][threadIdx.x] += (double)mu0[k];
+                    acc64[3 + k][threadIdx.x] += (double)mw0[k];
+                    acc64[k][UJ_THREADS + threadIdx.x] += (double)mu1[k];
+                    acc64[3 + k][UJ_THREADS + threadIdx.x] += (double)mw1[k];
+                    mu0[k] = mw0[k] = mu1[k] = mw1[k] = 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    acc64[6 + k][threadIdx.x] += (double)mj0[k];
+                    acc64[6 + k][UJ_THREADS + threadIdx.x] += (double)mj1[k];
+                    mj0[k] = mj1[k] = 0.f;
+                }
+                in_mid = 0;
+            }
+        }
+        __syncwarp();   // every lane is done with `buf` before it is refilled
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        if (!valid[k]) continue;
+        const int c = k * UJ_THREADS + threadIdx.x;
+        double fU[3], fW[3], fJ[8];
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            fU[m] = acc64[m][c] + ((double)(k ? mu1[m] : mu0[m]) + (double)(k ? u1[m] : u0[m]));
+            fW[m] = acc64[3 + m][c] + ((double)(k ? mw1[m] : mw0[m]) + (double)(k ? w1[m] : w0[m]));
+        }
+#pragma unroll
+        for (int m = 0; m < 8; m++)
+            fJ[m] = acc64[6 + m][c] + ((double)(k ? mj1[m] : mj0[m]) + (double)(k ? jq1[m] : jq0[m]));
+        double j9[9];
+#pragma unroll
+        for (int m = 0; m < 8; m++) j9[m] = -3.0 * fJ[m];
+        j9[8] = 3.0 * (fJ[0] + fJ[4]);
+        j9[1] -= fW[2]; j9[2] += fW[1]; j9[3] += fW[2]; j9[5] -= fW[0]; j9[6] -= fW[1]; j9[7] += fW[0];
+        double acc[12] = {fU[0], fU[1], fU[2], j9[0], j9[1], j9[2], j9[3], j9[4], j9[5], j9[6], j9[7], j9[8]};
+        write_uj(tt[k], idx[k], acc, U, ldU, J, ldJ, partial, nt_pad);
+    }
+}
+
 // ------------------------------------------------- packed-FP32 mixed kernel
 // The mixed kernel with the pair math in Blackwell's packed FP32 instructions
 // (fma / mul / sub .rn.f32x2: two FP32 operations per lane and instruction),
@@ -810,6 +1008,10 @@ static cudaError_t launch_uj_k(const UJArgs& a, const Workspace& w, int num_sms,
 #if VPM_UJ_F32X2
         uj_mixed_x2_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
                                                             a.J, a.ldJ, partial, nt_pad);
+#elif VPM_UJ_TPL == 2
+        const dim3 grid2((unsigned)((a.nt + 2 * UJ_THREADS - 1) / (2 * UJ_THREADS)), (unsigned)nsplit);
+        uj_mixed2_kernel<K><<<grid2, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
+                                                           a.J, a.ldJ, partial, nt_pad);
 #else
         uj_mixed_kernel<K><<<grid, UJ_THREADS, 0, st>>>(a.nt, tgt, ns_pad, src, per_split, a.U, a.ldU,
                                                          a.J, a.ldJ, partial, nt_pad);

@@ -63,6 +63,48 @@ __device__ __forceinline__ void pair4_far(const float3& to, const float4* __rest
     }
 }
 
+// pair4_far for two targets of the lane (offsets to0, to1), each source read once.
+template <int K>
+__device__ __forceinline__ void pair4_far2(const float3& to0, const float3& to1, const float4* __restrict__ off,
+                                           const SrcMixed* __restrict__ tile, int j0, float (&u0)[3],
+                                           float (&jq0)[8], float (&w0)[3], float (&u1)[3], float (&jq1)[8],
+                                           float (&w1)[3])
+{
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float4 h = off[j0 + q];
+        const float4 g = tile[j0 + q].gam;
+        {
+            const float dx = to0.x - h.x, dy = to0.y - h.y, dz = to0.z - h.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float G, Q;
+            if constexpr (singular_tail<K>()) {
+                const float rs = frsqrt(r2);
+                const float rs2 = rs * rs;
+                G = rs * rs2;
+                Q = G * rs2;
+            } else {
+                near_GQ<K>(r2 * h.w, h.w, G, Q);
+            }
+            accum_pair(dx, dy, dz, G, Q, g, u0, jq0, w0);
+        }
+        {
+            const float dx = to1.x - h.x, dy = to1.y - h.y, dz = to1.z - h.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float G, Q;
+            if constexpr (singular_tail<K>()) {
+                const float rs = frsqrt(r2);
+                const float rs2 = rs * rs;
+                G = rs * rs2;
+                Q = G * rs2;
+            } else {
+                near_GQ<K>(r2 * h.w, h.w, G, Q);
+            }
+            accum_pair(dx, dy, dz, G, Q, g, u1, jq1, w1);
+        }
+    }
+}
+
 // Full form of four sources j0..j0+3, per pair, with the displacement from the
 // double-float positions (th + tl) - (a + b); r == 0 contributes nothing.
 // off[].w as in pair4_far.
