@@ -25,6 +25,7 @@ namespace vpm {
 constexpr int NF_WARPS = 4;                  // warp groups per block
 constexpr int NF_THREADS = 32 * NF_WARPS;
 constexpr int NF_BLK_TILES = 2;              // 32-source tiles summed in FP32 per block
+constexpr int NF_ESTR_FLUSH = 8;             // nf_estr: tiles of compensated FP32 sums between FP64 adds
 constexpr int NF_MID_BLKS = 4;               // blocks summed in FP32 before the FP64 add
 #ifndef VPM_NF_MIN_BLOCKS
 #define VPM_NF_MIN_BLOCKS 4                  // resident blocks per SM the UJ kernel is compiled for
@@ -1018,7 +1019,8 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
     const float3 tl = make_float3((float)(me.tx - (double)th.x), (float)(me.ty - (double)th.y),
                                   (float)(me.tz - (double)th.z));
     double zg[3] = {0.0, 0.0, 0.0}, zv[3] = {0.0, 0.0, 0.0};
-    // mixed: compensated FP32 sums of 8-source partial sums (comp_add), FP64 every NF_BLK_TILES tiles
+    // mixed: compensated FP32 sums of 8-source partial sums (comp_add), FP64 every NF_ESTR_FLUSH tiles
+    // (as the all-pairs mixed Estr; the FP64 pipe runs at 1/64 of the FP32 rate)
     float sg[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
     int tiles = 0;
     IntervalWalk walk;
@@ -1075,7 +1077,7 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
 #pragma unroll
                 for (int k = 0; k < 3; k++) { comp_add(sg[k], cg[k], fg[k]); comp_add(sv[k], cv[k], fv[k]); }
             }
-            if (++tiles == NF_BLK_TILES) {
+            if (++tiles == NF_ESTR_FLUSH) {
                 tiles = 0;
 #pragma unroll
                 for (int k = 0; k < 3; k++) {

@@ -47,6 +47,22 @@ def test_library_exports_every_declared_symbol(lib):
         assert f in L.SIGNATURES, f"{f} has no ctypes signature in vpm_gb300._lib"
 
 
+def test_work_constants_agree():
+    """The flop-per-pair constants of the header are the ones the Python binding and the bench use."""
+    import importlib.util
+    import vpm_gb300._lib as L
+    src = open(HEADER).read()
+    defs = {k: int(v) for k, v in re.findall(r"#define\s+VPM_(FLOP_PER_\w+)\s+(\d+)", src)}
+    assert defs == {"FLOP_PER_UJ_PAIR": 74, "FLOP_PER_ESTR_PAIR": 25, "FLOP_PER_UJ_ADJ_PAIR": 186}
+    for k, v in defs.items():
+        assert getattr(L, k) == v, k
+    spec = importlib.util.spec_from_file_location("bench_consts", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench.FLOP_PER_PAIR == defs["FLOP_PER_UJ_PAIR"]
+    assert bench.FLOP_PER_ADJ_PAIR == defs["FLOP_PER_UJ_ADJ_PAIR"]
+
+
 def test_abi_version_and_build_info(lib):
     assert lib.vpm_abi_version() == 1
     assert b"sm_103a" in lib.vpm_build_info()
