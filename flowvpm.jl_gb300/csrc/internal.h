@@ -31,11 +31,6 @@ struct __align__(16) SrcMixed { float4 a, b, gam; };
 // Packed source of the FP64 UJ kernel, 64 B.
 struct __align__(16) SrcF64 { double2 xy, z_isig, gxy, gz_sig; };
 
-// Packed source of the mixed Estr kernels, 64 B: FP64 position, 1/sigma^2,
-// g = ZNORM Gamma / sigma^3 and v = ZNORM (J^T Gamma) / sigma^3 (or J Gamma), in
-// FP32; g = v = 0 for static sources.
-struct __align__(16) SrcEstrMixed { double x, y, z; float isig2, pad; float4 g; float4 v; };
-
 // Packed source of the all-pairs and near-field mixed Estr kernels, 64 B:
 // position as a double-float (a.xyz + b.xyz), a.w = 1/sigma^2,
 // g = ZNORM Gamma / sigma^3 and v = ZNORM (J^T Gamma) / sigma^3 (or J Gamma), in

@@ -132,14 +132,16 @@ __global__ void leaf_pack_estr(int64_t n, const double* __restrict__ x, const do
         }
     }
     const double isig = 1.0 / sgs[i];
-    if (precision) {
+    if (precision) {   // the position as a double-float, so that the kernel's staging is plain loads
         const double k = off ? 0.0 : zeta_norm(K) * isig * isig * isig;
-        SrcEstrMixed p;
-        p.x = x[3 * i]; p.y = x[3 * i + 1]; p.z = x[3 * i + 2];
-        p.isig2 = (float)(isig * isig); p.pad = 0.f;
+        const double px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+        const float xh = (float)px, yh = (float)py, zh = (float)pz;
+        SrcEstrDF p;
+        p.a = make_float4(xh, yh, zh, (float)(isig * isig));
+        p.b = make_float4((float)(px - (double)xh), (float)(py - (double)yh), (float)(pz - (double)zh), 0.f);
         p.g = make_float4((float)(k * gx), (float)(k * gy), (float)(k * gz), 0.f);
         p.v = make_float4((float)(k * vx), (float)(k * vy), (float)(k * vz), 0.f);
-        ((SrcEstrMixed*)out)[o] = p;
+        ((SrcEstrDF*)out)[o] = p;
     } else {
         const double m = off ? 0.0 : 1.0;
         SrcEstrF64 p;
@@ -1033,11 +1035,9 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
         __syncwarp();
         if constexpr (MIXED) {
             if (sp >= 0) {
-                const SrcEstrMixed p = ((const SrcEstrMixed*)srcv)[sp];
-                const float xh = (float)p.x, yh = (float)p.y, zh = (float)p.z;
-                mtile[warp][0][lane] = make_float4(xh, yh, zh, p.isig2);
-                mtile[warp][1][lane] = make_float4((float)(p.x - (double)xh), (float)(p.y - (double)yh),
-                                                   (float)(p.z - (double)zh), 0.f);
+                const SrcEstrDF p = ((const SrcEstrDF*)srcv)[sp];
+                mtile[warp][0][lane] = p.a;
+                mtile[warp][1][lane] = p.b;
                 mtile[warp][2][lane] = p.g;
                 mtile[warp][3][lane] = p.v;
             } else {   // padding: far away, no payload (read by the unrolled sub-blocks with mask 0)
@@ -1127,7 +1127,7 @@ nf_estr(int64_t n, int64_t ngroups, const TgtPos* __restrict__ tgt, const int32_
 size_t leaf_work_bytes(int64_t n)
 {
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t src = sizeof(SrcEstrMixed) > sizeof(SrcEstrF64) ? sizeof(SrcEstrMixed) : sizeof(SrcEstrF64);
+    const size_t src = sizeof(SrcEstrDF) > sizeof(SrcEstrF64) ? sizeof(SrcEstrDF) : sizeof(SrcEstrF64);
     return al(n * sizeof(TgtPos)) + al(n * src);
 }
 
