@@ -258,11 +258,19 @@ constexpr int BLOCK_TILES = UJ_BLOCK / WT;  // warp tiles per FP32 block
 // FP32 blocks per FP32 mid-level sum: 16 x 64 sources between FP64 adds (4 measured 1.2 %
 // slower -- the FP64 pipe runs at 1/64 rate -- with the same U, J error against the oracle)
 constexpr int MID_BLOCKS = 16;
-#ifndef VPM_UJ_MIN_BLOCKS
-// resident blocks per SM the register budget targets: 6 (80 registers) measured 0.9 % faster
-// than 7 (72 registers, a few spills) at N = 2^20 with the per-tile far flags
-#define VPM_UJ_MIN_BLOCKS 6
+// Resident blocks per SM the register budget targets, per kernel: at N = 2^20 with the
+// per-tile far flags, Gaussian-erf ran 1360 ms a launch at 5 (96 registers), 1400 at 6
+// (80) and 1408 at 7 (72, a few spills); Winckelmans, whose far form is its full form,
+// 1522 at 5 and 1503 at 6.  -DVPM_UJ_MIN_BLOCKS=n sets one budget for every kernel.
+template <int K>
+__host__ __device__ constexpr int uj_min_blocks()
+{
+#ifdef VPM_UJ_MIN_BLOCKS
+    return VPM_UJ_MIN_BLOCKS;
+#else
+    return K == K_WNKLMNS ? 6 : 5;
 #endif
+}
 #ifndef VPM_UJ_UNROLL
 #define VPM_UJ_UNROLL 2                     // 4-source groups unrolled per iteration of a tile
 #endif
@@ -290,7 +298,7 @@ constexpr int UJ_UNROLL = VPM_UJ_UNROLL;
 // Each warp streams the sources on its own: 32 per tile, double-buffered with
 // cp.async, so warps never wait for each other (no block-wide barrier).
 template <int K>
-__global__ void __launch_bounds__(UJ_THREADS, VPM_UJ_MIN_BLOCKS)
+__global__ void __launch_bounds__(UJ_THREADS, uj_min_blocks<K>())
 uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
                 const SrcMixed* __restrict__ src, int64_t per_split, double* U, int64_t ldU,
                 double* J, int64_t ldJ, double* partial, int64_t nt_pad)
