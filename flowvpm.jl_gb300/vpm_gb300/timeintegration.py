@@ -479,12 +479,21 @@ def _kernel_compatibility(viscous) -> tuple:
 
 
 def run_vpm(pfield: ParticleField, dt: float, nsteps: int, *, runtime_function=None,
-            static_particles_function=None, custom_UJ=None):
-    """The stepping loop of run_vpm! (src/FLOWVPM_utils.jl:41-136) without I/O:
-    the kernel/viscous-scheme check, relaxation every nsteps_relax steps, static
+            static_particles_function=None, custom_UJ=None, save_path=None, save_pfield: bool = True,
+            create_savepath: bool = True, run_name: str = "pfield", nsteps_save: int = 1,
+            save_time: bool = True):
+    """The stepping loop of run_vpm! (src/FLOWVPM_utils.jl:41-136): the
+    kernel/viscous-scheme check, relaxation every nsteps_relax steps, static
     particles added by static_particles_function(pfield, t, dt) before each step
-    and removed after it (unless it returns False), and runtime_function(pfield,
-    t, dt) after each step, which ends the run by returning True."""
+    and removed after it (unless it returns False), runtime_function(pfield, t,
+    dt) after each step, which ends the run by returning True, and, with a
+    save_path, the field saved by vpm_gb300.io.save at step 0, every nsteps_save
+    steps, at the last step and at a runtime stop (:122-126; save_time=False
+    stamps the files with nt instead of t).  Verbose output and the settings
+    file are not written."""
+    if save_path is not None and save_pfield and create_savepath:
+        import os
+        os.makedirs(save_path, exist_ok=True)
     if not any(pfield.kernel is k for k in _kernel_compatibility(pfield.viscous)):
         raise ValueError(f"Kernel {pfield.kernel} is not compatible with viscous scheme "
                          f"{type(pfield.viscous).__name__}; compatible kernels are "
@@ -500,5 +509,10 @@ def run_vpm(pfield: ParticleField, dt: float, nsteps: int, *, runtime_function=N
             if remove is None or remove:
                 for pi in range(pfield.np - 1, org_np - 1, -1):
                     pfield.remove_particle(pi)
-        if runtime_function is not None and runtime_function(pfield, pfield.t, dt):
+        breakflag = bool(runtime_function is not None and runtime_function(pfield, pfield.t, dt))
+        if save_pfield and save_path is not None and (i % nsteps_save == 0 or i == nsteps or breakflag):
+            from . import io as vio
+            vio.save(pfield, run_name, path=save_path, add_num=True,
+                     overwrite_time=None if save_time else pfield.nt)
+        if breakflag:
             break
