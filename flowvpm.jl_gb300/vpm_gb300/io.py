@@ -1,19 +1,17 @@
 """Particle-field files: the reference's `save` and `read!` (src/FLOWVPM_utils.jl:148-371,
-494-571), with the datasets in a raw binary file instead of HDF5.
+494-571), writing and reading the same files.
 
-The reference writes, per saved step, `<name>.<nt>.h5` (the scalars np, nt, t and the datasets
-X, Gamma, sigma, circulation, vol, static, velocity, velocity_gradient_x/y/z, vorticity and,
-with an SFS model, C; :179-221) and `<name>.<nt>.xmf`, an XDMF 3 description of the same
-datasets for ParaView (:256-370). No HDF5 library exists to this package, so `save` writes the
-same XDMF, element for element and name for name, with every DataItem pointing into one raw
-little-endian binary file `<name>.<nt>.bin` (`Format="Binary"`, a byte offset in `Seek`)
-instead of `<name>.<nt>.h5:/<dataset>`; the scalars np, nt and t also go into `Information`
-elements of the grid. ParaView's XDMF reader takes binary DataItems as it takes HDF ones.
-`read` is `read!` for these files (the reference's `read!` itself reads only `.h5`).
+Per saved step the reference writes `<name>.<nt>.h5` through HDF5.jl (:175-221): the scalar
+datasets np, nt (int64) and t, and the float64 arrays X, Gamma, sigma, circulation, vol, static,
+velocity, velocity_gradient_x/y/z, vorticity and, with an SFS model, C. Beside it,
+`<name>.<nt>.xmf` is an XDMF 3 description of the same datasets for ParaView (:256-370). `save`
+writes both, dataset for dataset and element for element, with `vpm_gb300.h5` (an HDF5 writer of
+the original file format, which needs no HDF5 library). `read` is `read!`.
 
-Array layout, as in the reference's HDF5 datasets: a 3-component field is np x 3 in C order
-(each particle's three values contiguous), a scalar field is np values; FP64 throughout, and
-`static` as 64-bit integers (the reference's XDMF declares it `Int`, precision 8).
+Array layout, as HDF5.jl stores the reference's Julia matrices: a 3-component field is an
+np x 3 dataset in C order (each particle's three values contiguous), a scalar field np values.
+`static` is float64, as the reference writes the particle matrix's row; its XDMF item still says
+`Int`, as the reference's does.
 """
 from __future__ import annotations
 
@@ -22,6 +20,7 @@ import xml.etree.ElementTree as ET
 
 import numpy as np
 
+from . import h5
 from .particlefield import (C_INDEX, CIRCULATION_INDEX, GAMMA_INDEX, J_INDEX, SIGMA_INDEX, STATIC_INDEX,
                             U_INDEX, VOL_INDEX, VORTICITY_INDEX, X_INDEX, ParticleField)
 
@@ -38,17 +37,17 @@ _SCALARS = (("sigma", "sigma", SIGMA_INDEX),
             ("vol", "vol", VOL_INDEX))
 
 
-def _data_item(parent, dims, offset: int, binname: str, dtype: str = "Float"):
-    el = ET.SubElement(parent, "DataItem", {"DataType": dtype, "Dimensions": dims, "Format": "Binary",
-                                             "Endian": "Little", "Precision": "8", "Seek": str(offset)})
-    el.text = binname
+def _data_item(parent, dims, h5fname: str, dataset: str, dtype: str = "Float"):
+    el = ET.SubElement(parent, "DataItem", {"DataType": dtype, "Dimensions": dims, "Format": "HDF",
+                                             "Precision": "8"})
+    el.text = f"{h5fname}:{dataset}"
     return el
 
 
 def save(pfield: ParticleField, file_name: str, *, path: str = "", add_num: bool = True, num: int = -1,
          createpath: bool = False, overwrite_time=None) -> str:
     """`save(pfield, file_name; path, add_num, num, createpath, overwrite_time)`,
-    src/FLOWVPM_utils.jl:148-371: writes `<file_name>.<nt>.xmf` and `<file_name>.<nt>.bin`
+    src/FLOWVPM_utils.jl:148-371: writes `<file_name>.<nt>.h5` and `<file_name>.<nt>.xmf`
     (`.<num>` when num >= 0, no number with add_num=False) and returns "<fname>.xmf;".
     An empty field is saved as one particle at the origin with zero strength and core
     size, as the reference does (:156-165)."""
@@ -60,53 +59,41 @@ def save(pfield: ParticleField, file_name: str, *, path: str = "", add_num: bool
     if createpath and path:
         os.makedirs(path, exist_ok=True)
     fname = file_name + ((f".{pfield.nt}" if num == -1 else f".{num}") if add_num else "")
-    binname = fname + ".bin"
+    h5fname = fname + ".h5"
     n = pfield.get_np()
-    time = float(overwrite_time) if overwrite_time is not None else float(pfield.t)
+    time = overwrite_time if overwrite_time is not None else pfield.t
+    time = int(time) if isinstance(time, (int, np.integer)) else float(time)   # an int stays int64
     P = pfield.particles
 
-    # the datasets, in the reference's order, and their byte offsets
-    blocks, offsets, off = [], {}, 0
-
-    def put(name, arr):
-        nonlocal off
-        a = np.ascontiguousarray(arr)
-        offsets[name] = off
-        blocks.append(a.astype("<f8" if a.dtype.kind == "f" else "<i8", copy=False).tobytes())
-        off += len(blocks[-1])
-    put("X", P[X_INDEX, :n].T)
-    put("Gamma", P[GAMMA_INDEX, :n].T)
-    put("sigma", P[SIGMA_INDEX, :n])
-    put("circulation", P[CIRCULATION_INDEX, :n])
-    put("vol", P[VOL_INDEX, :n])
-    put("static", P[STATIC_INDEX, :n].astype(np.int64))
-    for ds, _, rows in _VECTORS[1:]:
-        put(ds, P[rows, :n].T)
+    # the datasets of src/FLOWVPM_utils.jl:179-221, in its order
+    ds = {"np": int(n), "nt": int(pfield.nt),
+          "t": time,
+          "X": P[X_INDEX, :n].T, "Gamma": P[GAMMA_INDEX, :n].T, "sigma": P[SIGMA_INDEX, :n],
+          "circulation": P[CIRCULATION_INDEX, :n], "vol": P[VOL_INDEX, :n],
+          "static": P[STATIC_INDEX, :n]}
+    for name, _, rows in _VECTORS[1:]:
+        ds[name] = P[rows, :n].T
     les = pfield.isLES()
     if les:
-        put("C", P[C_INDEX, :n].T)
-    with open(os.path.join(path, binname), "wb") as f:
-        for b in blocks:
-            f.write(b)
+        ds["C"] = P[C_INDEX, :n].T
+    h5.write(os.path.join(path, h5fname), ds)
 
-    # the XDMF of src/FLOWVPM_utils.jl:256-370, binary DataItems
+    # the XDMF of src/FLOWVPM_utils.jl:256-370
     xdmf = ET.Element("Xdmf", {"xmlns:xi": "http://www.w3.org/2001/XInclude", "Version": "3.0"})
     dom = ET.SubElement(xdmf, "Domain")
     grid = ET.SubElement(dom, "Grid", {"Name": "particles", "GridType": "Uniform"})
-    for k, v in (("np", n), ("nt", pfield.nt), ("t", repr(time))):
-        ET.SubElement(grid, "Information", {"Name": k, "Value": str(v)})
     ET.SubElement(grid, "Time", {"Value": repr(time)})
     geo = ET.SubElement(grid, "Geometry", {"Type": "XYZ"})
-    _data_item(geo, f"{n} 3", offsets["X"], binname)
+    _data_item(geo, f"{n} 3", h5fname, "X")
     ET.SubElement(grid, "Topology", {"Dimensions": str(n), "Type": "Polyvertex"})
 
-    def attribute(ds, name, typ, dims, dtype="Float"):
+    def attribute(dataset, name, typ, dims, dtype="Float"):
         at = ET.SubElement(grid, "Attribute", {"Center": "Node", "Name": name, "Type": typ})
-        _data_item(at, dims, offsets[ds], binname, dtype)
-    for ds, name, _ in _VECTORS:
-        attribute(ds, name, "Vector", f"{n} 3")
-    for ds, name, _ in _SCALARS:
-        attribute(ds, name, "Scalar", str(n))
+        _data_item(at, dims, h5fname, dataset, dtype)
+    for dataset, name, _ in _VECTORS:
+        attribute(dataset, name, "Vector", f"{n} 3")
+    for dataset, name, _ in _SCALARS:
+        attribute(dataset, name, "Scalar", str(n))
     attribute("static", "static", "Scalar", str(n), "Int")
     if les:
         attribute("C", "C", "Vector", f"{n} 3")
@@ -145,42 +132,41 @@ def save_device(fld, file_name: str, *, les: bool = False, circulation=None, sta
 
 
 def _datasets(xmf_path: str):
-    """{dataset name: numpy array} and the grid's Information values of a file of `save`."""
+    """{dataset name: numpy array} of the DataItems of an XDMF file of `save`, each read from the
+    `<file>.h5:<dataset>` it names."""
     root = ET.parse(xmf_path).getroot()
-    grid = root.find("Domain/Grid")
-    info = {el.get("Name"): el.get("Value") for el in grid.findall("Information")}
     base = os.path.dirname(xmf_path)
-    names = {name: ds for ds, name, _ in _VECTORS + _SCALARS}
-    names.update({"static": "static", "C": "C"})
-    items = [("X", grid.find("Geometry/DataItem"))]
-    items += [(names[at.get("Name")], at.find("DataItem")) for at in grid.findall("Attribute")]
     out = {}
-    for ds, item in items:
-        dims = [int(d) for d in item.get("Dimensions").split()]
-        dtype = "<f8" if item.get("DataType") == "Float" else "<i8"
-        with open(os.path.join(base, item.text.strip()), "rb") as f:
-            f.seek(int(item.get("Seek", "0")))
-            a = np.frombuffer(f.read(8 * int(np.prod(dims))), dtype=dtype)
-        out[ds] = a.reshape(dims)
-    return out, info
+    for item in root.iter("DataItem"):
+        fname, dataset = item.text.strip().rsplit(":", 1)
+        a = h5.read(os.path.join(base, fname), [dataset])[dataset]
+        dims = tuple(int(d) for d in item.get("Dimensions").split())
+        if a.shape != dims:
+            raise ValueError(f"{fname}:{dataset} has shape {a.shape}, the XDMF says {dims}")
+        out[dataset] = a
+    return out
 
 
-def read(pfield: ParticleField, fname: str, *, path: str = "", overwrite: bool = True,
+def read(pfield: ParticleField, h5_fname: str, *, path: str = "", overwrite: bool = True,
          load_time: bool = True) -> ParticleField:
-    """`read!(pfield, fname; path, overwrite, load_time)`, src/FLOWVPM_utils.jl:494-571, for a
-    file of `save`: loads X, Gamma, sigma, vol, circulation, static (if present) and C (else
-    zero) after the field's particles (or in their place with overwrite), and the time stamp."""
+    """`read!(pfield, h5_fname; path, overwrite, load_time)`, src/FLOWVPM_utils.jl:494-571: loads
+    X, Gamma, sigma, vol, circulation, static (if present, else 0) and C (if present, else 0) of
+    `<h5_fname>.h5` after the field's particles (in their place with overwrite), and its time
+    stamp t, nt with load_time."""
     if overwrite:
         pfield.np = 0
-    xmf = fname if fname.endswith(".xmf") else fname + ".xmf"
-    data, info = _datasets(os.path.join(path, xmf))
-    n = int(info["np"])
+    h5fname = h5_fname if h5_fname.endswith(".h5") else h5_fname + ".h5"
+    fpath = os.path.join(path, h5fname)
+    names = h5.keys(fpath)
+    want = ["np", "t", "nt", "X", "Gamma", "sigma", "vol", "circulation"]
+    data = h5.read(fpath, want + [k for k in ("static", "C") if k in names])
+    n = int(data["np"])
     if pfield.np + n > pfield.maxparticles:
-        raise RuntimeError(f"The field to be read ({fname}) contains {n} particles but max number of "
+        raise RuntimeError(f"The field to be read ({h5_fname}) contains {n} particles but max number of "
                            f"particles is {pfield.maxparticles}.")
     if load_time:
-        pfield.t = float(info["t"])
-        pfield.nt = int(info["nt"])
+        pfield.t = data["t"].item()
+        pfield.nt = int(data["nt"])
     sl = slice(pfield.np, pfield.np + n)
     P = pfield.particles
     P[X_INDEX, sl] = data["X"].T
@@ -188,7 +174,13 @@ def read(pfield: ParticleField, fname: str, *, path: str = "", overwrite: bool =
     P[SIGMA_INDEX, sl] = data["sigma"]
     P[VOL_INDEX, sl] = data["vol"]
     P[CIRCULATION_INDEX, sl] = data["circulation"]
-    P[STATIC_INDEX, sl] = data["static"].astype(np.float64) if "static" in data else 0.0
+    if "static" in data:
+        st = data["static"]
+        if not np.all((st == 0) | (st == 1)):           # the reference converts them to Bool
+            raise ValueError(f"static flags of {h5_fname} other than 0 and 1")
+        P[STATIC_INDEX, sl] = st.astype(np.float64)
+    else:
+        P[STATIC_INDEX, sl] = 0.0
     P[C_INDEX, sl] = data["C"].T if "C" in data else 0.0
     pfield.np += n
     return pfield

@@ -1,5 +1,6 @@
-"""Particle-field files (vpm_gb300.io): the reference's save / read! (src/FLOWVPM_utils.jl:148-371,
-494-571) with the XDMF the reference writes and a raw binary file in place of HDF5. CPU only."""
+"""Particle-field files (vpm_gb300.io, vpm_gb300.h5): the reference's save / read!
+(src/FLOWVPM_utils.jl:148-371, 494-571), the .h5 and .xmf files it writes, and the HDF5 subset
+those use. CPU only."""
 import os
 import xml.etree.ElementTree as ET
 
@@ -31,7 +32,7 @@ def test_save_read_round_trip(tmp_path, les):
     pf = _field(257, les=les)
     out = vio.save(pf, "field", path=str(tmp_path))
     assert out == "field.17.xmf;"
-    assert os.path.exists(tmp_path / "field.17.xmf") and os.path.exists(tmp_path / "field.17.bin")
+    assert os.path.exists(tmp_path / "field.17.xmf") and os.path.exists(tmp_path / "field.17.h5")
     back = vpm.ParticleField(300)
     vio.read(back, "field.17", path=str(tmp_path))
     n = pf.np
@@ -60,39 +61,109 @@ def test_xdmf_follows_the_reference_layout(tmp_path):
                      ("velocity gradient y", "Vector"), ("velocity gradient z", "Vector"),
                      ("vorticity", "Vector"), ("sigma", "Scalar"), ("circulation", "Scalar"),
                      ("vol", "Scalar"), ("static", "Scalar"), ("C", "Vector")]
+    datasets = {"Gamma": "Gamma", "velocity gradient x": "velocity_gradient_x", "velocity": "velocity",
+                "velocity gradient y": "velocity_gradient_y", "velocity gradient z": "velocity_gradient_z"}
+    assert grid.find("Geometry/DataItem").text == "f.3.h5:X"
     for a in grid.findall("Attribute"):
         item = a.find("DataItem")
-        assert item.get("Format") == "Binary" and item.get("Precision") == "8"
+        assert item.get("Format") == "HDF" and item.get("Precision") == "8"
         assert item.get("DataType") == ("Int" if a.get("Name") == "static" else "Float")
-        assert item.text == "f.3.bin"
+        assert item.text == "f.3.h5:" + datasets.get(a.get("Name"), a.get("Name"))
+    # every item names a dataset of the .h5 file with the shape the item declares
+    data = vio._datasets(str(tmp_path / "f.3.xmf"))
+    assert len(data) == 12
 
 
-def test_binary_datasets_at_their_offsets(tmp_path):
+def test_h5_datasets_as_the_reference_writes_them(tmp_path):
+    """The .h5 holds the datasets of src/FLOWVPM_utils.jl:179-221 with HDF5.jl's types and
+    shapes: np and nt int64 scalars, t a float64 scalar, the fields float64 (np x 3 or np)."""
     pf = _field(33)
     vio.save(pf, "g", path=str(tmp_path), add_num=False)
-    raw = (tmp_path / "g.bin").read_bytes()
-    grid = ET.parse(tmp_path / "g.xmf").getroot().find("Domain/Grid")
+    from vpm_gb300 import h5
+    names = h5.keys(str(tmp_path / "g.h5"))
+    assert sorted(names) == sorted(["np", "nt", "t", "X", "Gamma", "sigma", "circulation", "vol", "static",
+                                    "velocity", "velocity_gradient_x", "velocity_gradient_y",
+                                    "velocity_gradient_z", "vorticity"])          # no C without SFS
+    d = h5.read(str(tmp_path / "g.h5"))
     n = pf.np
-
-    def at(name):
-        item = (grid.find("Geometry/DataItem") if name == "X" else
-                next(a for a in grid.findall("Attribute") if a.get("Name") == name).find("DataItem"))
-        dims = [int(d) for d in item.get("Dimensions").split()]
-        off = int(item.get("Seek"))
-        dt = "<f8" if item.get("DataType") == "Float" else "<i8"
-        return np.frombuffer(raw[off:off + 8 * int(np.prod(dims))], dtype=dt).reshape(dims)
+    assert d["np"].shape == () and d["np"].dtype == np.int64 and d["np"] == n
+    assert d["nt"].dtype == np.int64 and d["nt"] == 17
+    assert d["t"].shape == () and d["t"].dtype == np.float64 and d["t"] == 0.085
     P = pf.particles
-    np.testing.assert_array_equal(at("X"), P[0:3, :n].T)
-    np.testing.assert_array_equal(at("velocity gradient y"), P[J_INDEX.start + 3:J_INDEX.start + 6, :n].T)
-    np.testing.assert_array_equal(at("vorticity"), P[VORTICITY_INDEX, :n].T)
-    np.testing.assert_array_equal(at("static"), P[STATIC_INDEX, :n].astype(np.int64))
-    assert len(raw) == 8 * n * (3 * 7 + 4)      # X, 6 vector attributes, 4 scalars; no C without SFS
+    np.testing.assert_array_equal(d["X"], P[0:3, :n].T)
+    np.testing.assert_array_equal(d["velocity_gradient_y"], P[J_INDEX.start + 3:J_INDEX.start + 6, :n].T)
+    np.testing.assert_array_equal(d["vorticity"], P[VORTICITY_INDEX, :n].T)
+    assert d["static"].dtype == np.float64
+    np.testing.assert_array_equal(d["static"], P[STATIC_INDEX, :n])
+
+
+def test_h5_reader_reads_a_libhdf5_file():
+    """The reader against a file libhdf5 wrote: scipy's MATLAB 7.3 test file (HDF5 after a
+    512-byte user block) holds `testdouble` = pi/4 * (0..8), the value scipy's own MATLAB tests
+    expect of it."""
+    import scipy.io.matlab
+    from vpm_gb300 import h5
+    f = os.path.join(os.path.dirname(scipy.io.matlab.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    if not os.path.exists(f):
+        pytest.skip("scipy's HDF5 test file is not installed")
+    d = h5.read(f)
+    assert list(d) == ["testdouble"] and d["testdouble"].shape == (9, 1)
+    np.testing.assert_array_equal(d["testdouble"].ravel(), np.pi / 4 * np.arange(9.0))
+
+
+def test_h5_encodings_match_libhdf5(tmp_path):
+    """The float64 datatype and fill-value messages written here are byte for byte the ones
+    libhdf5 wrote for a float64 dataset (scipy's MATLAB 7.3 test file)."""
+    import scipy.io.matlab
+    from vpm_gb300 import h5
+    f = os.path.join(os.path.dirname(scipy.io.matlab.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    if not os.path.exists(f):
+        pytest.skip("scipy's HDF5 test file is not installed")
+    ref = h5._File(open(f, "rb").read())
+    ref_msgs = dict(ref.messages(ref.group(ref.root_ohdr, ref.root_cache)["testdouble"]))
+    h5.write(str(tmp_path / "x.h5"), {"a": np.zeros(3)})
+    ours = h5._File(open(tmp_path / "x.h5", "rb").read())
+    msgs = dict(ours.messages(ours.group(ours.root_ohdr, ours.root_cache)["a"]))
+    assert msgs[h5.MSG_DATATYPE] == ref_msgs[h5.MSG_DATATYPE]
+    assert msgs[h5.MSG_FILL] == ref_msgs[h5.MSG_FILL]
+
+
+def test_h5_file_structure(tmp_path):
+    """The invariants libhdf5 relies on when it opens a file: the superblock's end-of-file
+    address is the file size, the heap's free list is empty, every symbol-table node holds at
+    most 2 x 4 names in byte order, and B-tree key i+1 is the last name of child i."""
+    from vpm_gb300 import h5
+    rng = np.random.default_rng(1)
+    names = [f"d{i:02d}" for i in range(19)] + ["np", "X", "velocity_gradient_x"]
+    h5.write(str(tmp_path / "s.h5"), {k: rng.normal(size=(i + 1,)) for i, k in enumerate(names)})
+    raw = (tmp_path / "s.h5").read_bytes()
+    f = h5._File(raw)
+    assert int.from_bytes(raw[40:48], "little") == len(raw)
+    tree, heap = f.root_cache
+    assert raw[heap:heap + 4] == b"HEAP" and int.from_bytes(raw[heap + 16:heap + 24], "little") == h5.HEAP_FREE_NULL
+    hdata = int.from_bytes(raw[heap + 24:heap + 32], "little")
+    name = lambda off: raw[hdata + off:raw.index(b"\0", hdata + off)]
+    used = int.from_bytes(raw[tree + 6:tree + 8], "little")
+    assert used == 3
+    keys = [int.from_bytes(raw[tree + 24 + 16 * i:tree + 32 + 16 * i], "little") for i in range(used + 1)]
+    kids = [int.from_bytes(raw[tree + 32 + 16 * i:tree + 40 + 16 * i], "little") for i in range(used)]
+    assert name(keys[0]) == b""
+    seen = []
+    for i, k in enumerate(kids):
+        assert raw[k:k + 4] == b"SNOD"
+        ns = int.from_bytes(raw[k + 6:k + 8], "little")
+        assert 1 <= ns <= 8
+        child = [name(int.from_bytes(raw[k + 8 + 40 * e:k + 16 + 40 * e], "little")) for e in range(ns)]
+        assert child == sorted(child) and name(keys[i + 1]) == child[-1]
+        seen += child
+    assert seen == sorted(n.encode() for n in names)
+    assert sorted(h5.keys(str(tmp_path / "s.h5"))) == sorted(names)
 
 
 def test_empty_field_saves_one_dummy_particle(tmp_path):
     pf = vpm.ParticleField(10, nt=4, t=0.5)
     vio.save(pf, "e", path=str(tmp_path))
-    back = vio.read(vpm.ParticleField(2), "e.4", path=str(tmp_path))
+    back = vio.read(vpm.ParticleField(2), "e.4.h5", path=str(tmp_path))
     assert back.np == 1 and back.nt == 4 and back.t == 0.5
     np.testing.assert_array_equal(back.particles[0:7, 0], 0.0)
 
@@ -104,7 +175,7 @@ def test_read_overflow_and_append(tmp_path):
         vio.read(vpm.ParticleField(19), "h.17", path=str(tmp_path))
     two = vpm.ParticleField(40)
     vio.read(two, "h.17", path=str(tmp_path))
-    vio.read(two, "h.17.xmf", path=str(tmp_path), overwrite=False, load_time=False)
+    vio.read(two, "h.17.h5", path=str(tmp_path), overwrite=False, load_time=False)
     assert two.np == 40
     np.testing.assert_array_equal(two.particles[0:9, 20:40], pf.particles[0:9, :20])
 
@@ -148,5 +219,5 @@ def test_save_device_state(tmp_path):
     np.testing.assert_array_equal(back.particles[3:6, :n], fld.gam.numpy().T)
     np.testing.assert_array_equal(back.particles[6, :n], fld.sig.numpy())
     np.testing.assert_array_equal(back.particles[C_INDEX, :n], fld.C.numpy().T)
-    data, _ = vio._datasets(str(tmp_path / "dev.9.xmf"))
+    data = vio._datasets(str(tmp_path / "dev.9.xmf"))
     np.testing.assert_array_equal(data["velocity_gradient_z"], fld.J.numpy()[:, 6:9])
