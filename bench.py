@@ -46,6 +46,12 @@ FLOP_PER_ADJ_PAIR = 186   # VPM_FLOP_PER_UJ_ADJ_PAIR
 # ~0.16 GB (56 B in, 96 B out a particle); the rest is re-reads of the 50 MB source pack that
 # miss L2.  Either way it is ~0.42 GB/s over the 1.41 s launch: the kernel is FP32-bound.
 UJ_DRAM_BYTES_2P20 = 405_746_944 + 181_722_112
+# (warp, 32-source tile) pairs within reach that one estr_mixed_kernel<gaussianerf> launch
+# loads on the 200,000-particle leapfrog rings: one cp.async commit (LDGDEPBAR) per loaded tile
+# in ncu's per-opcode counts of `python bench.py --kernel-only --estr --cloud rings --n 200000
+# --warmup 0 --steps 1` (2,967,977 commits, 4 LDGSTS each), of the 6,250 x 6,250 tile pairs.
+# The reach depends on the positions and core sizes only, which the workload fixes.
+ESTR_TILES_IN_REACH_RINGS200K = 2_967_977
 # the headline metric as the reference's benchmark definition names it; `value` is the
 # FP32-comp rate, `fp64_gpu` / `mixed_over_fp64` and `adjoint` carry the other two parts
 METRIC = "UJ pair-interactions/s, FP32-comp vs FP64 GPU @≤1e-6 rel err; adjoint/fwd ratio"
@@ -419,12 +425,19 @@ def rings_blocks(ctx, vpm, torch, peak_tflops):
     pairs = float(n) * n
     estr_tf = 25 * pairs / (ms_estr / 1e3) / 1e12
     uj_tf = FLOP_PER_PAIR * pairs / (ms_uj / 1e3) / 1e12
+    in_reach = ESTR_TILES_IN_REACH_RINGS200K * 32 * 32
     estr = {"workload": "leapfrog rings, 200,000 particles, FP32-comp", "n_particles": n, "ms": ms_estr,
             "pairs_per_s": pairs / (ms_estr / 1e3), "flop_per_pair": 25, "achieved_tflops": estr_tf,
-            "frac_of_ffma_peak": estr_tf / peak_tflops, "kernel": "estr_mixed_kernel<gaussianerf>",
+            "all_pair_slots_frac_of_ffma_peak": estr_tf / peak_tflops,
+            "tile_pairs_in_reach": in_reach,
+            "in_reach_frac_of_ffma_peak": 25 * in_reach / (ms_estr / 1e3) / 1e12 / peak_tflops,
+            "kernel": "estr_mixed_kernel<gaussianerf>",
             "uj_ms_same_field": ms_uj, "uj_frac_of_ffma_peak": uj_tf / peak_tflops,
-            "note": "all N^2 pair slots counted; tiles and 8-source sub-blocks whose every pair is past "
-                    "zeta/zeta(0) < 1e-13 are skipped (their terms are below FP32 resolution)"}
+            "note": "pairs_per_s and all_pair_slots_frac count all N^2 pair slots, as the reference evaluates "
+                    "them; tiles and 8-source sub-blocks whose every pair is past zeta/zeta(0) < 1e-13 are "
+                    "skipped (their terms are below FP32 resolution), so that figure reads above 1. "
+                    "tile_pairs_in_reach = the 32 x 32 pair slots of the (warp, source tile) pairs the kernel "
+                    "loads (ncu count of one launch on this workload); in_reach_frac counts those at 25 flop"}
     fld = ds.DeviceField(x.clone(), g.clone(), sg.clone(), kernel=KERNEL, precision=vpm.FP32COMP)
     sfs = ds.DynamicSFSParams()
     visc = ds.CoreSpreadingParams(nu=1e-4, sgm0=0.05)
