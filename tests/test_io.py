@@ -221,3 +221,120 @@ def test_save_device_state(tmp_path):
     np.testing.assert_array_equal(back.particles[C_INDEX, :n], fld.C.numpy().T)
     data = vio._datasets(str(tmp_path / "dev.9.xmf"))
     np.testing.assert_array_equal(data["velocity_gradient_z"], fld.J.numpy()[:, 6:9])
+
+
+def _crafted_h5(path):
+    """A file that uses what the writer never writes but the reader reads: superblock version 1,
+    a two-level group B-tree (an internal node over two leaf nodes), a compact dataset, a
+    big-endian float64 and a big-endian int32 dataset, and a dataset whose object header continues
+    in a second chunk (a continuation message). Returns the expected {name: array}."""
+    import struct
+    from vpm_gb300 import h5
+    expect = {"a_compact": np.arange(5, dtype=np.float64) / 8,
+              "b_be_f64": np.linspace(-1, 1, 6).reshape(2, 3),
+              "c_be_i32": np.array([-7, 0, 9], dtype=np.int32),
+              "d_cont": np.array([3.25, -1.5])}
+    names = sorted(expect)
+    heap_data, off = b"\0" * 8, {}
+    for nm in names:
+        off[nm] = len(heap_data)
+        heap_data += nm.encode() + b"\0" * (h5._pad8(len(nm) + 1) - len(nm))
+    be_f64 = struct.pack("<B3BI HHBBBBI", 0x11, 0x21, 63, 0, 8, 0, 64, 52, 11, 0, 52, 1023)   # byte order bit set
+    be_i32 = struct.pack("<B3BI HH", 0x10, 0x09, 0, 0, 4, 0, 32)
+    le_f64 = h5._datatype_msg(np.dtype(np.float64))
+    sb, pos = 100, {}                      # superblock v1 is 100 bytes with 8-byte offsets
+    layout = ["root", "heap", "inner", "leaf0", "leaf1", "snod0", "snod1"] + names + ["cont", "data"]
+    sizes = {"root": 16 + 32, "heap": 32 + len(heap_data), "inner": h5._TREE_BYTES, "leaf0": h5._TREE_BYTES,
+             "leaf1": h5._TREE_BYTES, "snod0": h5._SNOD_BYTES, "snod1": h5._SNOD_BYTES}
+    data = {"b_be_f64": expect["b_be_f64"].astype(">f8").tobytes(), "c_be_i32": expect["c_be_i32"].astype(">i4").tobytes(),
+            "d_cont": expect["d_cont"].astype("<f8").tobytes()}
+    msgs = {}
+    msgs["a_compact"] = [(h5.MSG_DATATYPE, 1, le_f64), (h5.MSG_DATASPACE, 0, h5._dataspace_msg((5,))),
+                         (h5.MSG_LAYOUT, 1, struct.pack("<BBH", 3, 0, 40) + expect["a_compact"].tobytes())]
+    p = sb
+    for k in layout:
+        pos[k] = p
+        if k in names:
+            if k == "b_be_f64":
+                msgs[k] = [(h5.MSG_DATATYPE, 1, be_f64), (h5.MSG_DATASPACE, 0, h5._dataspace_msg((2, 3))),
+                           (h5.MSG_LAYOUT, 1, b"\0" * 18)]
+            elif k == "c_be_i32":
+                msgs[k] = [(h5.MSG_DATATYPE, 1, be_i32), (h5.MSG_DATASPACE, 0, h5._dataspace_msg((3,))),
+                           (h5.MSG_LAYOUT, 1, b"\0" * 18)]
+            elif k == "d_cont":
+                msgs[k] = [(h5.MSG_DATATYPE, 1, le_f64), (h5.MSG_CONTINUATION, 0, b"\0" * 16)]
+            sizes[k] = len(h5._object_header(msgs[k]))
+        elif k == "cont":
+            sizes[k] = 8 + 16 + 8 + 24               # the dataspace and layout messages of d_cont
+        elif k == "data":
+            sizes[k] = sum(len(v) for v in data.values())
+        p += sizes[k]
+    eof = p
+    dpos, q = {}, pos["data"]
+    for k in ("b_be_f64", "c_be_i32", "d_cont"):
+        dpos[k] = q
+        q += len(data[k])
+    for k in ("b_be_f64", "c_be_i32"):
+        msgs[k][2] = (h5.MSG_LAYOUT, 1, struct.pack("<BBQQ", 3, 1, dpos[k], len(data[k])))
+    msgs["d_cont"][1] = (h5.MSG_CONTINUATION, 0, struct.pack("<QQ", pos["cont"], sizes["cont"]))
+    out = bytearray(eof)
+    out[0:sb] = (h5.SIGNATURE + struct.pack("<8BHHI", 1, 0, 0, 0, 0, 8, 8, 0, 4, 16, 0) + struct.pack("<HH", 32, 0)
+                 + struct.pack("<QQQQ", 0, h5.UNDEF, eof, h5.UNDEF) + struct.pack("<QQII", 0, pos["root"], 0, 0) + b"\0" * 16)
+    root = h5._object_header([(h5.MSG_SYMTAB, 1, struct.pack("<QQ", pos["inner"], pos["heap"])), (h5.MSG_NIL, 0, b"")])
+    out[pos["root"]:pos["root"] + len(root)] = root
+    out[pos["heap"]:pos["heap"] + 32] = b"HEAP" + struct.pack("<B3xQQQ", 0, len(heap_data), 1, pos["heap"] + 32)
+    out[pos["heap"] + 32:pos["heap"] + 32 + len(heap_data)] = heap_data
+    groups = [names[:2], names[2:]]
+
+    def tree(level, kids, last_names):
+        node = b"TREE" + struct.pack("<BBHQQ", 0, level, len(kids), h5.UNDEF, h5.UNDEF) + struct.pack("<Q", 0)
+        for kid, nm in zip(kids, last_names):
+            node += struct.pack("<QQ", kid, off[nm])
+        return node
+    for at, node in ((pos["inner"], tree(1, [pos["leaf0"], pos["leaf1"]], [groups[0][-1], groups[1][-1]])),
+                     (pos["leaf0"], tree(0, [pos["snod0"]], [groups[0][-1]])),
+                     (pos["leaf1"], tree(0, [pos["snod1"]], [groups[1][-1]]))):
+        out[at:at + len(node)] = node
+    for g, at in zip(groups, (pos["snod0"], pos["snod1"])):
+        s = b"SNOD" + struct.pack("<BBH", 1, 0, len(g)) + b"".join(
+            struct.pack("<QQII16x", off[nm], pos[nm], 0, 0) for nm in g)
+        out[at:at + len(s)] = s
+    for nm in names:
+        hdr = h5._object_header(msgs[nm])
+        out[pos[nm]:pos[nm] + len(hdr)] = hdr
+    # d_cont: the prefix counts all 4 messages (the continuation included); the second chunk holds 2
+    struct.pack_into("<H", out, pos["d_cont"] + 2, 4)
+    chunk = h5._object_header([(h5.MSG_DATASPACE, 0, h5._dataspace_msg((2,))),
+                               (h5.MSG_LAYOUT, 1, struct.pack("<BBQQ", 3, 1, dpos["d_cont"], 16))])[16:]
+    out[pos["cont"]:pos["cont"] + len(chunk)] = chunk
+    for k in dpos:
+        out[dpos[k]:dpos[k] + len(data[k])] = data[k]
+    with open(path, "wb") as f:
+        f.write(out)
+    return expect
+
+
+def test_h5_reader_format_variants(tmp_path):
+    """Superblock 1, a two-level group B-tree, compact storage, big-endian types and an object
+    header continued in a second chunk read back to the values written."""
+    from vpm_gb300 import h5
+    expect = _crafted_h5(str(tmp_path / "v.h5"))
+    assert h5.keys(str(tmp_path / "v.h5")) == sorted(expect)
+    got = h5.read(str(tmp_path / "v.h5"))
+    for k, v in expect.items():
+        assert got[k].shape == v.shape and got[k].dtype == v.dtype.newbyteorder("="), k
+        np.testing.assert_array_equal(got[k], v)
+
+
+def test_h5_reader_rejects_what_it_does_not_read(tmp_path):
+    """A newer superblock and a non-HDF5 file raise, rather than read wrong values."""
+    from vpm_gb300 import h5
+    h5.write(str(tmp_path / "ok.h5"), {"a": np.zeros(2)})
+    raw = bytearray((tmp_path / "ok.h5").read_bytes())
+    raw[8] = 2                                            # superblock version 2
+    (tmp_path / "v2.h5").write_bytes(bytes(raw))
+    with pytest.raises(NotImplementedError):
+        h5.read(str(tmp_path / "v2.h5"))
+    (tmp_path / "no.h5").write_bytes(b"not an hdf5 file" * 4)
+    with pytest.raises(ValueError):
+        h5.read(str(tmp_path / "no.h5"))
