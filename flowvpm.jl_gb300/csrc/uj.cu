@@ -253,6 +253,43 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+#ifndef VPM_UJ_BULK
+// 1: one lane fills its warp's 1,536-byte source tile with a bulk copy (cp.async.bulk)
+// completed on an mbarrier, instead of 3 cp.async a lane (uj_mixed_kernel only).  Measured
+// at N = 2^20: the same U, J to every digit, but 3.4 % slower for Gaussian-erf (1394-1402 ms
+// a launch against 1352-1354) and 3.1 % for Winckelmans (1546-1548 against 1499-1502); not
+// profiled: each lane saves 2 copy instructions a tile and polls the barrier once instead.
+#define VPM_UJ_BULK 0
+#endif
+#if VPM_UJ_BULK
+constexpr int UJ_BULK_SPIN = 1 << 14;       // try_wait rounds before a wait gives up
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* m)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(m)) : "memory");
+}
+// bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) completing on m
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(m)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(m)) : "memory");
+}
+// true once the phase of m with this parity has completed; false after UJ_BULK_SPIN rounds
+__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity)
+{
+    for (int i = 0; i < UJ_BULK_SPIN; i++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done) : "r"(smem_addr(m)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+#endif
+
 constexpr int WT = 32;                      // sources per warp tile (one per lane)
 constexpr int BLOCK_TILES = UJ_BLOCK / WT;  // warp tiles per FP32 block
 // FP32 blocks per FP32 mid-level sum: 16 x 64 sources between FP64 adds (4 measured 1.2 %
@@ -379,6 +416,21 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
     const int64_t s0 = (int64_t)blockIdx.y * per_split;
     const int64_t s1 = min(s0 + per_split, ns_pad);
     const int ntiles = (int)((s1 - s0) / WT);
+#if VPM_UJ_BULK
+    // one mbarrier per buffer of the warp; tile it lands in buffer it & 1 on that barrier's
+    // phase it >> 1
+    __shared__ __align__(8) uint64_t tbar[UJ_WARPS][2];
+    if (lane == 0) {
+        mbar_init(&tbar[warp][0]);
+        mbar_init(&tbar[warp][1]);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncwarp();
+    bool bulk_ok = true;
+    int it_fail = 0;
+    if (ntiles > 0 && lane == 0)
+        bulk_g2s(&stage[warp][0][0], src + s0, WT * sizeof(SrcMixed), &tbar[warp][0]);
+#else
     const SrcMixed* wsrc = src + s0 + lane;
     if (ntiles > 0) {
         SrcMixed* d = &stage[warp][0][lane];
@@ -387,9 +439,24 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
         cp_async16(&d->gam, &wsrc->gam);
         cp_async_commit();
     }
+#endif
     int in_block = 0, in_mid = 0;
     for (int it = 0; it < ntiles; it++) {
         const int buf = it & 1;
+#if VPM_UJ_BULK
+        if (it + 1 < ntiles && lane == 0) {
+            // the lanes' reads of this buffer (ordered by the loop's last __syncwarp) before
+            // the async proxy overwrites it
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            bulk_g2s(&stage[warp][buf ^ 1][0], src + s0 + (int64_t)(it + 1) * WT, WT * sizeof(SrcMixed),
+                     &tbar[warp][buf ^ 1]);
+        }
+        if (!__all_sync(0xffffffffu, mbar_wait(&tbar[warp][buf], (uint32_t)(it >> 1) & 1u))) {
+            bulk_ok = false;
+            it_fail = it;
+            break;
+        }
+#else
         if (it + 1 < ntiles) {
             const SrcMixed* g = wsrc + (int64_t)(it + 1) * WT;
             SrcMixed* d = &stage[warp][buf ^ 1][lane];
@@ -401,6 +468,7 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
         } else {
             cp_async_wait<0>();
         }
+#endif
         __syncwarp();
 #if VPM_UJ_TILE_FLAGS
         bool far_src;
@@ -473,6 +541,19 @@ uj_mixed_kernel(int64_t nt, const TgtPos* __restrict__ tgt, int64_t ns_pad,
 #undef ACC_DU
 #undef ACC_DW
 #undef ACC_DJ
+#if VPM_UJ_BULK
+    if (!bulk_ok) {
+        // a tile that did not arrive: wait (bounded) for this warp's copies still in flight,
+        // then mark the warp's sums as failed
+        mbar_wait(&tbar[warp][it_fail & 1], (uint32_t)(it_fail >> 1) & 1u);
+        if (it_fail + 1 < ntiles) mbar_wait(&tbar[warp][(it_fail + 1) & 1], (uint32_t)((it_fail + 1) >> 1) & 1u);
+        const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+        for (int k = 0; k < 3; k++) { fU[k] = qnan; fW[k] = qnan; }
+#pragma unroll
+        for (int k = 0; k < 8; k++) fJ[k] = qnan;
+    }
+#endif
     if (!valid) return;
     // J = -3 J' (J'_33 = -J'_11 - J'_22) plus the Kronecker term of
     // src/FLOWVPM_fmm.jl:148-159 (W = sum aux2 Gamma)
