@@ -561,15 +561,14 @@ __device__ __forceinline__ void pair4_leaf(const float3& to, const float3& th, c
     }
 }
 
-constexpr int NF_BLK_PAIRS = 64;    // pairs per lane summed in FP32 before the mid-level sum
-constexpr int NF_MID_PAIRS = 256;   // pairs per lane summed in the mid-level FP32 sum before FP64
-
 template <int K>
 __global__ void __launch_bounds__(NF_THREADS, VPM_NF_MIN_BLOCKS)
 nf_uj_leaf(int64_t nleaves, const TgtPos* __restrict__ tgt, const int32_t* __restrict__ lb,
            const int32_t* __restrict__ le, const int32_t* __restrict__ row, const int32_t* __restrict__ col,
            const SrcMixed* __restrict__ src, double* U, double* J)
 {
+    constexpr int NF_BLK_PAIRS = 64;    // pairs per lane summed in FP32 before the mid-level sum
+    constexpr int NF_MID_PAIRS = 256;   // pairs per lane summed in the mid-level FP32 sum before FP64
     __shared__ SrcMixed tile[NF_WARPS][32];
     __shared__ float4 off[NF_WARPS][32];
     __shared__ double acc64[14][NF_THREADS];
