@@ -17,7 +17,7 @@ Static particles are not supported in this form (the host mirror has them).
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import torch
 

@@ -11,7 +11,7 @@ as is.  Row indices below are 0-based (the reference's minus one).
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

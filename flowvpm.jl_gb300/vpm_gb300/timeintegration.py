@@ -12,7 +12,7 @@ built with UJ=UJ_gb300.
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

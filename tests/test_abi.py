@@ -79,7 +79,6 @@ def test_context_creation_without_gpu_fails_cleanly(lib):
 
 
 def test_null_context_is_an_argument_error(lib):
-    import ctypes
     assert lib.vpm_uj(None, None, 46, 0, 2, 0, 1) == -1
     assert lib.vpm_ctx_create(None, 0) == -1
     assert lib.vpm_ctx_destroy(None) == 0

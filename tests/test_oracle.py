@@ -132,7 +132,6 @@ def test_oracle_ring_velocity_matches_reference_test():
     cVPM, Pedrizzetti every step, 50 steps over Rtot=2 radii; |err| < 2%."""
     import vpm_gb300.rings as rings
     from vpm_gb300.particlefield import ParticleField, cVPM, winckelmans
-    import vpm_gb300.timeintegration as ti
     R, Nphi, nc = 1.0, 100, 0
     Rcross = 0.15 * R
     pf = ParticleField(rings.number_particles(Nphi, nc), formulation=cVPM, kernel=winckelmans,

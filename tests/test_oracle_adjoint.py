@@ -1,7 +1,6 @@
 """The oracle's UJ adjoint (oracle_uj_adjoint) against central finite
 differences of the oracle's FP64 forward (CPU only).  This checks the per-pair
 derivative used by the GPU adjoint kernel: L = sum(Ubar*U) + sum(Jbar*J)."""
-import math
 
 import numpy as np
 import pytest

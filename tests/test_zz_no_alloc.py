@@ -9,8 +9,6 @@ Named test_zz_* so pytest collects it last.  It creates its own inputs and
 needs nothing from other test files, so it passes alone in a fresh process and
 after the rest of the suite.
 """
-import ctypes
-
 import numpy as np
 import pytest
 
