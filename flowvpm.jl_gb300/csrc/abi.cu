@@ -694,7 +694,7 @@ int vpm_uj(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, in
     RC(enter(c));
     if (!particles && np > 0) return fail(c, VPM_ERR_ARG, "vpm_uj: particles is NULL");
     if (ld != VPM_NFIELDS) return fail(c, VPM_ERR_ARG, "vpm_uj: ld must be %d (got %lld)", VPM_NFIELDS, (long long)ld);
-    if (np < 0 || np > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj: np=%lld out of range", (long long)np);
+    if (np < 0 || np > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "vpm_uj: np=%lld out of range", (long long)np);
     if (flags & ~(VPM_RESET | VPM_RESET_SFS | VPM_SFS | VPM_TRANSPOSED | VPM_CHECK_FINITE))
         return fail(c, VPM_ERR_ARG, "vpm_uj: unknown flag bits 0x%x", flags);
     RC(check_kernel(c, kernel, precision));
@@ -714,7 +714,7 @@ int vpm_uj_cross(vpm_ctx* c, const double* src, int64_t ld_src, int64_t ns, doub
     if ((!src && ns > 0) || (!tgt && nt > 0)) return fail(c, VPM_ERR_ARG, "vpm_uj_cross: NULL matrix");
     if (ld_src != VPM_NFIELDS || ld_tgt != VPM_NFIELDS)
         return fail(c, VPM_ERR_ARG, "vpm_uj_cross: ld must be %d", VPM_NFIELDS);
-    if (ns < 0 || nt < 0 || ns > (int64_t)1 << 31 || nt > (int64_t)1 << 31)
+    if (ns < 0 || nt < 0 || ns > (int64_t)INT32_MAX || nt > (int64_t)INT32_MAX)
         return fail(c, VPM_ERR_ARG, "vpm_uj_cross: sizes out of range");
     RC(check_kernel(c, kernel, precision));
     if (ns == 0 || nt == 0) return VPM_OK;
@@ -759,7 +759,7 @@ int vpm_uj_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const doubl
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+    if (nt < 0 || ns < 0 || nt > (int64_t)INT32_MAX || ns > (int64_t)INT32_MAX)
         return fail(c, VPM_ERR_ARG, "vpm_uj_dev: sizes out of range");
     RC(check_kernel(c, kernel, precision));
     if (nt == 0 || ns == 0) return VPM_OK;
@@ -785,7 +785,7 @@ int vpm_estr_dev(vpm_ctx* c, int64_t nt, const double* xt, const double* Jt, con
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_estr_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+    if (nt < 0 || ns < 0 || nt > (int64_t)INT32_MAX || ns > (int64_t)INT32_MAX)
         return fail(c, VPM_ERR_ARG, "vpm_estr_dev: sizes out of range");
     if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "vpm_estr_dev: only VPM_TRANSPOSED is accepted in flags");
     RC(check_kernel(c, kernel, precision));
@@ -815,7 +815,7 @@ int vpm_zeta_dev(vpm_ctx* c, int64_t nt, const double* xt, int64_t ns, const dou
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_zeta_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+    if (nt < 0 || ns < 0 || nt > (int64_t)INT32_MAX || ns > (int64_t)INT32_MAX)
         return fail(c, VPM_ERR_ARG, "vpm_zeta_dev: sizes out of range");
     RC(check_kernel(c, kernel, precision));
     if (nt == 0 || ns == 0) return VPM_OK;
@@ -841,7 +841,7 @@ int vpm_zeta(vpm_ctx* c, double* particles, int64_t ld, int64_t np, int kernel, 
     RC(enter(c));
     if (!particles && np > 0) return fail(c, VPM_ERR_ARG, "vpm_zeta: particles is NULL");
     if (ld != VPM_NFIELDS) return fail(c, VPM_ERR_ARG, "vpm_zeta: ld must be %d (got %lld)", VPM_NFIELDS, (long long)ld);
-    if (np < 0 || np > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_zeta: np=%lld out of range", (long long)np);
+    if (np < 0 || np > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "vpm_zeta: np=%lld out of range", (long long)np);
     RC(check_kernel(c, kernel, precision));
     if (np == 0) return VPM_OK;
     DeviceGuard dg(c->device);
@@ -886,7 +886,7 @@ int vpm_dynamic_diff_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     if (!(alpha > 0.0 && alpha < 1.0)) return fail(c, VPM_ERR_ARG, "%s: alpha must be in (0, 1)", fn);
     if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
     RC(check_kernel(c, kernel, precision));
@@ -1028,7 +1028,7 @@ int vpm_rk3_stage_dev(vpm_ctx* c, int64_t n, double a, double b, double dt, cons
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
     if (!Uinf) return fail(c, VPM_ERR_ARG, "%s: Uinf is NULL", fn);
     if (!(std::isfinite(a) && std::isfinite(b) && std::isfinite(dt) && std::isfinite(f) && std::isfinite(g) &&
@@ -1055,7 +1055,7 @@ int vpm_relax_dev(vpm_ctx* c, int64_t n, double rlxf, const double* J, double* g
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     if (!std::isfinite(rlxf)) return fail(c, VPM_ERR_ARG, "%s: bad rlxf", fn);
     if (n == 0) return VPM_OK;
     DeviceGuard dg(c->device);
@@ -1073,7 +1073,7 @@ int vpm_dynamic_after_dev(vpm_ctx* c, int64_t n, double alpha, double rlxf, doub
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     if (flags & ~(VPM_TRANSPOSED | VPM_DYN_FORCE_POSITIVE | VPM_DYN_CLIP_BACKSCATTER | VPM_DYN_SUBTRACT))
         return fail(c, VPM_ERR_ARG, "%s: unknown flags", fn);
     if (!(std::isfinite(alpha) && std::isfinite(rlxf) && !std::isnan(minC) && !std::isnan(maxC) &&
@@ -1238,7 +1238,7 @@ int vpm_p2p_lists_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam,
     if (row[0] != 0) return fail(c, VPM_ERR_ARG, "%s: row[0] must be 0", fn);
     for (int64_t l = 0; l < nl; l++)
         if (row[l + 1] < row[l]) return fail(c, VPM_ERR_ARG, "%s: row is not monotone", fn);
-    if (row[nl] > (int64_t)INT32_MAX) return fail(c, VPM_ERR_CAPACITY, "%s: more than 2^31 leaf pairs", fn);
+    if (row[nl] > (int64_t)INT32_MAX) return fail(c, VPM_ERR_CAPACITY, "%s: 2^31 or more leaf pairs", fn);
     if (row[nl] > 0 && !col) return fail(c, VPM_ERR_ARG, "%s: col is NULL", fn);
     std::vector<int32_t> cs(col, col + row[nl]);
     for (int64_t l = 0; l < nl; l++) {
@@ -1324,7 +1324,7 @@ int vpm_uj_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* gam
     if (!c) return fail(nullptr, VPM_ERR_ARG, "vpm_uj_adjoint_dev: ctx is NULL");
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: n out of range");
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: n out of range");
     RC(check_kernel(c, kernel, precision));
     if (precision == VPM_FP32COMP && kernel == VPM_KERNEL_GAUSSIAN)
         return fail(c, VPM_ERR_ARG, "vpm_uj_adjoint_dev: the FP32-comp adjoint covers the singular, Gaussian-erf "
@@ -1352,7 +1352,7 @@ int vpm_estr_adjoint_dev(vpm_ctx* c, int64_t n, const double* x, const double* g
     if (!c) return fail(nullptr, VPM_ERR_ARG, "%s: ctx is NULL", fn);
     std::lock_guard<std::mutex> lk(c->mu);
     RC(enter(c));
-    if (n < 0 || n > (int64_t)1 << 31) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(c, VPM_ERR_ARG, "%s: n out of range", fn);
     if (flags & ~VPM_TRANSPOSED) return fail(c, VPM_ERR_ARG, "%s: only VPM_TRANSPOSED is accepted in flags", fn);
     RC(check_kernel(c, kernel, precision));
     if (n == 0) return VPM_OK;

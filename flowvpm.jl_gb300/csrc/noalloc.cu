@@ -90,7 +90,7 @@ int vpm_uj_dev_noalloc(int64_t nt, const double* xt, int64_t ns, const double* x
                        const double* sgs, double* U, double* J, int kernel, int precision, void* stream)
 {
     vpm::TraceRange trace_("vpm_uj_dev_noalloc");
-    if (nt < 0 || ns < 0 || nt > (int64_t)1 << 31 || ns > (int64_t)1 << 31)
+    if (nt < 0 || ns < 0 || nt > (int64_t)INT32_MAX || ns > (int64_t)INT32_MAX)
         return nerr(VPM_ERR_ARG, "vpm_uj_dev_noalloc: sizes out of range");
     if (kernel < VPM_KERNEL_SINGULAR || kernel > VPM_KERNEL_WINCKELMANS)
         return nerr(VPM_ERR_ARG, "vpm_uj_dev_noalloc: unknown kernel id %d", kernel);
